@@ -1,0 +1,339 @@
+"""Generate the golden vectors in tests/golden/ by running the reference itself.
+
+Run in a container that has the reference sources (qandle 0.1.8, pure Python
+on torch):
+
+    python tests/golden/make_golden.py --reference /path/to/qandle/src
+
+qandle imports the third-party ``qw_map`` package (qw-map 0.1.2), which is not
+installed here; every parity case uses ``remapping=None``, which qandle maps
+to ``qw_map.none`` (the identity, operators.py:168-170), so a stand-in module
+with ``none`` = identity is placed on the path.  Its ``tanh`` raises, so a case
+that would silently use the unpinned default mapping fails instead.
+
+The cases follow the reference's own tests with the reference in PennyLane's
+place (PennyLane is not installed): per-gate sweeps
+(test/test_operators.py:85-128, :157-203), re-uploading (:131-154),
+embeddings (test/test_embeddings.py:56-153), measurements
+(test/test_measurements.py:6-48), strongly entangling layers
+(test/test_ansaetze.py:6-83), plus small instances of the four measured
+circuit families and torch-autograd gradients through the reference.
+
+Output: one compressed .npz per group, arrays only (no pickles).  Circuit
+descriptions are stored as JSON strings next to their arrays.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from qandle_gb300 import workloads  # noqa: E402
+
+QW_STUB = '''
+def none(x):
+    return x
+
+
+def tanh(x):
+    raise RuntimeError("qw_map.tanh is not pinned for parity; use remapping=None")
+'''
+
+
+def import_reference(src: str):
+    stub = tempfile.mkdtemp(prefix="qwstub")
+    os.makedirs(os.path.join(stub, "qw_map"))
+    with open(os.path.join(stub, "qw_map", "__init__.py"), "w") as f:
+        f.write(QW_STUB)
+    sys.path.insert(0, stub)
+    sys.path.insert(0, src)
+    import qandle  # noqa: F401
+
+    return qandle
+
+
+def desc_json(desc: dict) -> str:
+    gates = []
+    for g in desc["gates"]:
+        if g[0] == "u":
+            m = np.asarray(g[2], dtype=np.complex64)
+            gates.append(["u", g[1], [[float(v.real), float(v.imag)] for v in m.reshape(-1)]])
+        else:
+            gates.append(list(g))
+    d = {k: v for k, v in desc.items() if k not in ("gates", "inputs", "targets")}
+    d["gates"] = gates
+    d["input_names"] = sorted(desc.get("inputs", {}).keys())
+    return json.dumps(d)
+
+
+def to_reference(qandle, desc: dict, thetas_require_grad: bool = False):
+    layers, params = [], []
+    for g in desc["gates"]:
+        k = g[0]
+        if k == "emb":
+            layers.append(qandle.AngleEmbedding(name=g[2], qubits=list(g[3]), rotation=g[1]))
+        elif k in ("rx", "ry", "rz"):
+            cls = {"rx": qandle.RX, "ry": qandle.RY, "rz": qandle.RZ}[k]
+            if g[3] is None:
+                th = torch.tensor(np.float32(g[2]), dtype=torch.float, requires_grad=True)
+                params.append(th)
+                layers.append(cls(qubit=g[1], theta=th, remapping=None))
+            else:
+                layers.append(cls(qubit=g[1], name=g[3], remapping=None))
+        elif k == "u":
+            layers.append(qandle.U(qubit=g[1], matrix=torch.tensor(np.asarray(g[2], np.complex64))))
+        elif k == "cnot":
+            layers.append(qandle.CNOT(control=g[1], target=g[2]))
+        elif k == "cz":
+            layers.append(qandle.CZ(control=g[1], target=g[2]))
+        elif k == "swap":
+            layers.append(qandle.SWAP(a=g[1], b=g[2]))
+    m = desc.get("measure")
+    if m == "probs":
+        layers.append(qandle.MeasureJointProbability())
+    elif m in ("p0", "z"):
+        layers.append(qandle.MeasureProbability())
+    circ = qandle.Circuit(layers, num_qubits=desc["n"])
+    return circ
+
+
+def ref_thetas(qandle, circ):
+    """Theta parameters of the built reference circuit in gate order."""
+    out = []
+    for mod in circ.circuit.layers:
+        if isinstance(mod, qandle.operators.BuiltParametrizedOperator) and not mod.named:
+            out.append(mod.theta)
+    return out
+
+
+def kwargs_of(desc: dict, requires_grad: bool = False):
+    kw = {}
+    for k, v in desc.get("inputs", {}).items():
+        t = torch.tensor(np.asarray(v, dtype=np.float32))
+        kw[k] = t
+    return kw
+
+
+def gate_cases(qandle):
+    """Per-gate sweeps, as test_operators.py:85-128 (unbatched, theta=0.543321)
+    and :157-203 (batch 13, theta=-2.3456), plus U with non-symmetric
+    matrices so the row-vector convention is pinned."""
+    out = {}
+    idx = 0
+    for batched, v in ((False, 0.543321), (True, -2.3456)):
+        torch.manual_seed(42)
+        for n in range(1, 6):
+            inp = torch.rand(13, 2 ** n, dtype=torch.cfloat) if batched else \
+                torch.rand(2 ** n, dtype=torch.cfloat)
+            inp = inp / torch.linalg.norm(inp, dim=-1, keepdim=True)
+            for w in range(n):
+                specs = [("rx", w), ("ry", w), ("rz", w)]
+                specs += [(k, w, w2) for w2 in range(n) if w2 != w for k in ("cnot", "cz", "swap")]
+                for sp in specs:
+                    if sp[0] in ("rx", "ry", "rz"):
+                        cls = {"rx": qandle.RX, "ry": qandle.RY, "rz": qandle.RZ}[sp[0]]
+                        op = cls(qubit=w, theta=v, remapping=None).build(num_qubits=n)
+                        gate = [sp[0], w, float(np.float32(v)), None]
+                    else:
+                        cls = {"cnot": qandle.CNOT, "cz": qandle.CZ, "swap": qandle.SWAP}[sp[0]]
+                        op = (cls(sp[1], sp[2]) if sp[0] != "swap" else cls(a=sp[1], b=sp[2]))
+                        op = op.build(num_qubits=n)
+                        gate = list(sp)
+                    res = op(inp).detach()
+                    out[f"g{idx}_in"] = inp.numpy()
+                    out[f"g{idx}_out"] = res.numpy()
+                    out[f"g{idx}_desc"] = np.array(json.dumps({"n": n, "gate": gate}))
+                    idx += 1
+    # U with random non-symmetric complex matrices (U is not unitary-checked
+    # by the reference; use unitary ones anyway)
+    gen = torch.Generator().manual_seed(7)
+    for n in range(1, 5):
+        inp = torch.rand(5, 2 ** n, dtype=torch.cfloat, generator=gen)
+        inp = inp / torch.linalg.norm(inp, dim=-1, keepdim=True)
+        for w in range(n):
+            a, b, c = (torch.rand(3, generator=gen) * 2 * np.pi).tolist()
+            m = workloads.u3_row_matrix(a, b, c)
+            op = qandle.U(qubit=w, matrix=torch.tensor(m)).build(num_qubits=n)
+            res = op(inp).detach()
+            out[f"g{idx}_in"] = inp.numpy()
+            out[f"g{idx}_out"] = res.numpy()
+            g = ["u", w, [[float(z.real), float(z.imag)] for z in m.reshape(-1)]]
+            out[f"g{idx}_desc"] = np.array(json.dumps({"n": n, "gate": g}))
+            idx += 1
+    out["count"] = np.array(idx)
+    return out
+
+
+def embedding_cases(qandle):
+    """test_embeddings.py:56-153 (x3, y4, z5, each unbatched and batched),
+    plus a qubit subset and a repeated qubit."""
+    out = {}
+    torch.manual_seed(42)
+    cases = [
+        ("rx", 3, None, torch.arange(3).float() + 0.5),
+        ("rx", 3, None, torch.rand(10, 3) + 0.5),
+        ("ry", 4, None, torch.arange(4).float() + 2.5),
+        ("ry", 4, None, torch.rand(10, 4) + 2.5),
+        ("rz", 5, None, torch.arange(5).float() + 2.5),
+        ("rz", 5, None, torch.rand(10, 5) + 2.5),
+        ("rx", 4, [1, 3], torch.rand(6, 2) * 3.0),
+        ("ry", 3, [0, 0, 2], torch.rand(6, 3) * 3.0),
+    ]
+    for i, (rot, n, qubits, x) in enumerate(cases):
+        qs = list(range(n)) if qubits is None else qubits
+        emb = qandle.AngleEmbedding(qubits=qs, rotation=rot, name="e").build(num_qubits=n)
+        res = emb(e=x).detach()
+        out[f"e{i}_x"] = x.numpy()
+        out[f"e{i}_out"] = res.numpy()
+        out[f"e{i}_desc"] = np.array(json.dumps({"n": n, "rot": rot, "qubits": qs}))
+    out["count"] = np.array(len(cases))
+    return out
+
+
+def measurement_cases(qandle):
+    """test_measurements.py:6-48 plus the squeeze quirks of
+    measurements.py:120-123 (batch 1 and one qubit)."""
+    out = {}
+    torch.manual_seed(3)
+    shapes = [(None, 3), (17, 3), (1, 3), (5, 1), (None, 1), (4, 6)]
+    for i, (b, n) in enumerate(shapes):
+        inp = torch.rand(2 ** n, dtype=torch.cfloat) if b is None else \
+            torch.rand(b, 2 ** n, dtype=torch.cfloat)
+        inp = inp / torch.linalg.norm(inp, dim=-1, keepdim=True)
+        p0 = qandle.MeasureProbabilityBuilt(num_qubits=n)(inp).detach()
+        pj = qandle.MeasureJointProbability()(inp).detach()
+        out[f"m{i}_in"] = inp.numpy()
+        out[f"m{i}_p0"] = p0.numpy()
+        out[f"m{i}_joint"] = pj.numpy()
+    out["count"] = np.array(len(shapes))
+    return out
+
+
+def sel_cases(qandle):
+    """test_ansaetze.py:6-26 and :63-83 (remapping=None)."""
+    out = {}
+    torch.manual_seed(11)
+    for i, (n, depth, batch) in enumerate(((4, 10, None), (5, 7, 17), (6, 3, 4))):
+        inp = torch.rand(2 ** n, dtype=torch.cfloat) if batch is None else \
+            torch.rand(batch, 2 ** n, dtype=torch.cfloat)
+        inp = inp / torch.linalg.norm(inp, dim=-1, keepdim=True)
+        w = torch.rand(depth, n, 3)
+        sel = qandle.StronglyEntanglingLayer(qubits=list(range(n)), depth=depth, q_params=w,
+                                             remapping=None).build(num_qubits=n)
+        res = sel(inp).detach()
+        out[f"s{i}_in"] = inp.numpy()
+        out[f"s{i}_w"] = w.numpy()
+        out[f"s{i}_out"] = res.numpy()
+        out[f"s{i}_desc"] = np.array(json.dumps({"n": n, "depth": depth}))
+    out["count"] = np.array(3)
+    return out
+
+
+def reupload_cases(qandle):
+    """test_operators.py:131-154: a named RX equals the fixed-theta RX,
+    unbatched, batched with a scalar input and with a [7] input."""
+    q = 3
+    v = torch.tensor(0.123)
+    torch.manual_seed(42)
+    c2 = qandle.Circuit(layers=[qandle.RX(qubit=1, name="reupload", remapping=None)],
+                        num_qubits=q)
+    inp_u = torch.rand(2 ** q, dtype=torch.cfloat)
+    inp_u = inp_u / torch.linalg.norm(inp_u)
+    inp_b = torch.rand(7, 2 ** q, dtype=torch.cfloat)
+    inp_b = inp_b / torch.linalg.norm(inp_b, dim=-1, keepdim=True)
+    vb = torch.rand(7) * 3.0
+    return {
+        "inp_u": inp_u.numpy(), "inp_b": inp_b.numpy(), "v": v.numpy(), "vb": vb.numpy(),
+        "unb": c2(inp_u, reupload=v).detach().numpy(),
+        "bat_scalar": c2(inp_b, reupload=v).detach().numpy(),
+        "bat_vec": c2(inp_b, reupload=vb).detach().numpy(),
+        "unb_vec": c2(inp_u, reupload=vb).detach().numpy(),
+    }
+
+
+def circuit_cases(qandle):
+    """Small instances of the four measured families through qandle.Circuit,
+    and torch-autograd gradients through the reference."""
+    out = {}
+    descs = {
+        "plain_small": workloads.plain_small(),  # full size: 8 qubits, batch 64
+        "sel_small": workloads.sel_reupload(n=6, batch=8, layers=4, reupload_every=2,
+                                            measure="p0"),
+        "brick_small": workloads.adjoint_brick(n=6, batch=8, layers=4),
+        "deep_small": workloads.deep_u(n=6, batch=2, layers=6),
+    }
+    for name, desc in descs.items():
+        circ = to_reference(qandle, desc)
+        kw = kwargs_of(desc)
+        if name == "deep_small":
+            res = circ(torch.zeros(2, 2 ** 6, dtype=torch.cfloat).index_fill_(1, torch.tensor([0]), 1.0))
+        else:
+            res = circ(**kw) if kw else circ()
+        out[f"{name}_desc"] = np.array(desc_json(desc))
+        for k, v in desc.get("inputs", {}).items():
+            out[f"{name}_in_{k}"] = np.asarray(v)
+        out[f"{name}_out"] = res.detach().numpy()
+    # gradients: brick_small with MSE(<Z>, targets), <Z> = 2 P0 - 1
+    desc = descs["brick_small"]
+    circ = to_reference(qandle, desc)
+    circ.circuit.state = circ.circuit.state.expand(desc["batch"], -1).contiguous()
+    p0 = circ()
+    z = 2.0 * p0 - 1.0
+    t = torch.tensor(desc["targets"])
+    loss = ((z - t) ** 2).mean()
+    loss.backward()
+    ths = ref_thetas(qandle, circ)
+    out["brick_small_targets"] = desc["targets"]
+    out["brick_small_loss"] = np.array(loss.item())
+    out["brick_small_dtheta"] = np.array([th.grad.item() for th in ths], dtype=np.float32)
+    # gradients wrt the embedding inputs and shared thetas: sel_small, loss = sum(P0 * w)
+    desc = descs["sel_small"]
+    circ = to_reference(qandle, desc)
+    kw = {k: v.clone().requires_grad_(True) for k, v in kwargs_of(desc).items()}
+    # the re-uploads read columns of x; keep them tied to x for the gradient
+    x = kw["x"]
+    for q in range(desc["n"]):
+        kw[f"up{q}"] = x[:, q]
+    p0 = circ(**kw)
+    wts = torch.linspace(-1.0, 1.0, p0.numel()).reshape(p0.shape)
+    (p0 * wts).sum().backward()
+    ths = ref_thetas(qandle, circ)
+    out["sel_small_weights"] = wts.numpy()
+    out["sel_small_dtheta"] = np.array([th.grad.item() for th in ths], dtype=np.float32)
+    out["sel_small_dx"] = x.grad.numpy()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=os.environ.get("QANDLE_REFERENCE_SRC", ""))
+    args = ap.parse_args()
+    if not args.reference:
+        sys.exit("pass --reference <path to the qandle src directory>")
+    qandle = import_reference(args.reference)
+    torch.set_num_threads(max(1, os.cpu_count() or 1))
+    groups = {
+        "gates": gate_cases,
+        "embeddings": embedding_cases,
+        "measurements": measurement_cases,
+        "sel": sel_cases,
+        "reupload": reupload_cases,
+        "circuits": circuit_cases,
+    }
+    for name, fn in groups.items():
+        arrays = fn(qandle)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **arrays)
+        print(f"wrote {path} ({os.path.getsize(path)} bytes)")
+
+
+if __name__ == "__main__":
+    main()
