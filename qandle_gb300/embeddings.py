@@ -1,0 +1,84 @@
+"""AngleEmbedding (mirrors qandle/embeddings.py:114-214).
+
+The reference forms the per-sample product of n dense 2^n x 2^n rotation
+matrices and applies it to |0..0>.  The product of rotations on distinct
+qubits is the product state prod_q R_q(x_q)|0>, which the CUDA kernel writes
+directly (8 bytes per amplitude, no matmuls).
+"""
+from __future__ import annotations
+
+import typing
+
+import torch
+
+from . import operators as op
+from . import plain
+
+__all__ = ["AngleEmbedding", "AngleEmbeddingBuilt", "InputOperator", "InputOperatorBuilt"]
+
+_ROT = {"x": 0, "y": 1, "z": 2}
+
+
+def parse_rot(rot: str) -> int:
+    """Axis index of 'rx'/'x'/'ry'/... (utils.parse_rot, qandle/utils.py:26-37)."""
+    r = rot.lower().replace("r", "")
+    if r not in _ROT:
+        raise ValueError(f"Unknown rotation {rot}")
+    return _ROT[r]
+
+
+class InputOperator(op.UnbuiltOperator):
+    ...
+
+
+class InputOperatorBuilt(op.BuiltOperator):
+    def decompose(self):
+        raise NotImplementedError(f"Decomposing {self.__class__} is not yet supported")
+
+    def to_matrix(self):
+        raise ValueError("Input operators do not have a matrix representation")
+
+
+class AngleEmbeddingBuilt(InputOperatorBuilt):
+    """Ignores the incoming state and writes the embedded product state."""
+
+    def __init__(self, name: str, num_qubits: int, qubits: typing.List[int], rotation: str):
+        super().__init__()
+        self.num_qubits = num_qubits
+        self.qubits = list(qubits)
+        self.named = True
+        self.name = name
+        self.rotation = rotation
+        self.axis = parse_rot(rotation)
+        for q in self.qubits:
+            if not 0 <= q < num_qubits:
+                raise ValueError(f"embedded qubit {q} out of range for {num_qubits} qubits")
+
+    def forward(self, state=None, **kwargs):
+        inp = torch.as_tensor(kwargs[self.name])
+        out = plain.AngleEmbed.apply(inp, self.num_qubits, self.qubits, self.axis)
+        if inp.dim() == 1:
+            return out.reshape(1 << self.num_qubits)
+        return out.reshape(*inp.shape[:-1], 1 << self.num_qubits)
+
+    def __str__(self) -> str:
+        return f"AngleEmbedding_{self.rotation}"
+
+
+class AngleEmbedding(InputOperator):
+    """Angle embedding of named inputs (embeddings.py:184-214)."""
+
+    def __init__(self, name: str, qubits: typing.Union[typing.List[int], None] = None,
+                 rotation="rx"):
+        self.name = name
+        self.named = True
+        self.qubits = qubits
+        self.rotation = rotation
+
+    def build(self, num_qubits: int, **kwargs) -> AngleEmbeddingBuilt:
+        qubits = list(range(num_qubits)) if self.qubits is None else self.qubits
+        return AngleEmbeddingBuilt(name=self.name, qubits=qubits, num_qubits=num_qubits,
+                                   rotation=self.rotation)
+
+    def __str__(self) -> str:
+        return f"AngleEmbedding_{self.rotation}"

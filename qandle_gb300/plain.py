@@ -1,0 +1,207 @@
+"""Plain form: torch autograd Functions over the per-gate CUDA kernels.
+
+Each Function clones its input (the reference's layers are out-of-place,
+``state @ M``) and runs one in-place kernel pass on the clone.  Backward runs
+the adjoint of the same kernel on the incoming gradient, plus a reduction
+kernel for the angle gradient.  torch's complex gradient convention is used
+throughout: grad = 2 dL/dz*.
+
+States are viewed as [B, 2^n]; an unbatched [2^n] state is B = 1.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+
+AXES = {"x": 0, "y": 1, "z": 2, "rx": 0, "ry": 1, "rz": 2}
+
+
+def _as_batched(state: torch.Tensor, n: int) -> torch.Tensor:
+    _lib.require_cuda_state(state)
+    if state.shape[-1] != (1 << n):
+        raise ValueError(f"state has {state.shape[-1]} amplitudes, expected 2^{n}")
+    return state.reshape(-1, 1 << n).contiguous()
+
+
+def _scratch(nbytes: int, device) -> torch.Tensor:
+    return torch.empty(max(int(nbytes), 16), dtype=torch.uint8, device=device)
+
+
+class Rotation(torch.autograd.Function):
+    """RX/RY/RZ by ``angle`` (float32; one value, or one per sample)."""
+
+    @staticmethod
+    def forward(ctx, state, angle, n, qubit, axis):
+        st = _as_batched(state, n)
+        B = st.shape[0]
+        a = angle.to(device=st.device, dtype=torch.float32).reshape(-1).contiguous()
+        per_sample = a.numel() > 1
+        if per_sample and B == 1:
+            st = st.expand(a.numel(), -1)
+            B = a.numel()
+        if per_sample and a.numel() != B:
+            raise ValueError(f"named input has {a.numel()} values for a batch of {B}")
+        out = st.clone()
+        _lib.call("qg_apply_rotation", out.data_ptr(), B, n, qubit, axis, a.data_ptr(),
+                  1 if per_sample else 0, 0, _lib.stream())
+        ctx.save_for_backward(out, a)
+        ctx.meta = (n, qubit, axis, per_sample, angle.shape, state.shape, B)
+        if state.dim() == 1 and not per_sample:
+            return out.reshape(state.shape)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        out, a = ctx.saved_tensors
+        n, qubit, axis, per_sample, ashape, sshape, B = ctx.meta
+        g = g.reshape(B, 1 << n).contiguous()
+        gin = dth = None
+        if ctx.needs_input_grad[0]:
+            gin = g.clone()
+            _lib.call("qg_apply_rotation", gin.data_ptr(), B, n, qubit, axis, a.data_ptr(),
+                      1 if per_sample else 0, 1, _lib.stream())
+            orig_b = 1 if len(sshape) == 1 else sshape[0]
+            if orig_b != B:  # the state was broadcast over per-sample angles
+                gin = gin.sum(0, keepdim=True)
+            gin = gin.reshape(sshape)
+        if ctx.needs_input_grad[1]:
+            scr = _scratch(_lib.load().qg_rotation_grad_scratch_bytes(B, n), g.device)
+            dth = torch.empty(B if per_sample else 1, dtype=torch.float32, device=g.device)
+            _lib.call("qg_rotation_grad", out.data_ptr(), g.data_ptr(), dth.data_ptr(), B, n, qubit,
+                      axis, 1 if per_sample else 0, scr.data_ptr(), scr.numel(), _lib.stream())
+            dth = dth.reshape(ashape)
+        return gin, dth, None, None, None
+
+
+class Matrix(torch.autograd.Function):
+    """Fixed 2x2 ``row_matrix`` applied as state @ kron(.., M, ..)."""
+
+    @staticmethod
+    def forward(ctx, state, row_matrix, n, qubit):
+        st = _as_batched(state, n)
+        m = row_matrix.to(device=st.device, dtype=torch.complex64).contiguous()
+        out = st.clone()
+        _lib.call("qg_apply_matrix", out.data_ptr(), st.shape[0], n, qubit, m.data_ptr(), 0,
+                  _lib.stream())
+        ctx.save_for_backward(m)
+        ctx.meta = (n, qubit, state.shape)
+        return out.reshape(state.shape)
+
+    @staticmethod
+    def backward(ctx, g):
+        (m,) = ctx.saved_tensors
+        n, qubit, sshape = ctx.meta
+        gin = g.reshape(-1, 1 << n).contiguous().clone()
+        _lib.call("qg_apply_matrix", gin.data_ptr(), gin.shape[0], n, qubit, m.data_ptr(), 1,
+                  _lib.stream())
+        return gin.reshape(sshape), None, None, None
+
+
+_PERM = {"cnot": "qg_apply_cnot", "cz": "qg_apply_cz", "swap": "qg_apply_swap"}
+
+
+class Permutation(torch.autograd.Function):
+    """CNOT / CZ / SWAP: exact amplitude moves and sign flips (involutions,
+    so the backward applies the same kernel)."""
+
+    @staticmethod
+    def forward(ctx, state, n, kind, qa, qb):
+        st = _as_batched(state, n)
+        out = st.clone()
+        if not (kind == "swap" and qa == qb):
+            _lib.call(_PERM[kind], out.data_ptr(), st.shape[0], n, qa, qb, _lib.stream())
+        ctx.meta = (n, kind, qa, qb, state.shape)
+        return out.reshape(state.shape)
+
+    @staticmethod
+    def backward(ctx, g):
+        n, kind, qa, qb, sshape = ctx.meta
+        gin = g.reshape(-1, 1 << n).contiguous().clone()
+        if not (kind == "swap" and qa == qb):
+            _lib.call(_PERM[kind], gin.data_ptr(), gin.shape[0], n, qa, qb, _lib.stream())
+        return gin.reshape(sshape), None, None, None, None
+
+
+class AngleEmbed(torch.autograd.Function):
+    """Product state prod_j R(x_j) on qubits[j] |0..0>; x: [B, k]."""
+
+    @staticmethod
+    def forward(ctx, x, n, qubits, axis):
+        if not x.is_cuda:
+            raise RuntimeError("qandle_gb300 runs on CUDA tensors only; the embedding input is on "
+                               f"{x.device}")
+        xb = x.to(torch.float32).reshape(-1, len(qubits)).contiguous()
+        B = xb.shape[0]
+        out = torch.empty(B, 1 << n, dtype=torch.complex64, device=x.device)
+        scr = _scratch(_lib.load().qg_angle_embedding_scratch_bytes(B, n), x.device)
+        qarr = (_lib.c_int * max(1, len(qubits)))(*qubits)
+        _lib.call("qg_angle_embedding", out.data_ptr(), xb.data_ptr(), len(qubits), B, n, qarr,
+                  len(qubits), axis, scr.data_ptr(), scr.numel(), _lib.stream())
+        ctx.save_for_backward(out)
+        ctx.meta = (n, tuple(qubits), axis, x.shape, B)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        (out,) = ctx.saved_tensors
+        n, qubits, axis, xshape, B = ctx.meta
+        if not ctx.needs_input_grad[0]:
+            return None, None, None, None
+        g = g.reshape(B, 1 << n).contiguous()
+        dx = torch.empty(B, len(qubits), dtype=torch.float32, device=g.device)
+        scr = _scratch(_lib.load().qg_rotation_grad_scratch_bytes(B, n), g.device)
+        col = torch.empty(B, dtype=torch.float32, device=g.device)
+        for j, q in enumerate(qubits):
+            _lib.call("qg_rotation_grad", out.data_ptr(), g.data_ptr(), col.data_ptr(), B, n, q,
+                      axis, 1, scr.data_ptr(), scr.numel(), _lib.stream())
+            dx[:, j] = col
+        return dx.reshape(xshape), None, None, None
+
+
+class MeasureP0(torch.autograd.Function):
+    """P(qubit q = 0) -> [B, n] float32."""
+
+    @staticmethod
+    def forward(ctx, state, n):
+        st = _as_batched(state, n)
+        B = st.shape[0]
+        out = torch.empty(B, n, dtype=torch.float32, device=st.device)
+        scr = _scratch(_lib.load().qg_measure_p0_scratch_bytes(B, n), st.device)
+        _lib.call("qg_measure_p0", st.data_ptr(), out.data_ptr(), B, n, scr.data_ptr(), scr.numel(),
+                  _lib.stream())
+        ctx.save_for_backward(st)
+        ctx.meta = (n, state.shape)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        (st,) = ctx.saved_tensors
+        n, sshape = ctx.meta
+        g = g.to(torch.float32).contiguous()
+        gin = torch.empty_like(st)
+        _lib.call("qg_measure_p0_backward", st.data_ptr(), g.data_ptr(), gin.data_ptr(),
+                  st.shape[0], n, _lib.stream())
+        return gin.reshape(sshape), None
+
+
+class Probs(torch.autograd.Function):
+    """|psi|^2, same shape as the state, float32."""
+
+    @staticmethod
+    def forward(ctx, state):
+        _lib.require_cuda_state(state)
+        st = state.contiguous()
+        out = torch.empty(st.shape, dtype=torch.float32, device=st.device)
+        _lib.call("qg_probs", st.data_ptr(), out.data_ptr(), st.numel(), _lib.stream())
+        ctx.save_for_backward(st)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        (st,) = ctx.saved_tensors
+        g = g.to(torch.float32).contiguous()
+        gin = torch.empty_like(st)
+        _lib.call("qg_probs_backward", st.data_ptr(), g.data_ptr(), gin.data_ptr(), st.numel(),
+                  _lib.stream())
+        return gin

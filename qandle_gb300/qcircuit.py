@@ -1,0 +1,147 @@
+"""Circuit front end (mirrors qandle/qcircuit.py:13-212).
+
+``Circuit(layers, num_qubits=None, ...)`` builds its layers exactly like the
+reference and runs them on one of two executors:
+
+* ``engine="fused"`` (default): the circuit is lowered once to a gate
+  program and run by the fused CUDA engine (qandle_gb300.engine) -- gate
+  fusion into shared-memory passes, one graph replay per call, adjoint
+  backward.
+* ``engine="plain"``: the reference's per-layer loop
+  (UnsplittedCircuit.forward, qcircuit.py:163-174) with one CUDA kernel pass
+  per gate (qandle_gb300.plain).
+
+Both return what the reference returns for the same layers and inputs.
+"""
+from __future__ import annotations
+
+import typing
+import warnings
+
+import torch
+
+from . import operators
+from . import measurements
+
+__all__ = ["Circuit", "UnsplittedCircuit"]
+
+
+class Circuit(torch.nn.Module):
+    def __init__(self, layers: typing.List[operators.Operator], num_qubits=None,
+                 split_max_qubits=0, circuit=None, engine: str = "fused", **engine_options):
+        super().__init__()
+        self.name = ""
+        self.named = True
+        if not hasattr(layers, "__iter__"):
+            layers = [layers]
+        if num_qubits is not None:
+            self.num_qubits = num_qubits
+        else:
+            self.num_qubits = len(self._used_qubits(layers))
+        if split_max_qubits:
+            # the fused engine's planner already stages at most a tile of
+            # qubits per pass; circuit cutting is not needed to bound memory
+            warnings.warn("split_max_qubits is handled by the fused planner; running unsplit")
+        if engine not in ("fused", "plain"):
+            raise ValueError(f"engine must be 'fused' or 'plain', got {engine!r}")
+        self.engine = engine
+        if circuit is not None:
+            self.circuit = circuit
+        else:
+            self.circuit = UnsplittedCircuit(self.num_qubits, layers)
+        self._executor = None
+        self._engine_options = engine_options
+
+    def forward(self, state=None, **kwargs):
+        if self.engine == "plain":
+            return self.circuit.forward(state, **kwargs)
+        if self._executor is None:
+            from . import engine as _engine
+
+            self._executor = _engine.FusedExecutor(self.circuit, **self._engine_options)
+        return self._executor(state, **kwargs)
+
+    def to_matrix(self, **kwargs):
+        return self.circuit.to_matrix(**kwargs)
+
+    def __matmul__(self, x):
+        return self.forward(x)
+
+    @staticmethod
+    def _used_qubits(layers) -> typing.Set[int]:
+        """qcircuit.py:69-106."""
+        qubits = set()
+        for layer in layers:
+            if isinstance(layer, (operators.CNOT, operators.CZ)):
+                qubits.add(layer.c)
+                qubits.add(layer.t)
+            elif isinstance(layer, operators.SWAP):
+                qubits.add(layer.a)
+                qubits.add(layer.b)
+            elif hasattr(layer, "qubit"):
+                qubits.add(layer.qubit)
+            elif getattr(layer, "num_qubits", None) is not None:
+                qubits.update(range(layer.num_qubits))
+            elif getattr(layer, "qubits", None) is not None:
+                qubits.update(layer.qubits)
+            elif isinstance(layer, (measurements.UnbuiltMeasurement, measurements.BuiltMeasurement)):
+                pass
+            else:
+                raise ValueError(f"Unknown layer type {type(layer)}, number of qubits could not be "
+                                 "inferred. Pass :code:`num_qubits` to the circuit.")
+        if len(qubits) == 0:
+            raise ValueError("Number of qubits could not be inferred from layers. Please provide "
+                             "num_qubits to the circuit directly.")
+        return qubits
+
+    def decompose(self):
+        return Circuit(layers=[], num_qubits=self.num_qubits, circuit=self.circuit.decompose(),
+                       engine=self.engine)
+
+
+class UnsplittedCircuit(torch.nn.Module):
+    """Sequential executor (qcircuit.py:137-212); the plain engine's loop."""
+
+    def __init__(self, num_qubits: int, layers: list):
+        super().__init__()
+        self.num_qubits = num_qubits
+        state = torch.zeros(2 ** num_qubits, dtype=torch.complex64)
+        state[0] = 1
+        self.register_buffer("state", state, persistent=False)
+        self.layers = torch.nn.ModuleList(self._build_layers(layers, num_qubits))
+
+    @staticmethod
+    def _build_layers(layers: list, num_qubits: int) -> typing.List[torch.nn.Module]:
+        out = []
+        for la in layers:
+            out.append(la.build(num_qubits=num_qubits) if hasattr(la, "build") else la)
+        return out
+
+    def forward(self, state=None, **kwargs):
+        if state is None:
+            state = self.state
+        for mod in self.layers:
+            if mod.named:
+                state = mod(state, **kwargs)
+            else:
+                state = mod(state)
+        return state
+
+    def decompose(self) -> "UnsplittedCircuit":
+        new_layers = []
+        for layer in self.layers:
+            if hasattr(layer, "decompose"):
+                if isinstance(layer, Circuit):
+                    new_layers.extend(layer.decompose().circuit.layers)
+                else:
+                    new_layers.extend(layer.decompose())
+            else:
+                new_layers.append(layer)
+        return UnsplittedCircuit(self.num_qubits, new_layers)
+
+    def to_matrix(self, **kwargs):
+        m = None
+        for mod in self.layers:
+            mm = mod.to_matrix(**kwargs)
+            m = mm if m is None else m @ mm
+        return m

@@ -195,3 +195,45 @@ def random_sel_request(rng: np.random.Generator, n_range=(4, 24), depth_range=(2
             gates.append(("cnot", q, (q + rng_) % n))
     return {"name": "serve_req", "n": n, "batch": batch, "gates": gates,
             "inputs": {"x": x}, "measure": "z", "targets": None}
+
+
+def build_circuit(desc: dict, engine: str = "fused", **engine_options):
+    """qandle_gb300.Circuit for a description, built through the public
+    front end exactly as a user would write it."""
+    import qandle_gb300 as q
+
+    layers = []
+    for g in desc["gates"]:
+        k = g[0]
+        if k == "emb":
+            layers.append(q.AngleEmbedding(name=g[2], qubits=list(g[3]), rotation=g[1]))
+        elif k in ("rx", "ry", "rz"):
+            cls = {"rx": q.RX, "ry": q.RY, "rz": q.RZ}[k]
+            if g[3] is None:
+                layers.append(cls(qubit=g[1], theta=torch.tensor(np.float32(g[2])), remapping=None))
+            else:
+                layers.append(cls(qubit=g[1], name=g[3], remapping=None))
+        elif k == "u":
+            layers.append(q.U(qubit=g[1], matrix=torch.tensor(np.asarray(g[2], np.complex64))))
+        elif k == "cnot":
+            layers.append(q.CNOT(control=g[1], target=g[2]))
+        elif k == "cz":
+            layers.append(q.CZ(control=g[1], target=g[2]))
+        elif k == "swap":
+            layers.append(q.SWAP(a=g[1], b=g[2]))
+        else:
+            raise ValueError(f"unknown gate {k}")
+    m = desc.get("measure")
+    if m == "probs":
+        layers.append(q.MeasureJointProbability())
+    elif m == "p0":
+        layers.append(q.MeasureProbability())
+    elif m == "z":
+        layers.append(q.MeasureExpectationZ())
+    return q.Circuit(layers, num_qubits=desc["n"], engine=engine, **engine_options)
+
+
+def circuit_inputs(desc: dict, device) -> dict:
+    """Named inputs of a description as float32 tensors on `device`."""
+    return {k: torch.as_tensor(np.asarray(v, dtype=np.float32)).to(device)
+            for k, v in desc.get("inputs", {}).items()}
