@@ -109,6 +109,119 @@ int qg_rotation_grad(const void* out_state, const void* grad_out, float* dtheta,
                      int n, int qubit, int axis, int per_sample, void* scratch,
                      int64_t scratch_bytes, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Fused form: a circuit lowered once to a gate program, planned into passes
+ * that each apply many gates to a shared-memory tile of 2^13 amplitudes in
+ * one HBM round trip; adjoint backward over the same program.
+ * Replaces the per-layer loop UnsplittedCircuit.forward
+ * (qandle/qcircuit.py:163-174) and torch autograd through it.
+ * ------------------------------------------------------------------------ */
+
+/* Gate kinds (records shared with the host lowering). */
+#define QG_GATE_RX 0
+#define QG_GATE_RY 1
+#define QG_GATE_RZ 2
+#define QG_GATE_U 3
+#define QG_GATE_CNOT 4
+#define QG_GATE_CZ 5
+#define QG_GATE_SWAP 6
+#define QG_GATE_EMBED 7
+
+/* One lowered gate.
+ *   RX/RY/RZ: q0 = qubit; src 0: angle params[idx] (one for all samples),
+ *             src 1: angle named[b][idx] (per sample).  t = angle / 2.
+ *   U:        q0 = qubit; idx = index into the row-form 2x2 table umats;
+ *             aux bit 0 set = the matrix is diagonal.
+ *   CNOT/CZ:  q0 = control, q1 = target.  SWAP: q0, q1.
+ *   EMBED:    AngleEmbedding; q0 = axis (0 rx, 1 ry, 2 rz), q1 = number of
+ *             angles k, idx = named column of the first angle (columns
+ *             idx..idx+k-1), aux = offset of its qubits in `qlist`.
+ *             Gates before the last embedding are dead (it overwrites the
+ *             state, qandle/embeddings.py:148-154). */
+typedef struct qg_gate {
+    int32_t kind, q0, q1, src, idx, aux;
+} qg_gate;
+
+#define QG_MEASURE_NONE 0  /* state out */
+#define QG_MEASURE_STATE 1 /* state out (MeasureState) */
+#define QG_MEASURE_PROBS 2 /* |psi|^2 [B][2^n] (MeasureAllAbsolute) */
+#define QG_MEASURE_P0 3    /* P(q = 0) [B][n] (MeasureProbability) */
+#define QG_MEASURE_Z 4     /* <Z_q> = P0 - P1 [B][n] */
+
+typedef struct qg_plan_options {
+    int32_t tile_bits;  /* qubits per forward tile (11..13; backward uses one less) */
+    int32_t low_bits;   /* contiguous low qubits in every tile (>= 4) */
+    int32_t max_high;   /* k: at most this many strided qubits per pass (0 = no limit) */
+    int32_t measure;    /* QG_MEASURE_* */
+    int32_t keep_state; /* also write the final state when measuring (for backward) */
+    int32_t segments;   /* checkpoint segments: the forward stores the state at the
+                           end of each segment but the last; the backward restarts
+                           each segment from it */
+} qg_plan_options;
+
+typedef struct qg_program qg_program;
+
+typedef struct qg_program_info_t {
+    int32_t num_qubits, gates, forward_passes, backward_passes, forward_ops, backward_ops;
+    int32_t nparams, ncols, numats, grad_slots;
+    int32_t forward_shared_slots, forward_sample_slots, backward_shared_slots, backward_sample_slots;
+    int32_t segments, has_embedding;
+    int64_t table_bytes;
+    char summary[256];
+} qg_program_info_t;
+
+typedef struct qg_pass_info_t {
+    int32_t tile_bits, nq_tile, run_bits, nfixed;
+    int32_t gbit[16], fixed_gbit[32];
+    int32_t op_count, init, epi, init_map[3], ckpt, psi_from_ckpt, grad_base, ngrad;
+    const int32_t* ops; /* host pointer to op_count x 4 int32, valid while the program lives */
+} qg_pass_info_t;
+
+void qg_plan_options_default(qg_plan_options* opt);
+/* Plan a program (host only, no GPU work).  qlist: HOST array of embedded
+ * qubits.  5 <= n <= 30. */
+int qg_program_create(const qg_gate* gates, int ngates, const int32_t* qlist, int n,
+                      const qg_plan_options* opt, qg_program** out);
+void qg_program_destroy(qg_program* prog);
+int qg_program_info(const qg_program* prog, qg_program_info_t* info);
+/* Inspect one planned pass (backward = 0/1). */
+int qg_program_pass(const qg_program* prog, int backward, int index, qg_pass_info_t* out);
+/* Matrix slots of the forward (backward = 0) or backward plan as int32
+ * records {per_sample, table_index, chain_len, chain_len x {kind, src, idx,
+ * dagger}}; returns the record length (copies only if cap is large enough). */
+int qg_program_slots(const qg_program* prog, int backward, int32_t* out, int64_t cap);
+/* Gradient slots of the backward plan as {src, idx} pairs (src 0: params,
+ * 1: named column); returns the slot count. */
+int qg_program_grad_targets(const qg_program* prog, int32_t* out, int64_t cap);
+/* Serialise the device tables into a HOST buffer of info.table_bytes; the
+ * caller copies them to device memory once and passes that pointer below. */
+int qg_program_table(const qg_program* prog, void* host_out, int64_t bytes);
+
+/* Workspace bytes for a forward (backward = 0) or backward run at `batch`. */
+int64_t qg_program_workspace_bytes(const qg_program* prog, int64_t batch, int backward);
+
+/* Forward.  state: [B][2^n]; input unless the program starts with an
+ * embedding (zero_init != 0 starts from |0..0> instead), and output when the
+ * plan stores the state.  params [nparams], named [B][ncols], umats
+ * [numats][4] complex.  out: probs [B][2^n] or P0/<Z> [B][n] per `measure`.
+ * ckpt: [segments-1][B][2^n] or NULL when segments == 1. */
+int qg_program_forward(const qg_program* prog, const void* dev_table, void* workspace,
+                       int64_t workspace_bytes, void* state, int64_t batch, int zero_init,
+                       const float* params, const float* named, const void* umats, float* out,
+                       void* ckpt, void* stream);
+
+/* Adjoint backward.  state: the forward's final state (overwritten: it is
+ * un-computed gate by gate); lam: [B][2^n] buffer.  grad_out is the upstream
+ * gradient of the forward output (float [B][n] for P0/<Z>, float [B][2^n]
+ * for probs, complex [B][2^n] torch gradient for a state output).
+ * dparams [nparams] and dnamed [B][ncols] are overwritten; dstate (optional)
+ * receives torch's gradient of the input state. */
+int qg_program_backward(const qg_program* prog, const void* dev_table, void* workspace,
+                        int64_t workspace_bytes, void* state, void* lam, int64_t batch,
+                        const float* params, const float* named, const void* umats,
+                        const void* grad_out, float* dparams, float* dnamed, void* dstate,
+                        const void* ckpt, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

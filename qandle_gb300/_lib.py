@@ -20,6 +20,42 @@ _lib = None
 c_void_p, c_int, c_int64, c_char_p = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_char_p
 c_double, c_float = ctypes.c_double, ctypes.c_float
 
+
+
+class Gate(ctypes.Structure):
+    """qg_gate (include/qandle_gb300.h)."""
+    _fields_ = [(f, ctypes.c_int32) for f in ("kind", "q0", "q1", "src", "idx", "aux")]
+
+
+class PlanOptions(ctypes.Structure):
+    """qg_plan_options."""
+    _fields_ = [(f, ctypes.c_int32) for f in ("tile_bits", "low_bits", "max_high", "measure",
+                                              "keep_state", "segments")]
+
+
+class ProgramInfo(ctypes.Structure):
+    """qg_program_info_t."""
+    _fields_ = [(f, ctypes.c_int32) for f in (
+        "num_qubits", "gates", "forward_passes", "backward_passes", "forward_ops", "backward_ops",
+        "nparams", "ncols", "numats", "grad_slots", "forward_shared_slots", "forward_sample_slots",
+        "backward_shared_slots", "backward_sample_slots", "segments", "has_embedding")] + [
+        ("table_bytes", ctypes.c_int64), ("summary", ctypes.c_char * 256)]
+
+
+class PassInfo(ctypes.Structure):
+    """qg_pass_info_t."""
+    _fields_ = [("tile_bits", ctypes.c_int32), ("nq_tile", ctypes.c_int32),
+                ("run_bits", ctypes.c_int32), ("nfixed", ctypes.c_int32),
+                ("gbit", ctypes.c_int32 * 16), ("fixed_gbit", ctypes.c_int32 * 32)] + [
+        (f, ctypes.c_int32) for f in ("op_count", "init", "epi")] + [
+        ("init_map", ctypes.c_int32 * 3)] + [
+        (f, ctypes.c_int32) for f in ("ckpt", "psi_from_ckpt", "grad_base", "ngrad")] + [
+        ("ops", ctypes.POINTER(ctypes.c_int32))]
+
+
+GATE = {"rx": 0, "ry": 1, "rz": 2, "u": 3, "cnot": 4, "cz": 5, "swap": 6, "emb": 7}
+MEASURE = {"none": 0, "state": 1, "probs": 2, "p0": 3, "z": 4}
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "qg_version": (c_int, []),
@@ -40,6 +76,21 @@ SIGNATURES = {
     "qg_rotation_grad_scratch_bytes": (c_int64, [c_int64, c_int]),
     "qg_rotation_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_int, c_int, c_int,
                                  c_void_p, c_int64, c_void_p]),
+    "qg_plan_options_default": (None, [ctypes.POINTER(PlanOptions)]),
+    "qg_program_create": (c_int, [ctypes.POINTER(Gate), c_int, c_void_p, c_int,
+                                  ctypes.POINTER(PlanOptions), ctypes.POINTER(c_void_p)]),
+    "qg_program_destroy": (None, [c_void_p]),
+    "qg_program_info": (c_int, [c_void_p, ctypes.POINTER(ProgramInfo)]),
+    "qg_program_pass": (c_int, [c_void_p, c_int, c_int, ctypes.POINTER(PassInfo)]),
+    "qg_program_table": (c_int, [c_void_p, c_void_p, c_int64]),
+    "qg_program_slots": (c_int, [c_void_p, c_int, c_void_p, c_int64]),
+    "qg_program_grad_targets": (c_int, [c_void_p, c_void_p, c_int64]),
+    "qg_program_workspace_bytes": (c_int64, [c_void_p, c_int64, c_int]),
+    "qg_program_forward": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int,
+                                   c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "qg_program_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
+                                    c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p]),
 }
 
 

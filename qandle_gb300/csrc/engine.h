@@ -1,0 +1,108 @@
+// Internal descriptors shared by the fusion planner (program.cpp) and the
+// fused pass kernels (fused.cu).  All structs are plain data copied verbatim
+// to device memory.
+#pragma once
+#include <stdint.h>
+
+namespace qg {
+
+constexpr int kRegBits = 5;         // amplitudes per thread = 2^5, held in registers
+constexpr int kMaxTileBits = 13;    // forward tile: 2^13 amplitudes, 256 threads, 64 KiB
+constexpr int kMaxQubits = 30;      // fused engine limit (global bit masks are 32-bit)
+constexpr int kMaxGradPerPass = 96; // backward: gradient slots per pass (shared-memory partials)
+
+// Device op codes (int4 per op: x = opcode, y/z/w operands).
+enum Opcode : int32_t {
+    OP_MAP = 1,   // exchange through shared memory to a new register/lane/warp mapping
+                  //   y = 5 register local bits (4 bits each), z = 5 lane local bits,
+                  //   w = warp local bits (4 bits each) | (count << 16)
+    OP_MAT = 2,   // 2x2 on register position y with matrix slot z; w = flags
+    OP_DIAG = 3,  // diag(m00, m11) on the bit at location y with slot z; w = flags
+    OP_CX = 4,    // X on register position y when the control at location z is 1
+    OP_CZ = 5,    // negate when the bits at locations y and z are both 1
+    OP_SWAP = 6,  // exchange register positions y and z
+    OP_GRAD = 7,  // backward: gradient partial Im<lam|P|psi> of axis z on register
+                  //   position y into grad slot w (no state change)
+};
+constexpr int32_t LOC_REG = 0x100;  // location = register position (low bits); else global bit
+constexpr int32_t OPF_PER_SAMPLE = 1;  // matrix slot is per sample
+constexpr int32_t OPF_GRAD = 2;        // OP_MAT in the backward: gradient first (axis in bits 8..9)
+
+enum InitKind : int32_t { INIT_LOAD = 0, INIT_ZERO = 1, INIT_EMBED = 2 };
+enum EpiFlags : int32_t { EPI_STORE = 1, EPI_PROBS = 2, EPI_P0 = 4 };
+
+struct PassDesc {
+    int32_t tile_bits;        // TB (13 forward, 12 backward)
+    int32_t nq_tile;          // local bits that are qubits: min(n, TB); the rest are sample bits
+    int32_t run_bits;         // low local bits contiguous in memory
+    int32_t nfixed;           // qubit bits outside the tile (n - nq_tile)
+    int32_t gbit[16];         // local bit -> global bit (local < nq_tile)
+    int32_t fixed_gbit[32];   // global bits outside the tile, ascending
+    int32_t op_begin, op_count;
+    int32_t init;             // InitKind
+    int32_t epi;              // EpiFlags
+    int32_t init_map[3];      // mapping the init produces (OP_MAP encoding y, z, w)
+    int32_t ckpt;             // forward: also store the state into checkpoint ckpt (-1: none)
+    int32_t grad_base;        // backward: first grad slot of this pass
+    int32_t ngrad;            // backward: grad slots in this pass
+    int32_t psi_from_ckpt;    // backward: read psi from checkpoint (>= 0) instead of the state
+    int32_t pad[3];
+};
+
+struct SlotDesc {
+    int32_t chain_begin, chain_len;
+    int32_t per_sample;       // 1: one matrix per sample
+    int32_t out_index;        // index within the shared or per-sample matrix table
+};
+
+struct ChainEntry {
+    int32_t kind;    // 0..2 rotation axis, 3 = explicit row matrix
+    int32_t src;     // rotation: 0 = params[idx], 1 = named[b][idx]; matrix: umats[idx]
+    int32_t idx;
+    int32_t dagger;  // use the inverse
+};
+
+struct GradTarget {
+    int32_t src;     // 0 = params[idx] (summed over samples), 1 = named[b][idx]
+    int32_t idx;
+};
+
+struct EmbedDesc {
+    int32_t axis;
+    int32_t nq;
+    int32_t col0;        // first named column
+    int32_t pad;
+    int8_t qubit[64];
+};
+
+// Launch-time pointers of one fused program run (forward or backward).
+struct RunArgs {
+    float2* state;            // [B][2^n] working state (psi)
+    float2* lam;              // backward: cotangent [B][2^n]
+    float2* ckpt;             // checkpoints [nckpt][B][2^n] (may be null)
+    float* out;               // probs [B][2^n] (EPI_PROBS)
+    float* p0part;            // P0 partials [B][tps][TB + 1] (EPI_P0)
+    float* gradpart;          // backward: grad partials [grad slot][tiles]
+    const float2* mats;       // shared matrices [S][4]
+    const float2* mats_ps;    // per-sample matrices [B][P][4]
+    const float2* embfac;     // embedding factors [B][n][2]
+    int* status;              // device status word (bounded waits)
+    int64_t batch;
+    int32_t n;
+    int32_t nslots_ps;        // P
+};
+
+// Host view of a planned program, for the launch code in fused.cu.
+struct ProgramRun {
+    int n, tile_bits, measure, keep_state, segments;
+    int nparams, ncols, numats, ngrads, has_embed;
+    int nfslots, f_shared, f_ps, nbslots, b_shared, b_ps;
+    int nfpass, nbpass;
+    const PassDesc* fpass;  // host copies
+    const PassDesc* bpass;
+    size_t off_fpass, off_fops, off_fslot, off_fchain;
+    size_t off_bpass, off_bops, off_bslot, off_bchain, off_embed, off_pcsr, off_ccsr;
+};
+void program_run_info(const void* prog, ProgramRun* out);
+
+}  // namespace qg

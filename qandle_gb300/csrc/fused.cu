@@ -1,0 +1,1200 @@
+// Fused form: shared-memory-staged passes that apply many gates per HBM round
+// trip, and the adjoint backward over the same program.
+//
+// One persistent CTA per SM walks the tiles of a pass.  A tile is 2^TB
+// amplitudes (TB = 13 forward, 12 backward) spanning TB qubits of one sample,
+// or whole samples when n < TB.  Its memory image is 2^(TB - run_bits)
+// contiguous runs of 2^run_bits amplitudes; the runs are moved by bulk async
+// copies (cp.async.bulk, completion on an mbarrier) into a double buffer, so
+// the next tile streams in while the current one is computed.  Threads hold 32
+// amplitudes each in registers; gates act in registers, and an OP_MAP
+// exchange through a swizzled shared-memory layout changes which five tile
+// qubits are register qubits.
+//
+// The gate programs come from the planner in program.cpp.  The rotation and
+// matrix algebra follows the reference's row-vector convention,
+// out = in @ M (qandle/operators.py:265-298, :368-395, :125-126).
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "engine.h"
+#include "qandle_gb300.h"
+
+namespace qg {
+
+// ------------------------------------------------------------------ PTX --
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Bounded wait on an mbarrier phase.  Returns false if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t addr = smem_u32(bar);
+    for (int it = 0; it < (1 << 22); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read0() {
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_all0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// ------------------------------------------------------- tile geometry --
+
+// Swizzled shared-memory slot of local index j: the low 4 bits are XORed with
+// the 4-bit groups above them, so any 4 lane bits with distinct (bit mod 4)
+// hit distinct 8-byte bank pairs.
+__device__ __forceinline__ int swz(int j) { return j ^ (((j >> 4) ^ (j >> 8) ^ (j >> 12)) & 15); }
+
+struct TileGeo {
+    int64_t sample;       // first sample of the tile
+    int nsamples;         // valid samples in the tile (n < TB) else 1
+    uint32_t fixed_val;   // global-bit values of the qubits outside the tile
+    int64_t base;         // amplitude offset of local index 0
+    int tile_in_sample;   // n >= TB: tile index within the sample
+};
+
+__device__ __forceinline__ TileGeo tile_geo(const PassDesc& d, int64_t t, int n, int64_t batch) {
+    TileGeo g;
+    if (n >= d.tile_bits) {
+        int64_t tps = int64_t(1) << (n - d.tile_bits);
+        g.sample = t / tps;
+        int64_t ti = t - g.sample * tps;
+        g.tile_in_sample = (int)ti;
+        uint32_t fv = 0;
+        for (int k = 0; k < d.nfixed; ++k) fv |= (uint32_t)((ti >> k) & 1) << d.fixed_gbit[k];
+        g.fixed_val = fv;
+        g.base = (g.sample << n) + fv;
+        g.nsamples = 1;
+    } else {
+        int spt = 1 << (d.tile_bits - n);
+        g.sample = t * spt;
+        int64_t rem = batch - g.sample;
+        g.nsamples = rem < spt ? (int)rem : spt;
+        g.fixed_val = 0;
+        g.base = g.sample << n;
+        g.tile_in_sample = 0;
+    }
+    return g;
+}
+
+// global amplitude offset of the first element of run r
+__device__ __forceinline__ int64_t run_offset(const PassDesc& d, int r) {
+    int64_t off = 0;
+    int hi = d.tile_bits - d.run_bits;
+    for (int k = 0; k < hi; ++k)
+        if ((r >> k) & 1) {
+            int lb = d.run_bits + k;
+            off += (lb < d.nq_tile) ? (int64_t(1) << d.gbit[lb]) : 0;
+        }
+    return off;
+}
+
+// Bytes of one tile's state image.
+__device__ __forceinline__ uint32_t tile_bytes(const PassDesc& d, const TileGeo& g, int n) {
+    if (n < d.tile_bits) return (uint32_t)((int64_t)g.nsamples << n) * 8u;
+    return (1u << d.tile_bits) * 8u;
+}
+
+// Issue the bulk copies of one tile (one thread; the caller has armed `bar`
+// with the expected byte count through a single arrive.expect_tx).
+__device__ void issue_tile_load(const PassDesc& d, const TileGeo& g, const float2* src, float2* dst,
+                                uint64_t* bar, int n) {
+    if (n < d.tile_bits) {
+        bulk_g2s(dst, src + g.base, tile_bytes(d, g, n), bar);
+        return;
+    }
+    int runs = 1 << (d.tile_bits - d.run_bits);
+    uint32_t rb = (1u << d.run_bits) * 8u;
+    for (int r = 0; r < runs; ++r) bulk_g2s(dst + ((int64_t)r << d.run_bits), src + g.base + run_offset(d, r), rb, bar);
+}
+
+__device__ void issue_tile_store(const PassDesc& d, const TileGeo& g, float2* dstg, const float2* src, int n) {
+    if (n < d.tile_bits) {
+        uint32_t bytes = (uint32_t)((int64_t)g.nsamples << n) * 8u;
+        bulk_s2g(dstg + g.base, src, bytes);
+        return;
+    }
+    int runs = 1 << (d.tile_bits - d.run_bits);
+    uint32_t rb = (1u << d.run_bits) * 8u;
+    for (int r = 0; r < runs; ++r) bulk_s2g(dstg + g.base + run_offset(d, r), src + ((int64_t)r << d.run_bits), rb);
+}
+
+// float (probability) image of a tile: half the bytes of the state image
+__device__ void issue_tile_store_f32(const PassDesc& d, const TileGeo& g, float* dstg, const float* src, int n) {
+    if (n < d.tile_bits) {
+        uint32_t bytes = (uint32_t)((int64_t)g.nsamples << n) * 4u;
+        bulk_s2g(dstg + g.base, src, bytes);
+        return;
+    }
+    int runs = 1 << (d.tile_bits - d.run_bits);
+    uint32_t rb = (1u << d.run_bits) * 4u;
+    for (int r = 0; r < runs; ++r) bulk_s2g(dstg + g.base + run_offset(d, r), src + ((int64_t)r << d.run_bits), rb);
+}
+
+// ----------------------------------------------------- thread mapping --
+
+struct ThreadMap {
+    int regl[5];     // register bit k -> local bit
+    int thr_off;     // local-index contribution of this thread's lane/warp bits
+    uint32_t tglob;  // global-bit values of this thread's qubit thread bits | tile fixed bits
+    int sample_off;  // sample offset within the tile (n < TB)
+};
+
+__device__ __forceinline__ void decode_map(const PassDesc& d, int32_t y, int32_t z, int32_t w, int tid,
+                                           uint32_t fixed_val, ThreadMap& m) {
+    for (int k = 0; k < 5; ++k) m.regl[k] = (y >> (4 * k)) & 15;
+    int nw = (w >> 16) & 7;
+    int off = 0, soff = 0;
+    uint32_t tg = fixed_val;
+    for (int k = 0; k < 5 + nw; ++k) {
+        int lb = k < 5 ? ((z >> (4 * k)) & 15) : ((w >> (4 * (k - 5))) & 15);
+        int bit = (tid >> k) & 1;
+        off |= bit << lb;
+        if (lb < d.nq_tile)
+            tg |= (uint32_t)bit << d.gbit[lb];
+        else
+            soff |= bit << (lb - d.nq_tile);
+    }
+    m.thr_off = off;
+    m.tglob = tg;
+    m.sample_off = soff;
+}
+
+template <int K>
+__device__ __forceinline__ int roff(const ThreadMap& m) {
+    return ((K & 1) ? (1 << m.regl[0]) : 0) + ((K & 2) ? (1 << m.regl[1]) : 0) +
+           ((K & 4) ? (1 << m.regl[2]) : 0) + ((K & 8) ? (1 << m.regl[3]) : 0) +
+           ((K & 16) ? (1 << m.regl[4]) : 0);
+}
+
+__device__ __forceinline__ int roff_rt(const ThreadMap& m, int r) {
+    int o = 0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+        if ((r >> k) & 1) o += 1 << m.regl[k];
+    return o;
+}
+
+template <int K = 0>
+__device__ __forceinline__ void xwrite(float2* buf, const float2 (&a)[32], const ThreadMap& m) {
+    buf[swz(m.thr_off + roff<K>(m))] = a[K];
+    if constexpr (K + 1 < 32) xwrite<K + 1>(buf, a, m);
+}
+template <int K = 0>
+__device__ __forceinline__ void xread(const float2* buf, float2 (&a)[32], const ThreadMap& m) {
+    a[K] = buf[swz(m.thr_off + roff<K>(m))];
+    if constexpr (K + 1 < 32) xread<K + 1>(buf, a, m);
+}
+
+// natural mapping: lanes = local bits 0..4, registers 5..9, warps 10..
+__device__ __forceinline__ int nat_index(int r, int tid) { return (tid & 31) | (r << 5) | ((tid >> 5) << 10); }
+
+template <int TB>
+struct NatMap {
+    static constexpr int32_t y = 0x98765;
+    static constexpr int32_t z = 0x43210;
+    static constexpr int32_t w = (TB >= 11 ? 0xA : 0) | (TB >= 12 ? 0xB0 : 0) | (TB >= 13 ? 0xC00 : 0) |
+                                 ((TB - 10) << 16);
+};
+
+// ---------------------------------------------------------- gate ops --
+
+template <int P>
+__device__ __forceinline__ void mat_reg(float2 (&a)[32], const float2 m[4]) {
+#pragma unroll
+    for (int r = 0; r < 32; ++r)
+        if (!(r & (1 << P))) apply_row2(a[r], a[r | (1 << P)], m);
+}
+
+__device__ __forceinline__ void mat_dispatch(int p, float2 (&a)[32], const float2 m[4]) {
+    switch (p) {
+        case 0: mat_reg<0>(a, m); break;
+        case 1: mat_reg<1>(a, m); break;
+        case 2: mat_reg<2>(a, m); break;
+        case 3: mat_reg<3>(a, m); break;
+        default: mat_reg<4>(a, m); break;
+    }
+}
+
+template <int P>
+__device__ __forceinline__ void diag_reg(float2 (&a)[32], float2 d0, float2 d1) {
+#pragma unroll
+    for (int r = 0; r < 32; ++r) a[r] = cmul(a[r], (r & (1 << P)) ? d1 : d0);
+}
+
+// X on register position P when (ctrl_reg >= 0 ? bit ctrl_reg of r : tcond)
+template <int P>
+__device__ __forceinline__ void cx_reg(float2 (&a)[32], int ctrl_reg, bool tcond) {
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+        if (r & (1 << P)) continue;
+        bool c = ctrl_reg >= 0 ? ((r >> ctrl_reg) & 1) : tcond;
+        float2 x = a[r], y = a[r | (1 << P)];
+        a[r] = c ? y : x;
+        a[r | (1 << P)] = c ? x : y;
+    }
+}
+
+template <int P0, int P1>
+__device__ __forceinline__ void swap_reg(float2 (&a)[32]) {
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+        if ((r & (1 << P0)) && !(r & (1 << P1))) {
+            int s = r ^ (1 << P0) ^ (1 << P1);
+            float2 t = a[r];
+            a[r] = a[s];
+            a[s] = t;
+        }
+    }
+}
+
+template <int P0>
+__device__ __forceinline__ void swap_dispatch1(int p1, float2 (&a)[32]) {
+    switch (p1) {
+        case 0: swap_reg<P0, 0>(a); break;
+        case 1: swap_reg<P0, 1>(a); break;
+        case 2: swap_reg<P0, 2>(a); break;
+        case 3: swap_reg<P0, 3>(a); break;
+        default: swap_reg<P0, 4>(a); break;
+    }
+}
+
+__device__ __forceinline__ void swap_dispatch(int p0, int p1, float2 (&a)[32]) {
+    if (p0 == p1) return;
+    switch (p0) {
+        case 0: swap_dispatch1<0>(p1, a); break;
+        case 1: swap_dispatch1<1>(p1, a); break;
+        case 2: swap_dispatch1<2>(p1, a); break;
+        case 3: swap_dispatch1<3>(p1, a); break;
+        default: swap_dispatch1<4>(p1, a); break;
+    }
+}
+
+__device__ __forceinline__ bool loc_bit_thread(int32_t loc, uint32_t tglob) {
+    return (tglob >> (loc & 31)) & 1;
+}
+
+// Im( conj(l0) (P p)_0 + conj(l1) (P p)_1 ) summed over the pairs of position P
+template <int P>
+__device__ __forceinline__ float grad_reg(const float2 (&psi)[32], const float2 (&lam)[32], int axis) {
+    float acc = 0.f;
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+        if (r & (1 << P)) continue;
+        float2 p0 = psi[r], p1 = psi[r | (1 << P)];
+        apply_pauli(axis, p0, p1);
+        float2 l0 = lam[r], l1 = lam[r | (1 << P)];
+        acc += l0.x * p0.y - l0.y * p0.x + l1.x * p1.y - l1.y * p1.x;
+    }
+    return acc;
+}
+
+__device__ __forceinline__ float grad_dispatch(int p, const float2 (&psi)[32], const float2 (&lam)[32], int axis) {
+    switch (p) {
+        case 0: return grad_reg<0>(psi, lam, axis);
+        case 1: return grad_reg<1>(psi, lam, axis);
+        case 2: return grad_reg<2>(psi, lam, axis);
+        case 3: return grad_reg<3>(psi, lam, axis);
+        default: return grad_reg<4>(psi, lam, axis);
+    }
+}
+
+__device__ __forceinline__ void load_slot(const RunArgs& A, int32_t slot, int32_t flags, int64_t sample,
+                                          float2 m[4]) {
+    // lanes of a partial tile past the last sample compute on garbage that is
+    // never stored; keep their table reads inside the table
+    if (sample >= A.batch) sample = A.batch - 1;
+    const float4* src = (flags & OPF_PER_SAMPLE)
+                            ? reinterpret_cast<const float4*>(A.mats_ps + (sample * A.nslots_ps + slot) * 4)
+                            : reinterpret_cast<const float4*>(A.mats + (int64_t)slot * 4);
+    float4 u = __ldg(src), v = __ldg(src + 1);
+    m[0] = make_float2(u.x, u.y);
+    m[1] = make_float2(u.z, u.w);
+    m[2] = make_float2(v.x, v.y);
+    m[3] = make_float2(v.z, v.w);
+}
+
+// Apply one non-map op to a register set.
+__device__ __forceinline__ void apply_op(const int4 op, float2 (&a)[32], const ThreadMap& tm, const RunArgs& A,
+                                         int64_t sample, bool dagger_slots) {
+    switch (op.x) {
+        case OP_MAT: {
+            float2 m[4];
+            load_slot(A, op.z, op.w, sample, m);
+            mat_dispatch(op.y, a, m);
+            break;
+        }
+        case OP_DIAG: {
+            float2 m[4];
+            load_slot(A, op.z, op.w, sample, m);
+            if (op.y & LOC_REG) {
+                switch (op.y & 7) {
+                    case 0: diag_reg<0>(a, m[0], m[3]); break;
+                    case 1: diag_reg<1>(a, m[0], m[3]); break;
+                    case 2: diag_reg<2>(a, m[0], m[3]); break;
+                    case 3: diag_reg<3>(a, m[0], m[3]); break;
+                    default: diag_reg<4>(a, m[0], m[3]); break;
+                }
+            } else {
+                float2 d = loc_bit_thread(op.y, tm.tglob) ? m[3] : m[0];
+#pragma unroll
+                for (int r = 0; r < 32; ++r) a[r] = cmul(a[r], d);
+            }
+            break;
+        }
+        case OP_CX: {
+            int cr = (op.z & LOC_REG) ? (op.z & 7) : -1;
+            bool tc = cr < 0 ? loc_bit_thread(op.z, tm.tglob) : false;
+            if (cr < 0 && !tc) break;
+            switch (op.y) {
+                case 0: cx_reg<0>(a, cr, tc); break;
+                case 1: cx_reg<1>(a, cr, tc); break;
+                case 2: cx_reg<2>(a, cr, tc); break;
+                case 3: cx_reg<3>(a, cr, tc); break;
+                default: cx_reg<4>(a, cr, tc); break;
+            }
+            break;
+        }
+        case OP_CZ: {
+            int r0 = (op.y & LOC_REG) ? (op.y & 7) : -1;
+            int r1 = (op.z & LOC_REG) ? (op.z & 7) : -1;
+            bool t0 = r0 < 0 ? loc_bit_thread(op.y, tm.tglob) : true;
+            bool t1 = r1 < 0 ? loc_bit_thread(op.z, tm.tglob) : true;
+            if (!(t0 && t1)) break;
+            uint32_t need = (r0 >= 0 ? (1u << r0) : 0u) | (r1 >= 0 ? (1u << r1) : 0u);
+#pragma unroll
+            for (int r = 0; r < 32; ++r)
+                if (((uint32_t)r & need) == need) a[r] = make_float2(-a[r].x, -a[r].y);
+            break;
+        }
+        case OP_SWAP:
+            swap_dispatch(op.y, op.z, a);
+            break;
+        default:
+            break;
+    }
+    (void)dagger_slots;
+}
+
+// --------------------------------------------------------- the pass --
+
+template <int TB>
+struct PassSmem {
+    static constexpr int kAmps = 1 << TB;
+    static constexpr int kThreads = 1 << (TB - 5);
+};
+
+// Forward pass kernel.  One persistent CTA per SM.
+template <int TB>
+__global__ void __launch_bounds__(1 << (TB - 5), 1)
+    k_fwd_pass(const PassDesc* __restrict__ passes, const int4* __restrict__ ops_all, int pass_index, RunArgs A,
+               int zero_init, const EmbedDesc* __restrict__ emb, int64_t num_tiles) {
+    constexpr int NT = 1 << (TB - 5);
+    constexpr int AMPS = 1 << TB;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float2* buf0 = reinterpret_cast<float2*>(smem_raw);
+    float2* buf1 = buf0 + AMPS;
+    __shared__ __align__(8) uint64_t bars[2];
+
+    const PassDesc d = passes[pass_index];
+    const int4* ops = ops_all + d.op_begin;
+    const int tid = threadIdx.x;
+    const int n = A.n;
+    const bool load_in = (d.init == INIT_LOAD) && !zero_init;
+
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    int64_t t0 = blockIdx.x;
+    if (load_in && tid == 0 && t0 < num_tiles) {
+        TileGeo g = tile_geo(d, t0, n, A.batch);
+        mbar_expect_tx(&bars[0], tile_bytes(d, g, n));
+        issue_tile_load(d, g, A.state, buf0, &bars[0], n);
+    }
+    int iter = 0;
+    for (int64_t t = t0; t < num_tiles; t += gridDim.x, ++iter) {
+        float2* buf = (iter & 1) ? buf1 : buf0;
+        float2* nbuf = (iter & 1) ? buf0 : buf1;
+        TileGeo g = tile_geo(d, t, n, A.batch);
+        float2 a[32];
+        ThreadMap tm;
+        if (load_in) {
+            bool ok = mbar_wait(&bars[iter & 1], (iter >> 1) & 1);
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) atomicExch(A.status, QG_ETIMEOUT);
+                break;
+            }
+#pragma unroll
+            for (int r = 0; r < 32; ++r) a[r] = buf[nat_index(r, tid)];
+            decode_map(d, NatMap<TB>::y, NatMap<TB>::z, NatMap<TB>::w, tid, g.fixed_val, tm);
+        } else {
+            if (d.init == INIT_EMBED)
+                decode_map(d, d.init_map[0], d.init_map[1], d.init_map[2], tid, g.fixed_val, tm);
+            else
+                decode_map(d, NatMap<TB>::y, NatMap<TB>::z, NatMap<TB>::w, tid, g.fixed_val, tm);
+            int64_t smp = g.sample + tm.sample_off;
+            if (d.init == INIT_EMBED && smp < A.batch) {
+                // amplitude = prod over qubits of the per-sample factor of its bit
+                const float2* fac = A.embfac + smp * n * 2;
+                float2 c = make_float2(1.f, 0.f);
+                uint32_t regmask = 0;
+                for (int k = 0; k < 5; ++k) regmask |= 1u << d.gbit[tm.regl[k]];
+                for (int b = 0; b < n; ++b) {
+                    if (regmask & (1u << b)) continue;
+                    c = cmul(c, fac[2 * (n - 1 - b) + ((tm.tglob >> b) & 1)]);
+                }
+                a[0] = c;
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    int b = d.gbit[tm.regl[k]];
+                    float2 f0 = fac[2 * (n - 1 - b)], f1 = fac[2 * (n - 1 - b) + 1];
+#pragma unroll
+                    for (int r = 0; r < (1 << k); ++r) {
+                        a[r + (1 << k)] = cmul(a[r], f1);
+                        a[r] = cmul(a[r], f0);
+                    }
+                }
+            } else if (d.init == INIT_EMBED) {
+#pragma unroll
+                for (int r = 0; r < 32; ++r) a[r] = make_float2(0.f, 0.f);
+            } else {
+                // |0..0>: amplitude 1 where every qubit bit (in and outside the tile) is 0
+                const int qmask = (1 << d.nq_tile) - 1;
+#pragma unroll
+                for (int r = 0; r < 32; ++r) {
+                    bool origin = g.fixed_val == 0 && ((tm.thr_off + roff_rt(tm, r)) & qmask) == 0;
+                    a[r] = make_float2(origin ? 1.f : 0.f, 0.f);
+                }
+            }
+        }
+        // everybody has read `buf`; prefetch the next tile into the other buffer
+        __syncthreads();
+        if (load_in && tid == 0 && t + gridDim.x < num_tiles) {
+            bulk_wait_read0();  // stores issued from nbuf two tiles ago have read it
+            TileGeo gn = tile_geo(d, t + gridDim.x, n, A.batch);
+            mbar_expect_tx(&bars[(iter + 1) & 1], tile_bytes(d, gn, n));
+            issue_tile_load(d, gn, A.state, nbuf, &bars[(iter + 1) & 1], n);
+        }
+        const int64_t my_sample = g.sample + tm.sample_off;
+        // ---- the gate program of this pass ----
+        for (int o = 0; o < d.op_count; ++o) {
+            int4 op = __ldg(ops + o);
+            if (op.x == OP_MAP) {
+                __syncthreads();
+                xwrite(buf, a, tm);
+                __syncthreads();
+                decode_map(d, op.y, op.z, op.w, tid, g.fixed_val, tm);
+                xread(buf, a, tm);
+            } else {
+                apply_op(op, a, tm, A, g.sample + tm.sample_off, false);
+            }
+        }
+        (void)my_sample;
+        // ---- epilogue (the planner left the natural mapping) ----
+        __syncthreads();  // all exchange reads of `buf` are done
+        const int64_t smp0 = g.sample;
+        if (d.epi & EPI_STORE) {
+#pragma unroll
+            for (int r = 0; r < 32; ++r) buf[nat_index(r, tid)] = a[r];
+            fence_proxy_async();
+            __syncthreads();
+            if (tid == 0) {
+                issue_tile_store(d, g, A.state, buf, n);
+                if (d.ckpt >= 0) issue_tile_store(d, g, A.ckpt + (int64_t)d.ckpt * (A.batch << n), buf, n);
+                bulk_commit();
+            }
+        }
+        if (d.epi & (EPI_PROBS | EPI_P0)) {
+            if (d.epi & EPI_STORE) {
+                if (tid == 0) bulk_wait_read0();
+                __syncthreads();
+            }
+            float* pb = reinterpret_cast<float*>(buf);
+#pragma unroll
+            for (int r = 0; r < 32; ++r) pb[nat_index(r, tid)] = a[r].x * a[r].x + a[r].y * a[r].y;
+            if (d.epi & EPI_PROBS) {
+                fence_proxy_async();
+                __syncthreads();
+                if (tid == 0) {
+                    issue_tile_store_f32(d, g, A.out, pb, n);
+                    bulk_commit();
+                    bulk_wait_read0();
+                }
+            }
+            __syncthreads();
+            if (d.epi & EPI_P0) {
+                // phase A: thread t owns the 32 consecutive probabilities of chunk t
+                float* ptot = pb + AMPS;          // [NT]
+                float* psub = ptot + NT;          // [5][NT]
+                const float* chunk = pb + tid * 32;
+                float tot = 0.f, sj[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int k = 0; k < 32; ++k) {
+                    int idx = (k + tid) & 31;  // rotated start: conflict-free across lanes
+                    float v = chunk[idx];
+                    tot += v;
+#pragma unroll
+                    for (int j = 0; j < 5; ++j) sj[j] += ((idx >> j) & 1) ? 0.f : v;
+                }
+                __syncthreads();  // every chunk is read before the partial arrays overwrite nothing
+                ptot[tid] = tot;
+#pragma unroll
+                for (int j = 0; j < 5; ++j) psub[j * NT + tid] = sj[j];
+                __syncthreads();
+                // phase B: (sample, local bit) items
+                const int nq = d.nq_tile;
+                const int cps = 1 << (nq - 5);            // chunks (threads) per sample
+                const int spt = NT / cps;                 // samples per tile
+                const int items = spt * (nq + 1);
+                const int64_t tps = (n >= TB) ? (int64_t(1) << (n - TB)) : 1;
+                if (cps >= 32) {
+                    const int warp = tid >> 5, lane = tid & 31;
+                    for (int it = warp; it < items; it += NT / 32) {
+                        int s = it / (nq + 1), j = it % (nq + 1);
+                        float acc = 0.f;
+                        for (int c = lane; c < cps; c += 32) {
+                            int t2 = s * cps + c;
+                            if (j < 5) acc += psub[j * NT + t2];
+                            else if (j < nq) acc += ((t2 >> (j - 5)) & 1) ? 0.f : ptot[t2];
+                            else acc += ptot[t2];
+                        }
+                        for (int o2 = 16; o2 > 0; o2 >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o2);
+                        if (lane == 0 && s < g.nsamples) {
+                            int64_t smp = smp0 + s;
+                            float* dst = A.p0part + ((smp * tps + g.tile_in_sample) * (TB + 1));
+                            dst[j < nq ? j : TB] = acc;
+                        }
+                    }
+                } else {
+                    for (int it = tid; it < items; it += NT) {
+                        int s = it / (nq + 1), j = it % (nq + 1);
+                        float acc = 0.f;
+                        for (int c = 0; c < cps; ++c) {
+                            int t2 = s * cps + c;
+                            if (j < 5) acc += psub[j * NT + t2];
+                            else if (j < nq) acc += ((t2 >> (j - 5)) & 1) ? 0.f : ptot[t2];
+                            else acc += ptot[t2];
+                        }
+                        if (s < g.nsamples) {
+                            int64_t smp = smp0 + s;
+                            float* dst = A.p0part + ((smp * tps + g.tile_in_sample) * (TB + 1));
+                            dst[j < nq ? j : TB] = acc;
+                        }
+                    }
+                }
+            }
+        }
+        // make `buf` free before it receives the prefetch two tiles ahead
+        fence_proxy_async();
+        __syncthreads();
+    }
+    if (tid == 0) bulk_wait_all0();
+    (void)emb;
+}
+
+// Backward pass kernel: psi and lambda tiles (TB = 12), gradient partials.
+template <int TB>
+__global__ void __launch_bounds__(1 << (TB - 5), 1)
+    k_bwd_pass(const PassDesc* __restrict__ passes, const int4* __restrict__ ops_all, int pass_index, RunArgs A,
+               int store_lam_last, int64_t num_tiles) {
+    constexpr int NT = 1 << (TB - 5);
+    constexpr int AMPS = 1 << TB;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float2* pbuf0 = reinterpret_cast<float2*>(smem_raw);  // psi, lambda, psi, lambda
+    float* gacc = reinterpret_cast<float*>(pbuf0 + 4 * AMPS);  // [ngrad][NT]
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int s_tsample[NT];
+
+    const PassDesc d = passes[pass_index];
+    const int4* ops = ops_all + d.op_begin;
+    const int tid = threadIdx.x;
+    const int n = A.n;
+    const float2* psi_src = d.psi_from_ckpt >= 0 ? A.ckpt + (int64_t)d.psi_from_ckpt * (A.batch << n) : A.state;
+    const bool last = (d.epi & EPI_STORE) == 0;  // final backward pass: nothing to store but lambda
+    (void)last;
+
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int64_t t0 = blockIdx.x;
+    if (tid == 0 && t0 < num_tiles) {
+        TileGeo g = tile_geo(d, t0, n, A.batch);
+        mbar_expect_tx(&bars[0], 2 * tile_bytes(d, g, n));
+        issue_tile_load(d, g, psi_src, pbuf0, &bars[0], n);
+        issue_tile_load(d, g, A.lam, pbuf0 + AMPS, &bars[0], n);
+    }
+    int iter = 0;
+    for (int64_t t = t0; t < num_tiles; t += gridDim.x, ++iter) {
+        float2* ps = pbuf0 + (iter & 1) * 2 * AMPS;
+        float2* ls = ps + AMPS;
+        float2* nps = pbuf0 + ((iter + 1) & 1) * 2 * AMPS;
+        TileGeo g = tile_geo(d, t, n, A.batch);
+        float2 psi[32], lam[32];
+        ThreadMap tm;
+        bool ok = mbar_wait(&bars[iter & 1], (iter >> 1) & 1);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicExch(A.status, QG_ETIMEOUT);
+            break;
+        }
+#pragma unroll
+        for (int r = 0; r < 32; ++r) {
+            psi[r] = ps[nat_index(r, tid)];
+            lam[r] = ls[nat_index(r, tid)];
+        }
+        decode_map(d, NatMap<TB>::y, NatMap<TB>::z, NatMap<TB>::w, tid, g.fixed_val, tm);
+        __syncthreads();
+        if (tid == 0 && t + gridDim.x < num_tiles) {
+            bulk_wait_read0();
+            TileGeo gn = tile_geo(d, t + gridDim.x, n, A.batch);
+            mbar_expect_tx(&bars[(iter + 1) & 1], 2 * tile_bytes(d, gn, n));
+            issue_tile_load(d, gn, psi_src, nps, &bars[(iter + 1) & 1], n);
+            issue_tile_load(d, gn, A.lam, nps + AMPS, &bars[(iter + 1) & 1], n);
+        }
+        for (int o = 0; o < d.op_count; ++o) {
+            int4 op = __ldg(ops + o);
+            if (op.x == OP_MAP) {
+                __syncthreads();
+                xwrite(ps, psi, tm);
+                xwrite(ls, lam, tm);
+                __syncthreads();
+                decode_map(d, op.y, op.z, op.w, tid, g.fixed_val, tm);
+                xread(ps, psi, tm);
+                xread(ls, lam, tm);
+            } else if (op.x == OP_GRAD) {
+                float gsum = grad_dispatch(op.y, psi, lam, op.z);
+                gacc[(op.w - d.grad_base) * NT + tid] = gsum;
+            } else if (op.x == OP_MAT && (op.w & OPF_GRAD)) {
+                int axis = (op.w >> 8) & 3;
+                int gslot = op.w >> 12;
+                float gsum = grad_dispatch(op.y, psi, lam, axis);
+                gacc[(gslot - d.grad_base) * NT + tid] = gsum;
+                float2 m[4];
+                load_slot(A, op.z, op.w, g.sample + tm.sample_off, m);
+                mat_dispatch(op.y, psi, m);
+                mat_dispatch(op.y, lam, m);
+            } else {
+                apply_op(op, psi, tm, A, g.sample + tm.sample_off, true);
+                apply_op(op, lam, tm, A, g.sample + tm.sample_off, true);
+            }
+        }
+        s_tsample[tid] = tm.sample_off;
+        __syncthreads();
+        // gradient partials of this tile: per sample when samples share the tile
+        if (d.ngrad > 0) {
+            const int nq = d.nq_tile;
+            const int spt = (nq < TB) ? (1 << (TB - nq)) : 1;
+            const int64_t tps = (n >= TB) ? (int64_t(1) << (n - TB)) : 1;
+            const int64_t units = (n >= TB) ? A.batch * tps : A.batch;
+            const int items = d.ngrad * spt;
+            const int warp = tid >> 5, lane = tid & 31;
+            for (int it = warp; it < items; it += NT / 32) {
+                int gi = it / spt, s = it % spt;
+                float acc = 0.f;
+                for (int c = lane; c < NT; c += 32)
+                    if (s_tsample[c] == s) acc += gacc[gi * NT + c];
+                for (int o2 = 16; o2 > 0; o2 >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o2);
+                if (lane == 0 && s < g.nsamples) {
+                    int64_t unit = (n >= TB) ? (g.sample * tps + g.tile_in_sample) : (g.sample + s);
+                    A.gradpart[(int64_t)(d.grad_base + gi) * units + unit] = acc;
+                }
+            }
+        }
+        // store psi and lambda (natural mapping)
+        if (d.epi & EPI_STORE) {
+#pragma unroll
+            for (int r = 0; r < 32; ++r) {
+                ps[nat_index(r, tid)] = psi[r];
+                ls[nat_index(r, tid)] = lam[r];
+            }
+            fence_proxy_async();
+            __syncthreads();
+            if (tid == 0) {
+                issue_tile_store(d, g, A.state, ps, n);
+                issue_tile_store(d, g, A.lam, ls, n);
+                bulk_commit();
+            }
+        } else if (store_lam_last) {
+#pragma unroll
+            for (int r = 0; r < 32; ++r) ls[nat_index(r, tid)] = lam[r];
+            fence_proxy_async();
+            __syncthreads();
+            if (tid == 0) {
+                issue_tile_store(d, g, A.lam, ls, n);
+                bulk_commit();
+            }
+        }
+        fence_proxy_async();
+        __syncthreads();
+    }
+    if (tid == 0) bulk_wait_all0();
+}
+
+// ------------------------------------------------------------ helpers --
+
+// Build the matrix tables: product of each slot's chain in row form.
+__global__ void k_build_mats(const SlotDesc* __restrict__ slots, const ChainEntry* __restrict__ chain, int nslots,
+                             int nshared, int nps, int64_t batch, const float* __restrict__ params,
+                             const float* __restrict__ named, int ncols, const float2* __restrict__ umats,
+                             float2* __restrict__ mats, float2* __restrict__ mats_ps) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    // items: shared slots once, per-sample slots once per sample
+    int64_t total = (int64_t)nslots * 1;  // slot index space
+    (void)total;
+    int64_t s_items = nshared;
+    int64_t p_items = (int64_t)nps * batch;
+    if (i >= s_items + p_items) return;
+    int slot_index;
+    int64_t b = 0;
+    bool per_sample;
+    if (i < s_items) {
+        slot_index = (int)i;
+        per_sample = false;
+    } else {
+        int64_t k = i - s_items;
+        b = k / nps;
+        slot_index = (int)(k % nps);
+        per_sample = true;
+    }
+    // find the slot with this out_index (slots are few; linear scan is fine)
+    const SlotDesc* sd = nullptr;
+    for (int s = 0; s < nslots; ++s)
+        if (slots[s].per_sample == (per_sample ? 1 : 0) && slots[s].out_index == slot_index) {
+            sd = &slots[s];
+            break;
+        }
+    if (!sd) return;
+    float2 m[4] = {make_float2(1.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(1.f, 0.f)};
+    for (int c = 0; c < sd->chain_len; ++c) {
+        ChainEntry e = chain[sd->chain_begin + c];
+        float2 g[4];
+        if (e.kind == 3) {
+            g[0] = umats[4 * e.idx];
+            g[1] = umats[4 * e.idx + 1];
+            g[2] = umats[4 * e.idx + 2];
+            g[3] = umats[4 * e.idx + 3];
+        } else {
+            float th = e.src == 0 ? params[e.idx] : named[b * ncols + e.idx];
+            rotation_row_matrix(e.kind, th, g);
+        }
+        if (e.dagger) dagger_row_matrix(g);
+        // m = m @ g
+        float2 r0 = cadd(cmul(m[0], g[0]), cmul(m[1], g[2]));
+        float2 r1 = cadd(cmul(m[0], g[1]), cmul(m[1], g[3]));
+        float2 r2 = cadd(cmul(m[2], g[0]), cmul(m[3], g[2]));
+        float2 r3 = cadd(cmul(m[2], g[1]), cmul(m[3], g[3]));
+        m[0] = r0;
+        m[1] = r1;
+        m[2] = r2;
+        m[3] = r3;
+    }
+    float2* dst = per_sample ? mats_ps + (b * nps + slot_index) * 4 : mats + (int64_t)slot_index * 4;
+    dst[0] = m[0];
+    dst[1] = m[1];
+    dst[2] = m[2];
+    dst[3] = m[3];
+}
+
+// Embedding factors R(x)|0> per sample and qubit; unlisted qubits keep |0>.
+__global__ void k_embed_fac(const EmbedDesc* __restrict__ ed, const float* __restrict__ named, int ncols,
+                            int64_t batch, int n, float2* __restrict__ fac) {
+    int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= batch) return;
+    EmbedDesc e = *ed;
+    float2* f = fac + b * n * 2;
+    for (int q = 0; q < n; ++q) {
+        f[2 * q] = make_float2(1.f, 0.f);
+        f[2 * q + 1] = make_float2(0.f, 0.f);
+    }
+    for (int j = 0; j < e.nq; ++j) {
+        int q = e.qubit[j];
+        float2 m[4];
+        rotation_row_matrix(e.axis, named[b * ncols + e.col0 + j], m);
+        float2 v0 = f[2 * q], v1 = f[2 * q + 1];
+        f[2 * q] = cadd(cmul(m[0], v0), cmul(m[2], v1));
+        f[2 * q + 1] = cadd(cmul(m[1], v0), cmul(m[3], v1));
+    }
+}
+
+// P0 / <Z> from the last pass's tile partials, in double, in tile order.
+__global__ void k_p0_finalize(const PassDesc* __restrict__ last, const float* __restrict__ part, float* out,
+                              int64_t batch, int n, int tb, int z) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= batch * n) return;
+    const PassDesc& d = *last;
+    int64_t b = i / n;
+    int q = (int)(i % n);
+    int gb = n - 1 - q;
+    int local = -1, fixed_k = -1;
+    for (int j = 0; j < d.nq_tile; ++j)
+        if (d.gbit[j] == gb) local = j;
+    for (int k = 0; k < d.nfixed; ++k)
+        if (d.fixed_gbit[k] == gb) fixed_k = k;
+    int64_t tps = (n >= tb) ? (int64_t(1) << (n - tb)) : 1;
+    const float* p = part + b * tps * (tb + 1);
+    double p0 = 0.0, tot = 0.0;
+    for (int64_t t = 0; t < tps; ++t) {
+        const float* row = p + t * (tb + 1);
+        tot += row[tb];
+        if (local >= 0)
+            p0 += row[local];
+        else if (fixed_k >= 0 && !((t >> fixed_k) & 1))
+            p0 += row[tb];
+    }
+    out[i] = z ? (float)(2.0 * p0 - tot) : (float)p0;
+}
+
+// lambda = dL/dpsi* from the upstream gradient of the measured output.
+__global__ void k_seed(const float2* __restrict__ psi, const void* __restrict__ gout, float2* __restrict__ lam,
+                       int64_t total, int n, int measure) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    float2 a = psi[i];
+    if (measure == QG_MEASURE_P0 || measure == QG_MEASURE_Z) {
+        int64_t b = i >> n;
+        uint32_t k = (uint32_t)(i & ((int64_t(1) << n) - 1));
+        const float* g = reinterpret_cast<const float*>(gout) + b * n;
+        float w = 0.f;
+        for (int q = 0; q < n; ++q) {
+            bool zero = !((k >> (n - 1 - q)) & 1);
+            w += measure == QG_MEASURE_Z ? (zero ? g[q] : -g[q]) : (zero ? g[q] : 0.f);
+        }
+        lam[i] = make_float2(w * a.x, w * a.y);
+    } else if (measure == QG_MEASURE_PROBS) {
+        float w = reinterpret_cast<const float*>(gout)[i];
+        lam[i] = make_float2(w * a.x, w * a.y);
+    } else {
+        float2 g = reinterpret_cast<const float2*>(gout)[i];
+        lam[i] = make_float2(0.5f * g.x, 0.5f * g.y);
+    }
+}
+
+// Reduce gradient partials per target in double, in a fixed order.
+__global__ void k_grad_finalize(const int32_t* __restrict__ pcsr, int nparams, const int32_t* __restrict__ ccsr,
+                                int ncols, const float* __restrict__ part, int64_t units, int64_t batch,
+                                int64_t tps, float* __restrict__ dparams, float* __restrict__ dnamed) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < nparams) {
+        double acc = 0.0;
+        for (int k = pcsr[i]; k < pcsr[i + 1]; ++k) {
+            int gs = pcsr[nparams + 1 + k];
+            const float* p = part + (int64_t)gs * units;
+            for (int64_t u = 0; u < units; ++u) acc += p[u];
+        }
+        if (dparams) dparams[i] = (float)acc;
+        return;
+    }
+    i -= nparams;
+    if (i >= (int64_t)ncols * batch) return;
+    int64_t b = i / ncols;
+    int c = (int)(i % ncols);
+    double acc = 0.0;
+    for (int k = ccsr[c]; k < ccsr[c + 1]; ++k) {
+        int gs = ccsr[ncols + 1 + k];
+        const float* p = part + (int64_t)gs * units + b * tps;
+        for (int64_t u = 0; u < tps; ++u) acc += p[u];
+    }
+    if (dnamed) dnamed[b * ncols + c] = (float)acc;
+}
+
+__global__ void k_scale2(const float2* __restrict__ lam, float2* __restrict__ out, int64_t total) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < total) out[i] = make_float2(2.f * lam[i].x, 2.f * lam[i].y);
+}
+
+}  // namespace qg
+
+// ---------------------------------------------------------- host side --
+
+namespace qg {
+
+static int sm_count() {
+    static int cached = 0;
+    if (!cached) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev);
+        if (cached <= 0) cached = 1;
+    }
+    return cached;
+}
+
+static size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct FwdLayout {
+    size_t status, mats, mats_ps, embfac, p0part, total;
+};
+struct BwdLayout {
+    size_t status, mats, mats_ps, gradpart, total;
+    int64_t units, tps;
+};
+
+static FwdLayout fwd_layout(const ProgramRun& R, int64_t B) {
+    FwdLayout L;
+    size_t o = 0;
+    L.status = o;
+    o = al(o + 16);
+    L.mats = o;
+    o = al(o + (size_t)R.f_shared * 32);
+    L.mats_ps = o;
+    o = al(o + (size_t)B * R.f_ps * 32);
+    L.embfac = o;
+    o = al(o + (R.has_embed ? (size_t)B * R.n * 16 : 0));
+    L.p0part = o;
+    int tb = R.tile_bits;
+    int64_t tps = R.n >= tb ? (int64_t(1) << (R.n - tb)) : 1;
+    bool p0 = R.measure == QG_MEASURE_P0 || R.measure == QG_MEASURE_Z;
+    o = al(o + (p0 ? (size_t)B * tps * (tb + 1) * 4 : 0));
+    L.total = o;
+    return L;
+}
+
+static BwdLayout bwd_layout(const ProgramRun& R, int64_t B) {
+    BwdLayout L;
+    size_t o = 0;
+    L.status = o;
+    o = al(o + 16);
+    L.mats = o;
+    o = al(o + (size_t)R.b_shared * 32);
+    L.mats_ps = o;
+    o = al(o + (size_t)B * R.b_ps * 32);
+    int tb = R.tile_bits - 1;
+    L.tps = R.n >= tb ? (int64_t(1) << (R.n - tb)) : 1;
+    L.units = R.n >= tb ? B * L.tps : B;
+    L.gradpart = o;
+    o = al(o + (size_t)R.ngrads * L.units * 4);
+    L.total = o;
+    return L;
+}
+
+template <int TB>
+static int launch_fwd_pass(const PassDesc* dpass, const int4* dops, int p, const RunArgs& A, int zero_init,
+                           const EmbedDesc* demb, int64_t tiles, cudaStream_t st) {
+    constexpr int NT = 1 << (TB - 5);
+    size_t smem = 2 * (size_t(1) << TB) * sizeof(float2);
+    static bool attr_set = false;
+    if (!attr_set) {
+        QG_CUDA_TRY(cudaFuncSetAttribute(k_fwd_pass<TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_set = true;
+    }
+    int64_t grid = tiles < sm_count() ? tiles : sm_count();
+    k_fwd_pass<TB><<<(unsigned)grid, NT, smem, st>>>(dpass, dops, p, A, zero_init, demb, tiles);
+    QG_LAUNCH_CHECK();
+    return QG_OK;
+}
+
+template <int TB>
+static int launch_bwd_pass(const PassDesc* dpass, const int4* dops, int p, const RunArgs& A, int store_lam,
+                           int64_t tiles, cudaStream_t st) {
+    constexpr int NT = 1 << (TB - 5);
+    size_t smem = 4 * (size_t(1) << TB) * sizeof(float2) + (size_t)kMaxGradPerPass * NT * sizeof(float);
+    static bool attr_set = false;
+    if (!attr_set) {
+        QG_CUDA_TRY(cudaFuncSetAttribute(k_bwd_pass<TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_set = true;
+    }
+    int64_t grid = tiles < sm_count() ? tiles : sm_count();
+    k_bwd_pass<TB><<<(unsigned)grid, NT, smem, st>>>(dpass, dops, p, A, store_lam, tiles);
+    QG_LAUNCH_CHECK();
+    return QG_OK;
+}
+
+static int64_t num_tiles(int n, int tb, int64_t B) {
+    if (n >= tb) return B << (n - tb);
+    int64_t spt = int64_t(1) << (tb - n);
+    return (B + spt - 1) / spt;
+}
+
+}  // namespace qg
+
+extern "C" {
+
+int64_t qg_program_workspace_bytes(const qg_program* prog, int64_t batch, int backward) {
+    if (!prog || batch < 1) return -1;
+    qg::ProgramRun R;
+    qg::program_run_info(prog, &R);
+    return backward ? (int64_t)qg::bwd_layout(R, batch).total : (int64_t)qg::fwd_layout(R, batch).total;
+}
+
+int qg_program_forward(const qg_program* prog, const void* dev_table, void* workspace, int64_t workspace_bytes,
+                       void* state, int64_t batch, int zero_init, const float* params, const float* named,
+                       const void* umats, float* out, void* ckpt, void* stream) {
+    using namespace qg;
+    QG_CHECK_ARG(prog && dev_table && workspace && state, "null pointer");
+    QG_CHECK_ARG(batch >= 1, "batch must be >= 1");
+    QG_CHECK_ARG(((uintptr_t)state & 15) == 0, "state must be 16-byte aligned");
+    ProgramRun R;
+    program_run_info(prog, &R);
+    FwdLayout L = fwd_layout(R, batch);
+    QG_CHECK_ARG(workspace_bytes >= (int64_t)L.total, "workspace too small");
+    QG_CHECK_ARG(R.nparams == 0 || params, "params is null");
+    QG_CHECK_ARG(R.ncols == 0 || named, "named inputs are null");
+    QG_CHECK_ARG(R.numats == 0 || umats, "umats is null");
+    bool p0 = R.measure == QG_MEASURE_P0 || R.measure == QG_MEASURE_Z;
+    QG_CHECK_ARG(!(p0 || R.measure == QG_MEASURE_PROBS) || out, "out is null");
+    QG_CHECK_ARG(R.segments <= 1 || ckpt, "checkpoint buffer is null");
+    QG_CHECK_ARG(!out || ((uintptr_t)out & 15) == 0, "out must be 16-byte aligned");
+    cudaStream_t st = (cudaStream_t)stream;
+    char* ws = (char*)workspace;
+    const char* tab = (const char*)dev_table;
+    RunArgs A{};
+    A.state = (float2*)state;
+    A.ckpt = (float2*)ckpt;
+    A.out = out;
+    A.p0part = (float*)(ws + L.p0part);
+    A.mats = (const float2*)(ws + L.mats);
+    A.mats_ps = (const float2*)(ws + L.mats_ps);
+    A.embfac = (const float2*)(ws + L.embfac);
+    A.status = (int*)(ws + L.status);
+    A.batch = batch;
+    A.n = R.n;
+    A.nslots_ps = R.f_ps;
+    QG_CUDA_TRY(cudaMemsetAsync(ws + L.status, 0, 16, st));
+    int64_t items = R.f_shared + (int64_t)R.f_ps * batch;
+    if (items > 0) {
+        k_build_mats<<<grid_for(items, 128), 128, 0, st>>>(
+            (const SlotDesc*)(tab + R.off_fslot), (const ChainEntry*)(tab + R.off_fchain), R.nfslots, R.f_shared,
+            R.f_ps, batch, params, named, R.ncols, (const float2*)umats, (float2*)(ws + L.mats),
+            (float2*)(ws + L.mats_ps));
+        QG_LAUNCH_CHECK();
+    }
+    if (R.has_embed) {
+        k_embed_fac<<<grid_for(batch, 128), 128, 0, st>>>((const EmbedDesc*)(tab + R.off_embed), named, R.ncols,
+                                                         batch, R.n, (float2*)(ws + L.embfac));
+        QG_LAUNCH_CHECK();
+    }
+    const PassDesc* dpass = (const PassDesc*)(tab + R.off_fpass);
+    const int4* dops = (const int4*)(tab + R.off_fops);
+    const EmbedDesc* demb = (const EmbedDesc*)(tab + R.off_embed);
+    int64_t tiles = num_tiles(R.n, R.tile_bits, batch);
+    for (int p = 0; p < R.nfpass; ++p) {
+        int zi = (p == 0) ? zero_init : 0;
+        int rc;
+        switch (R.tile_bits) {
+            case 13: rc = launch_fwd_pass<13>(dpass, dops, p, A, zi, demb, tiles, st); break;
+            case 12: rc = launch_fwd_pass<12>(dpass, dops, p, A, zi, demb, tiles, st); break;
+            default: rc = launch_fwd_pass<11>(dpass, dops, p, A, zi, demb, tiles, st); break;
+        }
+        if (rc) return rc;
+    }
+    if (p0) {
+        k_p0_finalize<<<grid_for(batch * R.n, 128), 128, 0, st>>>(dpass + (R.nfpass - 1), A.p0part, out, batch, R.n,
+                                                                  R.tile_bits, R.measure == QG_MEASURE_Z);
+        QG_LAUNCH_CHECK();
+    }
+    return QG_OK;
+}
+
+int qg_program_backward(const qg_program* prog, const void* dev_table, void* workspace, int64_t workspace_bytes,
+                        void* state, void* lam, int64_t batch, const float* params, const float* named,
+                        const void* umats, const void* grad_out, float* dparams, float* dnamed, void* dstate,
+                        const void* ckpt, void* stream) {
+    using namespace qg;
+    QG_CHECK_ARG(prog && dev_table && workspace && state && lam && grad_out, "null pointer");
+    QG_CHECK_ARG(batch >= 1, "batch must be >= 1");
+    QG_CHECK_ARG(((uintptr_t)state & 15) == 0 && ((uintptr_t)lam & 15) == 0, "state / lam must be 16-byte aligned");
+    ProgramRun R;
+    program_run_info(prog, &R);
+    BwdLayout L = bwd_layout(R, batch);
+    QG_CHECK_ARG(workspace_bytes >= (int64_t)L.total, "workspace too small");
+    QG_CHECK_ARG(R.segments <= 1 || ckpt, "checkpoint buffer is null");
+    cudaStream_t st = (cudaStream_t)stream;
+    char* ws = (char*)workspace;
+    const char* tab = (const char*)dev_table;
+    RunArgs A{};
+    A.state = (float2*)state;
+    A.lam = (float2*)lam;
+    A.ckpt = (float2*)ckpt;
+    A.gradpart = (float*)(ws + L.gradpart);
+    A.mats = (const float2*)(ws + L.mats);
+    A.mats_ps = (const float2*)(ws + L.mats_ps);
+    A.status = (int*)(ws + L.status);
+    A.batch = batch;
+    A.n = R.n;
+    A.nslots_ps = R.b_ps;
+    QG_CUDA_TRY(cudaMemsetAsync(ws + L.status, 0, 16, st));
+    int64_t items = R.b_shared + (int64_t)R.b_ps * batch;
+    if (items > 0) {
+        k_build_mats<<<grid_for(items, 128), 128, 0, st>>>(
+            (const SlotDesc*)(tab + R.off_bslot), (const ChainEntry*)(tab + R.off_bchain), R.nbslots, R.b_shared,
+            R.b_ps, batch, params, named, R.ncols, (const float2*)umats, (float2*)(ws + L.mats),
+            (float2*)(ws + L.mats_ps));
+        QG_LAUNCH_CHECK();
+    }
+    int64_t total = batch << R.n;
+    k_seed<<<grid_for(total, 256), 256, 0, st>>>((const float2*)state, grad_out, (float2*)lam, total, R.n,
+                                                 R.measure);
+    QG_LAUNCH_CHECK();
+    if (R.ngrads > 0) QG_CUDA_TRY(cudaMemsetAsync(A.gradpart, 0, (size_t)R.ngrads * L.units * 4, st));
+    const PassDesc* dpass = (const PassDesc*)(tab + R.off_bpass);
+    const int4* dops = (const int4*)(tab + R.off_bops);
+    int tb = R.tile_bits - 1;
+    int64_t tiles = num_tiles(R.n, tb, batch);
+    for (int p = 0; p < R.nbpass; ++p) {
+        int store_lam = (p + 1 == R.nbpass) && dstate != nullptr;
+        int rc;
+        switch (tb) {
+            case 12: rc = launch_bwd_pass<12>(dpass, dops, p, A, store_lam, tiles, st); break;
+            case 11: rc = launch_bwd_pass<11>(dpass, dops, p, A, store_lam, tiles, st); break;
+            default: rc = launch_bwd_pass<10>(dpass, dops, p, A, store_lam, tiles, st); break;
+        }
+        if (rc) return rc;
+    }
+    int64_t fitems = R.nparams + (int64_t)R.ncols * batch;
+    if (fitems > 0) {
+        k_grad_finalize<<<grid_for(fitems, 128), 128, 0, st>>>(
+            (const int32_t*)(tab + R.off_pcsr), R.nparams, (const int32_t*)(tab + R.off_ccsr), R.ncols, A.gradpart,
+            L.units, batch, (R.n >= tb ? L.tps : 1), dparams, dnamed);
+        QG_LAUNCH_CHECK();
+    }
+    if (dstate) {
+        k_scale2<<<grid_for(total, 256), 256, 0, st>>>((const float2*)lam, (float2*)dstate, total);
+        QG_LAUNCH_CHECK();
+    }
+    return QG_OK;
+}
+
+}  // extern "C"

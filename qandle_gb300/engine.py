@@ -1,0 +1,375 @@
+"""Fused engine: lowering of built layers to a gate program, and the
+autograd Function that runs it forward (fused passes) and backward (adjoint).
+
+The lowering reads the same attributes the reference's built modules carry
+(qandle/operators.py:215-238 BuiltParametrizedOperator .qubit/.theta/
+.remapping/.named/.name, :87-104 BuiltU .qubit/.original_matrix, :536-545
+BuiltCNOT .c/.t, :570-579 BuiltCZ, :653-659 BuiltSWAP .a/.b,
+embeddings.py:114-137 AngleEmbeddingBuilt .qubits/.rotation/.name,
+measurements.py:73-123), so a circuit of either qandle's or this package's
+layer classes lowers the same way.  Unknown layers raise: there is no silent
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_AXIS = {"BuiltRX": 0, "BuiltRY": 1, "BuiltRZ": 2}
+_MEAS = {"MeasureProbabilityBuilt": "p0", "MeasureAllAbsolute": "probs", "MeasureState": "state",
+         "MeasureExpectationZBuilt": "z"}
+_ROT = {"x": 0, "y": 1, "z": 2}
+
+
+def _rot_axis(rotation: str) -> int:
+    r = rotation.lower().replace("r", "")
+    if r not in _ROT:
+        raise ValueError(f"Unknown rotation {rotation}")
+    return _ROT[r]
+
+
+class Lowered:
+    """Gate records plus where each runtime value comes from."""
+
+    def __init__(self, num_qubits: int):
+        self.n = num_qubits
+        self.gates: list[tuple] = []
+        self.qlist: list[int] = []
+        self.param_mods: list = []        # modules whose remapped theta feeds params[i]
+        self.named_cols: list[tuple] = []  # (kwarg name, column or None)
+        self.umats: list[torch.Tensor] = []
+        self.measure = "state"
+
+    def add_layer(self, mod) -> None:
+        name = type(mod).__name__
+        if self.measure != "state" or getattr(self, "_measured", False):
+            raise ValueError("layers after a measurement are not supported by the fused engine")
+        if name in _AXIS:
+            if mod.named:
+                self.gates.append((_AXIS[name], mod.qubit, 0, 1, len(self.named_cols), 0))
+                self.named_cols.append((mod.name, None))
+            else:
+                self.gates.append((_AXIS[name], mod.qubit, 0, 0, len(self.param_mods), 0))
+                self.param_mods.append(mod)
+        elif name == "BuiltU":
+            m = torch.as_tensor(mod.original_matrix).to(torch.complex64).reshape(2, 2)
+            diag = bool(m[0, 1] == 0 and m[1, 0] == 0)
+            self.gates.append((_lib.GATE["u"], mod.qubit, 0, 0, len(self.umats), 1 if diag else 0))
+            self.umats.append(m)
+        elif name == "BuiltCNOT":
+            self.gates.append((_lib.GATE["cnot"], mod.c, mod.t, 0, 0, 0))
+        elif name == "BuiltCZ":
+            self.gates.append((_lib.GATE["cz"], mod.c, mod.t, 0, 0, 0))
+        elif name == "BuiltSWAP":
+            self.gates.append((_lib.GATE["swap"], mod.a, mod.b, 0, 0, 0))
+        elif name == "AngleEmbeddingBuilt":
+            qs = list(mod.qubits)
+            self.gates.append((_lib.GATE["emb"], _rot_axis(mod.rotation), len(qs), 1,
+                               len(self.named_cols), len(self.qlist)))
+            for j in range(len(qs)):
+                self.named_cols.append((mod.name, j))
+            self.qlist.extend(qs)
+        elif name in _MEAS:
+            self.measure = _MEAS[name]
+            self._measured = True
+        elif hasattr(mod, "mods"):  # StronglyEntanglingLayerBuilt and other built ansaetze
+            for m in mod.mods:
+                self.add_layer(m)
+        elif hasattr(mod, "layers") and hasattr(mod, "num_qubits"):
+            for m in mod.layers:
+                self.add_layer(m)
+        else:
+            raise ValueError(f"the fused engine cannot lower layer {name}")
+
+
+def lower(circuit) -> Lowered:
+    """Lower an UnsplittedCircuit (qandle's or this package's)."""
+    lo = Lowered(circuit.num_qubits)
+    for mod in circuit.layers:
+        lo.add_layer(mod)
+    return lo
+
+
+class Program:
+    """A planned gate program: host handle plus device copies of its tables."""
+
+    def __init__(self, lowered: Lowered, measure: str, keep_state: bool, tile_bits: int = 13,
+                 low_bits: int = 6, max_high: int = 0, segments: int = 1):
+        lib = _lib.load()
+        self.n = lowered.n
+        self.measure = measure
+        self.keep_state = keep_state
+        gates = (_lib.Gate * max(1, len(lowered.gates)))()
+        for i, g in enumerate(lowered.gates):
+            gates[i] = _lib.Gate(*g)
+        ql = (ctypes.c_int32 * max(1, len(lowered.qlist)))(*lowered.qlist)
+        opt = _lib.PlanOptions()
+        lib.qg_plan_options_default(ctypes.byref(opt))
+        opt.tile_bits, opt.low_bits, opt.max_high = tile_bits, low_bits, max_high
+        opt.measure = _lib.MEASURE[measure]
+        opt.keep_state = 1 if keep_state else 0
+        opt.segments = segments
+        handle = ctypes.c_void_p()
+        _lib.check(lib.qg_program_create(gates, len(lowered.gates), ctypes.cast(ql, ctypes.c_void_p),
+                                         self.n, ctypes.byref(opt), ctypes.byref(handle)))
+        self.handle = handle
+        self.info = _lib.ProgramInfo()
+        _lib.check(lib.qg_program_info(self.handle, ctypes.byref(self.info)))
+        host = (ctypes.c_uint8 * self.info.table_bytes)()
+        _lib.check(lib.qg_program_table(self.handle, host, self.info.table_bytes))
+        self._table_host = torch.frombuffer(bytearray(host), dtype=torch.uint8)
+        self._tables = {}
+        self._lock = threading.Lock()
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().qg_program_destroy(h)
+            except Exception:
+                pass
+
+    def table(self, device) -> torch.Tensor:
+        key = str(device)
+        with self._lock:
+            t = self._tables.get(key)
+            if t is None:
+                t = self._table_host.to(device)
+                self._tables[key] = t
+            return t
+
+    def summary(self) -> str:
+        return self.info.summary.decode()
+
+    def passes(self, backward: bool = False):
+        """Planned passes as dicts (introspection and CPU tests)."""
+        lib = _lib.load()
+        out = []
+        count = self.info.backward_passes if backward else self.info.forward_passes
+        for i in range(count):
+            pi = _lib.PassInfo()
+            _lib.check(lib.qg_program_pass(self.handle, 1 if backward else 0, i, ctypes.byref(pi)))
+            ops = np.ctypeslib.as_array(pi.ops, shape=(pi.op_count * 4,)).reshape(-1, 4).copy() \
+                if pi.op_count else np.zeros((0, 4), np.int32)
+            out.append({
+                "tile_bits": pi.tile_bits, "nq_tile": pi.nq_tile, "run_bits": pi.run_bits,
+                "gbit": list(pi.gbit[:pi.nq_tile]), "fixed_gbit": list(pi.fixed_gbit[:pi.nfixed]),
+                "ops": ops, "init": pi.init, "epi": pi.epi, "init_map": list(pi.init_map),
+                "ckpt": pi.ckpt, "psi_from_ckpt": pi.psi_from_ckpt, "grad_base": pi.grad_base,
+                "ngrad": pi.ngrad})
+        return out
+
+    def slots(self, backward: bool = False):
+        """Matrix slots: list of (per_sample, table_index, [(kind, src, idx, dagger), ...])."""
+        lib = _lib.load()
+        size = lib.qg_program_slots(self.handle, 1 if backward else 0, None, 0)
+        buf = (ctypes.c_int32 * max(1, size))()
+        lib.qg_program_slots(self.handle, 1 if backward else 0, ctypes.cast(buf, ctypes.c_void_p), size)
+        v, out, i = list(buf)[:size], [], 0
+        while i < size:
+            ps, ti, cl = v[i], v[i + 1], v[i + 2]
+            chain = [tuple(v[i + 3 + 4 * k: i + 7 + 4 * k]) for k in range(cl)]
+            out.append((ps, ti, chain))
+            i += 3 + 4 * cl
+        return out
+
+    def grad_targets(self):
+        """Backward gradient slots as (src, idx): src 0 = params, 1 = named column."""
+        lib = _lib.load()
+        count = lib.qg_program_grad_targets(self.handle, None, 0)
+        buf = (ctypes.c_int32 * max(1, 2 * count))()
+        lib.qg_program_grad_targets(self.handle, ctypes.cast(buf, ctypes.c_void_p), 2 * count)
+        return [(buf[2 * i], buf[2 * i + 1]) for i in range(count)]
+
+    def workspace(self, batch: int, backward: bool, device) -> torch.Tensor:
+        nb = _lib.load().qg_program_workspace_bytes(self.handle, batch, 1 if backward else 0)
+        if nb < 0:
+            raise RuntimeError("invalid workspace query")
+        return torch.empty(max(int(nb), 256), dtype=torch.uint8, device=device)
+
+
+class _Inputs:
+    """Runtime values of one call, gathered on the device."""
+
+    def __init__(self, lo: Lowered, state, kwargs, device):
+        sizes = []
+        if state is not None and state.dim() == 2:
+            sizes.append(state.shape[0])
+        cols = []
+        for name, j in lo.named_cols:
+            if name not in kwargs:
+                raise KeyError(f"missing named input {name!r}")
+            v = torch.as_tensor(kwargs[name])
+            v = v.to(device=device, dtype=torch.float32)
+            if j is not None:
+                v = v[..., j]
+            if v.dim() > 1:
+                raise ValueError(f"named input {name!r} must be a scalar or [batch] per gate")
+            if v.dim() == 1:
+                sizes.append(v.shape[0])
+            cols.append(v)
+        big = [s for s in sizes if s != 1]
+        if big and any(s != big[0] for s in big):
+            raise ValueError(f"inconsistent batch sizes {sizes}")
+        self.batch = big[0] if big else (1 if not sizes else sizes[0])
+        self.unbatched = not sizes
+        if cols:
+            self.named = torch.stack([c.reshape(-1).expand(self.batch) for c in cols], 1).contiguous()
+        else:
+            self.named = torch.zeros(1, 1, dtype=torch.float32, device=device)
+        if lo.param_mods:
+            self.params = torch.cat([m.remapping(m.theta).reshape(-1)[:1].to(device=device, dtype=torch.float32)
+                                     for m in lo.param_mods]).contiguous()
+        else:
+            self.params = torch.zeros(1, dtype=torch.float32, device=device)
+        if lo.umats:
+            self.umats = torch.stack([u.to(device) for u in lo.umats]).contiguous()
+        else:
+            self.umats = torch.zeros(1, 2, 2, dtype=torch.complex64, device=device)
+
+
+def _out_shape(measure, out, n, unbatched):
+    if measure in ("p0", "z"):
+        return out.transpose(0, 1).squeeze().transpose(-1, 0)
+    if unbatched:
+        return out.reshape(1 << n)
+    return out
+
+
+class _FusedRun(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, ex, state_in, params, named, umats, batch, zero_init):
+        prog = ex.program(training=torch.is_grad_enabled() and any(
+            t is not None and t.requires_grad for t in (state_in, params, named)))
+        return ex.run_forward(ctx, prog, state_in, params, named, umats, batch, zero_init)
+
+    @staticmethod
+    def backward(ctx, gout):
+        return ctx.ex.run_backward(ctx, gout)
+
+
+class FusedExecutor:
+    """Runs a built circuit through the fused engine (used by Circuit)."""
+
+    def __init__(self, circuit, tile_bits: int = 13, low_bits: int = 6, max_high: int = 0,
+                 checkpoint_segments: int = 1):
+        self.circuit = circuit
+        self.n = circuit.num_qubits
+        self.lowered = lower(circuit)
+        self.options = dict(tile_bits=tile_bits, low_bits=low_bits, max_high=max_high)
+        self.checkpoint_segments = checkpoint_segments
+        self._programs = {}
+
+    def program(self, training: bool) -> Program:
+        key = bool(training)
+        p = self._programs.get(key)
+        if p is None:
+            p = Program(self.lowered, self.lowered.measure, keep_state=key,
+                        segments=self.checkpoint_segments if key else 1, **self.options)
+            self._programs[key] = p
+        return p
+
+    def __call__(self, state=None, **kwargs):
+        if self.n < 5:
+            # the fused tile needs five qubits in registers; tiny circuits run the per-gate kernels
+            return self.circuit.forward(state, **kwargs)
+        dev = state.device if state is not None else self._device(kwargs)
+        if dev.type != "cuda":
+            raise RuntimeError("qandle_gb300 runs on CUDA tensors only; move the circuit and its inputs "
+                               "with .to('cuda')")
+        if state is not None:
+            _lib.require_cuda_state(state)
+        inp = _Inputs(self.lowered, state, kwargs, dev)
+        zero_init = 1 if (state is None and not self._has_embedding()) else 0
+        out = _FusedRun.apply(self, state, inp.params, inp.named, inp.umats, inp.batch, zero_init)
+        return _out_shape(self.lowered.measure, out, self.n, inp.unbatched)
+
+    def _has_embedding(self) -> bool:
+        return any(g[0] == _lib.GATE["emb"] for g in self.lowered.gates)
+
+    def _device(self, kwargs):
+        for v in kwargs.values():
+            if isinstance(v, torch.Tensor):
+                return v.device
+        buf = getattr(self.circuit, "state", None)
+        if isinstance(buf, torch.Tensor):
+            return buf.device
+        return torch.device("cpu")
+
+    # -- forward / backward bodies (called from the autograd Function) --
+
+    def run_forward(self, ctx, prog: Program, state_in, params, named, umats, batch, zero_init):
+        n = self.n
+        dev = params.device
+        B = batch
+        if state_in is not None and not prog.info.has_embedding:
+            st = state_in.reshape(-1, 1 << n)
+            st = (st.expand(B, -1) if st.shape[0] == 1 and B > 1 else st).contiguous().clone()
+        else:
+            st = torch.empty(B, 1 << n, dtype=torch.complex64, device=dev)
+        m = prog.measure
+        if m in ("p0", "z"):
+            out = torch.empty(B, n, dtype=torch.float32, device=dev)
+        elif m == "probs":
+            out = torch.empty(B, 1 << n, dtype=torch.float32, device=dev)
+        else:
+            out = None
+        ckpt = None
+        if prog.info.segments > 1:
+            ckpt = torch.empty(prog.info.segments - 1, B, 1 << n, dtype=torch.complex64, device=dev)
+        ws = prog.workspace(B, False, dev)
+        _lib.call("qg_program_forward", prog.handle, prog.table(dev).data_ptr(), ws.data_ptr(), ws.numel(),
+                  st.data_ptr(), B, zero_init, params.data_ptr(), named.data_ptr(), umats.data_ptr(),
+                  _lib.ptr(out), _lib.ptr(ckpt), _lib.stream())
+        ctx.ex = self
+        ctx.prog = prog
+        ctx.batch = B
+        ctx.state_shape = None if state_in is None else state_in.shape
+        if prog.keep_state:
+            ctx.save_for_backward(st, params, named, umats)
+            ctx.ckpt = ckpt
+        result = st if out is None else out
+        return result
+
+    def run_backward(self, ctx, gout):
+        prog: Program = ctx.prog
+        if not prog.keep_state:
+            raise RuntimeError("the fused forward ran without gradient tracking")
+        st, params, named, umats = ctx.saved_tensors
+        if getattr(ctx, "_consumed", False):
+            raise RuntimeError("the fused engine's backward can run once per forward "
+                               "(retain_graph is not supported)")
+        ctx._consumed = True
+        n, B, dev = self.n, ctx.batch, st.device
+        m = prog.measure
+        if m in ("p0", "z", "probs"):
+            g = gout.to(torch.float32).reshape(B, -1).contiguous()
+        else:
+            g = gout.to(torch.complex64).reshape(B, 1 << n).contiguous()
+        lam = torch.empty_like(st)
+        ws = prog.workspace(B, True, dev)
+        dparams = torch.empty(max(1, prog.info.nparams), dtype=torch.float32, device=dev)
+        dnamed = torch.empty(B, max(1, prog.info.ncols), dtype=torch.float32, device=dev)
+        need_state = ctx.needs_input_grad[1] and not prog.info.has_embedding
+        dstate = torch.empty_like(st) if need_state else None
+        _lib.call("qg_program_backward", prog.handle, prog.table(dev).data_ptr(), ws.data_ptr(), ws.numel(),
+                  st.data_ptr(), lam.data_ptr(), B, params.data_ptr(), named.data_ptr(), umats.data_ptr(),
+                  g.data_ptr(), dparams.data_ptr(), dnamed.data_ptr(), _lib.ptr(dstate),
+                  _lib.ptr(ctx.ckpt), _lib.stream())
+        gstate = None
+        if need_state:
+            shp = ctx.state_shape
+            gstate = dstate
+            if len(shp) == 1:
+                gstate = dstate.sum(0)
+            elif shp[0] != B:
+                gstate = dstate.sum(0, keepdim=True)
+            gstate = gstate.reshape(shp)
+        gp = dparams[:params.numel()] if ctx.needs_input_grad[2] else None
+        gn = dnamed[:, :named.shape[1]].reshape(named.shape) if (ctx.needs_input_grad[3] and named.dim() == 2) else None
+        return None, gstate, gp, gn, None, None, None

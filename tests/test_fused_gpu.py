@@ -1,0 +1,168 @@
+"""Fused engine on the GPU against the reference's golden vectors and the
+complex128 oracle: forward (every measurement kind, several tile shapes,
+n below and above the tile size, partial tiles) and the adjoint backward
+(shared angles, named inputs, embedding inputs, input-state gradient,
+checkpoint segments)."""
+import numpy as np
+import pytest
+import torch
+
+import qandle_gb300 as q
+from oracle import oracle
+from qandle_gb300 import workloads
+from tests import golden_io
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5    # max-abs on probabilities / P0 / <Z> / amplitudes
+GTOL = 1e-4   # max-abs on gradients (sums over up to 2^n * batch terms in float32)
+
+
+def _run(desc, dev, engine="fused", state=None, **opt):
+    circ = workloads.build_circuit(desc, engine=engine, **opt).to(dev)
+    kw = workloads.circuit_inputs(desc, dev)
+    with torch.no_grad():
+        out = circ(state, **kw) if state is not None else circ(**kw)
+    return out.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("name", ["plain_small", "sel_small", "deep_small"])
+def test_fused_vs_reference_golden(cuda_device, name):
+    z = golden_io.load("circuits")
+    desc = golden_io.circuit_desc(z, name)
+    if desc["measure"] == "z":
+        desc["measure"] = "p0"
+    st = None
+    if name == "deep_small":
+        st = torch.zeros(desc["batch"], 1 << desc["n"], dtype=torch.complex64, device=cuda_device)
+        st[:, 0] = 1
+    out = _run(desc, cuda_device, state=st)
+    ref = z[f"{name}_out"]
+    assert out.shape == ref.shape
+    assert np.abs(out - ref).max() < TOL
+
+
+CASES = {
+    "sel_n10": lambda: workloads.sel_reupload(n=10, batch=37, layers=3, reupload_every=2),
+    "sel_n14": lambda: workloads.sel_reupload(n=14, batch=3, layers=4, reupload_every=2),
+    "sel_n16": lambda: workloads.sel_reupload(n=16, batch=2, layers=3, reupload_every=2, measure="p0"),
+    "brick_n15": lambda: workloads.adjoint_brick(n=15, batch=3, layers=6),
+    "deep_n15": lambda: workloads.deep_u(n=15, batch=2, layers=5),
+    "plain_n5": lambda: workloads.plain_small(n=5, batch=300, layers=3),
+    "plain_n8": lambda: workloads.plain_small(n=8, batch=64, layers=4),
+    "plain_n12": lambda: workloads.plain_small(n=12, batch=5, layers=3),
+}
+OPTS = [dict(), dict(tile_bits=12, low_bits=4, max_high=2), dict(tile_bits=11, low_bits=5, max_high=1),
+        dict(tile_bits=13, low_bits=7, max_high=6)]
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("oi", range(len(OPTS)))
+def test_fused_forward_vs_oracle(cuda_device, case, oi):
+    desc = CASES[case]()
+    out = _run(desc, cuda_device, **OPTS[oi])
+    ref = oracle.forward(desc)
+    assert out.shape == ref.shape
+    err = np.abs(out - ref).max()
+    assert err < TOL, (case, OPTS[oi], err)
+
+
+@pytest.mark.parametrize("measure", ["state", "probs", "p0", "z"])
+def test_fused_measure_kinds(cuda_device, measure):
+    desc = workloads.sel_reupload(n=14, batch=3, layers=2, reupload_every=2, measure=measure)
+    out = _run(desc, cuda_device)
+    ref = oracle.forward(desc)
+    assert out.shape == ref.shape
+    assert np.abs(out - ref).max() < TOL
+
+
+def test_fused_unbatched_and_input_state(cuda_device):
+    desc = workloads.adjoint_brick(n=13, batch=1, layers=3)
+    desc["measure"] = "state"
+    g = torch.Generator().manual_seed(5)
+    st = torch.randn(1 << 13, generator=g, dtype=torch.complex64)
+    st = st / st.abs().pow(2).sum().sqrt()
+    out = _run(desc, cuda_device, state=st.to(cuda_device))
+    assert out.shape == (1 << 13,)
+    ref = oracle.run(desc, state=st.numpy(), batch=1)[0]
+    assert np.abs(out - ref).max() < TOL
+
+
+def _grad_case(desc, dev, opts, weights_seed=3):
+    circ = workloads.build_circuit(desc, engine="fused", **opts).to(dev)
+    x = None
+    kw = {}
+    if "x" in desc["inputs"]:
+        x = torch.tensor(desc["inputs"]["x"], device=dev, requires_grad=True)
+        kw["x"] = x
+        for qq in range(desc["n"]):
+            if f"up{qq}" in desc["inputs"]:
+                kw[f"up{qq}"] = x[:, qq]
+    out = circ(**kw)
+    g = torch.Generator().manual_seed(weights_seed)
+    w = torch.rand(out.shape, generator=g).to(dev) * 2 - 1
+    (out * w).sum().backward()
+    thetas = [m.theta.grad.item() for m in circ.circuit.layers
+              if isinstance(m, q.BuiltParametrizedOperator) and not m.named]
+    return np.array(thetas), (x.grad.cpu().numpy() if x is not None else None), w.cpu().numpy()
+
+
+@pytest.mark.parametrize("case,opts", [
+    ("brick_n10", dict()), ("brick_n14", dict()), ("brick_n16", dict(checkpoint_segments=3)),
+    ("sel_n9", dict()), ("sel_n14", dict(checkpoint_segments=2)), ("sel_n15", dict(tile_bits=12, low_bits=4)),
+])
+def test_fused_adjoint_vs_oracle(cuda_device, case, opts):
+    kind, nq = case.split("_n")
+    n = int(nq)
+    if kind == "brick":
+        desc = workloads.adjoint_brick(n=n, batch=4, layers=5)
+        desc["measure"] = "p0"
+    else:
+        desc = workloads.sel_reupload(n=n, batch=3, layers=3, reupload_every=2, measure="p0")
+    dth, dx, w = _grad_case(desc, cuda_device, opts)
+    rdp, rdn, _ = oracle.adjoint(desc, w, "p0")
+    assert np.abs(dth - rdp).max() < GTOL, np.abs(dth - rdp).max()
+    if dx is not None:
+        ref = rdn["x"].copy()
+        for qq in range(n):
+            ref[:, qq] += rdn[f"up{qq}"]
+        assert np.abs(dx - ref).max() < GTOL
+
+
+def test_fused_adjoint_vs_reference_autograd(cuda_device):
+    """MSE(<Z>, targets) on the adjoint-brick family equals qandle's own torch
+    autograd gradient (golden)."""
+    z = golden_io.load("circuits")
+    desc = golden_io.circuit_desc(z, "brick_small")
+    desc["measure"] = "p0"
+    circ = workloads.build_circuit(desc, engine="fused").to(cuda_device)
+    st = torch.zeros(desc["batch"], 1 << desc["n"], dtype=torch.complex64, device=cuda_device)
+    st[:, 0] = 1
+    p0 = circ(st)
+    zexp = 2.0 * p0 - 1.0
+    loss = ((zexp - torch.tensor(desc["targets"], device=cuda_device)) ** 2).mean()
+    loss.backward()
+    grads = [m.theta.grad.item() for m in circ.circuit.layers if isinstance(m, q.BuiltParametrizedOperator)]
+    assert abs(loss.item() - float(z["brick_small_loss"])) < 1e-5
+    assert np.abs(np.array(grads) - z["brick_small_dtheta"]).max() < 1e-5
+
+
+def test_fused_state_gradient(cuda_device):
+    desc = workloads.adjoint_brick(n=11, batch=2, layers=2)
+    desc["measure"] = "probs"
+    circ = workloads.build_circuit(desc, engine="fused").to(cuda_device)
+    g = torch.Generator().manual_seed(9)
+    st0 = torch.randn(2, 1 << 11, generator=g, dtype=torch.complex64)
+    st = st0.to(cuda_device).requires_grad_(True)
+    out = circ(st)
+    w = torch.rand(out.shape, generator=g).to(cuda_device)
+    (out * w).sum().backward()
+    _, _, dps = oracle.adjoint(desc, w.cpu().numpy(), "probs", state=st0.numpy())
+    assert np.abs(st.grad.cpu().numpy() - dps).max() < GTOL
+
+
+def test_fused_matches_plain(cuda_device):
+    desc = workloads.sel_reupload(n=13, batch=4, layers=3, reupload_every=2)
+    a = _run(desc, cuda_device, engine="fused")
+    b = _run(desc, cuda_device, engine="plain")
+    assert np.abs(a - b).max() < TOL

@@ -40,7 +40,7 @@ def test_gates_vs_reference(cuda_device):
         gate = golden_io.parse_gate(d["gate"])
         mod = _gate_module(gate, d["n"]).to(cuda_device)
         inp = torch.tensor(z[f"g{i}_in"], device=cuda_device)
-        out = mod(inp).cpu().numpy()
+        out = mod(inp).detach().cpu().numpy()
         ref = z[f"g{i}_out"]
         assert out.shape == ref.shape
         if gate[0] in ("cnot", "cz", "swap"):
@@ -62,7 +62,7 @@ def test_embeddings_vs_reference(cuda_device):
         d = json.loads(str(z[f"e{i}_desc"]))
         emb = q.AngleEmbedding(name="e", qubits=d["qubits"], rotation=d["rot"]).build(d["n"])
         x = torch.tensor(z[f"e{i}_x"], device=cuda_device)
-        out = emb(e=x).cpu().numpy()
+        out = emb(e=x).detach().cpu().numpy()
         ref = z[f"e{i}_out"]
         assert out.shape == ref.shape
         assert np.abs(out - ref).max() < TOL, i
@@ -73,11 +73,11 @@ def test_measurements_vs_reference(cuda_device):
     for i in range(int(z["count"])):
         inp = torch.tensor(z[f"m{i}_in"], device=cuda_device)
         n = inp.shape[-1].bit_length() - 1
-        p0 = q.MeasureProbabilityBuilt(num_qubits=n)(inp).cpu().numpy()
+        p0 = q.MeasureProbabilityBuilt(num_qubits=n)(inp).detach().cpu().numpy()
         ref = z[f"m{i}_p0"]
         assert p0.shape == ref.shape, (i, p0.shape, ref.shape)  # the reference's squeeze quirks
         assert np.abs(p0 - ref).max() < TOL
-        pj = q.MeasureJointProbability()(inp).cpu().numpy()
+        pj = q.MeasureJointProbability()(inp).detach().cpu().numpy()
         assert pj.shape == z[f"m{i}_joint"].shape
         assert np.abs(pj - z[f"m{i}_joint"]).max() < TOL
 
@@ -89,7 +89,7 @@ def test_sel_vs_reference(cuda_device):
         sel = q.StronglyEntanglingLayer(qubits=list(range(d["n"])), depth=d["depth"],
                                         q_params=torch.tensor(z[f"s{i}_w"]), remapping=None)
         mod = sel.build(num_qubits=d["n"]).to(cuda_device)
-        out = mod(torch.tensor(z[f"s{i}_in"], device=cuda_device)).detach().cpu().numpy()
+        out = mod(torch.tensor(z[f"s{i}_in"], device=cuda_device)).detach().detach().cpu().numpy()
         assert np.abs(out - z[f"s{i}_out"]).max() < TOL, i
 
 
@@ -103,7 +103,7 @@ def test_reupload_vs_reference(cuda_device):
                      (c2(dev(z["inp_b"]), reupload=v), z["bat_scalar"]),
                      (c2(dev(z["inp_b"]), reupload=vb), z["bat_vec"]),
                      (c2(dev(z["inp_u"]), reupload=vb), z["unb_vec"])):
-        got = got.detach().cpu().numpy()
+        got = got.detach().detach().cpu().numpy()
         assert got.shape == ref.shape
         assert np.abs(got - ref).max() < TOL
 
@@ -122,7 +122,7 @@ def test_circuits_plain_vs_reference(cuda_device, name):
         out = circ(st)
     else:
         out = circ(**kw)
-    out = out.detach().cpu().numpy()
+    out = out.detach().detach().cpu().numpy()
     ref = z[f"{name}_out"]
     assert out.shape == ref.shape
     assert np.abs(out - ref).max() < TOL
@@ -172,7 +172,7 @@ def test_plain_edge_cases(cuda_device):
         st = torch.randn(*shape, dtype=torch.complex64, device=cuda_device)
         for k in ("rx", "ry", "rz"):
             g = (k, 0, 0.7, None)
-            out = _gate_module(g, 1).to(cuda_device)(st).cpu().numpy()
+            out = _gate_module(g, 1).to(cuda_device)(st).detach().cpu().numpy()
             o = oracle.run({"n": 1, "batch": None, "gates": [g], "inputs": {}},
                            state=st.cpu().numpy(), batch=st.reshape(-1, 2).shape[0])
             assert np.abs(out.reshape(o.shape) - o).max() < TOL

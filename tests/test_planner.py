@@ -1,0 +1,122 @@
+"""Fusion planner on the CPU: planned programs, executed by the op emulator
+(tests/program_emulator.py), equal the complex128 oracle.  Covers tile
+selection, commutation reordering, slot merging, op encoding, checkpoint
+segments and the adjoint plan, for several tile shapes."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle
+from qandle_gb300 import engine, workloads
+from tests import program_emulator as emu
+
+
+def _runtime(lo, desc, B):
+    params = np.array([float(m.remapping(m.theta).reshape(-1)[0].detach()) for m in lo.param_mods])
+    inputs = desc.get("inputs", {})
+    cols = []
+    for name, j in lo.named_cols:
+        v = np.asarray(inputs[name], dtype=np.float32).astype(np.float64)
+        v = v[..., j] if j is not None else v
+        cols.append(np.broadcast_to(v, (B,)))
+    named = np.stack(cols, 1) if cols else np.zeros((B, 1))
+    umats = [np.asarray(u.numpy(), dtype=complex) for u in lo.umats]
+    embed = None
+    emb = [g for g in lo.gates if g[0] == 7]
+    if emb:
+        g = emb[-1]
+        axis, k, col0, qoff = g[1], g[2], g[4], g[5]
+        embed = np.zeros((B, lo.n, 2), complex)
+        embed[:, :, 0] = 1.0
+        for jj in range(k):
+            q = lo.qlist[qoff + jj]
+            m = np.stack([emu.row_matrix(axis, x) for x in named[:, col0 + jj]])
+            v0, v1 = embed[:, q, 0].copy(), embed[:, q, 1].copy()
+            embed[:, q, 0] = m[:, 0, 0] * v0 + m[:, 1, 0] * v1
+            embed[:, q, 1] = m[:, 0, 1] * v0 + m[:, 1, 1] * v1
+    return params, named, umats, embed
+
+
+CASES = [
+    ("sel_n10", lambda: workloads.sel_reupload(n=10, batch=3, layers=3, reupload_every=2, measure="z")),
+    ("sel_n15", lambda: workloads.sel_reupload(n=15, batch=2, layers=3, reupload_every=2, measure="z")),
+    ("brick_n14", lambda: workloads.adjoint_brick(n=14, batch=2, layers=4)),
+    ("deep_n14", lambda: workloads.deep_u(n=14, batch=1, layers=4)),
+    ("plain_n8", lambda: workloads.plain_small(n=8, batch=5, layers=2)),
+]
+OPTS = [dict(tile_bits=13, low_bits=6, max_high=0), dict(tile_bits=12, low_bits=4, max_high=2),
+        dict(tile_bits=11, low_bits=5, max_high=1), dict(tile_bits=13, low_bits=8, max_high=3)]
+
+
+@pytest.mark.parametrize("case", [c[0] for c in CASES])
+@pytest.mark.parametrize("oi", range(len(OPTS)))
+def test_forward_plan_matches_oracle(case, oi):
+    desc = dict(CASES)[case]()
+    desc["measure"] = "state"
+    circ = workloads.build_circuit(desc, engine="fused")
+    lo = engine.lower(circ.circuit)
+    B = desc["batch"]
+    prog = engine.Program(lo, "state", keep_state=True, segments=2, **OPTS[oi])
+    params, named, umats, embed = _runtime(lo, desc, B)
+    st, ck = emu.run_forward(prog, desc["n"], B, params, named, umats, embed=embed)
+    ref = oracle.run(desc)
+    assert np.abs(st - ref).max() < 1e-10
+    assert prog.info.forward_passes >= 1
+
+
+@pytest.mark.parametrize("case", ["sel_n10", "brick_n14", "deep_n14", "sel_n15"])
+def test_backward_plan_matches_oracle(case):
+    desc = dict(CASES)[case]()
+    desc["measure"] = "p0"
+    n, B = desc["n"], desc["batch"]
+    circ = workloads.build_circuit(desc, engine="fused")
+    lo = engine.lower(circ.circuit)
+    prog = engine.Program(lo, "p0", keep_state=True, segments=3, tile_bits=13, low_bits=5)
+    params, named, umats, embed = _runtime(lo, desc, B)
+    st, ck = emu.run_forward(prog, n, B, params, named, umats, embed=embed)
+    w = np.linspace(-1.0, 1.0, B * n).reshape(B, n)
+    # lambda = dL/dpsi* for L = sum(w * P0)
+    amp = np.arange(1 << n)
+    wt = np.zeros((B, 1 << n))
+    for q in range(n):
+        wt += np.where(((amp >> (n - 1 - q)) & 1) == 0, 1.0, 0.0)[None, :] * w[:, q:q + 1]
+    lam = wt * st
+    tg = prog.grad_targets()
+    dp, dn, _ = emu.run_backward(prog, n, B, params, named, umats, st, lam, ck, tg)
+    rdp, rdn, _ = oracle.adjoint(desc, w, "p0")
+    assert dp.size == rdp.size and (dp.size == 0 or np.abs(dp - rdp).max() < 1e-9)
+    # every occurrence of a named input has its own column; sum them per
+    # input the way autograd does, then compare with the oracle's totals
+    got = {}
+    for c, (name, j) in enumerate(lo.named_cols):
+        ref = rdn[name]
+        arr = got.setdefault(name, np.zeros_like(ref))
+        if j is None:
+            arr += dn[:, c] if arr.ndim == 1 else dn[:, c:c + 1]
+        else:
+            arr[:, j] += dn[:, c]
+    for name, arr in got.items():
+        assert np.abs(arr - rdn[name]).max() < 1e-9, name
+
+
+def test_fusion_reduces_passes():
+    desc = workloads.sel_reupload(n=20, batch=1, layers=10)
+    circ = workloads.build_circuit(desc, engine="fused")
+    lo = engine.lower(circ.circuit)
+    prog = engine.Program(lo, "z", keep_state=False)
+    gates = len(lo.gates)
+    # every pass is one HBM round trip; the plain form needs one per gate
+    assert prog.info.forward_passes * 10 <= gates, prog.summary()
+
+
+def test_planner_rejects_bad_programs():
+    from qandle_gb300 import _lib
+    import ctypes
+
+    lib = _lib.load()
+    g = (_lib.Gate * 1)(_lib.Gate(0, 9, 0, 0, 0, 0))  # qubit 9 in a 6-qubit circuit
+    h = ctypes.c_void_p()
+    rc = lib.qg_program_create(g, 1, None, 6, None, ctypes.byref(h))
+    assert rc == 1 and b"out of range" in lib.qg_last_error()
+    rc = lib.qg_program_create(g, 1, None, 3, None, ctypes.byref(h))
+    assert rc == 1 and b"num_qubits" in lib.qg_last_error()
