@@ -210,6 +210,14 @@ int qg_program_forward(const qg_program* prog, const void* dev_table, void* work
                        const float* params, const float* named, const void* umats, float* out,
                        void* ckpt, void* stream);
 
+/* Same as qg_program_forward, and records pass_events[2p] / [2p+1]
+ * (cudaEvent_t, created by the caller) on `stream` around forward pass p, so
+ * a caller can time the pass kernels on the stream they run on. */
+int qg_program_forward_timed(const qg_program* prog, const void* dev_table, void* workspace,
+                             int64_t workspace_bytes, void* state, int64_t batch, int zero_init,
+                             const float* params, const float* named, const void* umats, float* out,
+                             void* ckpt, void* const* pass_events, void* stream);
+
 /* Adjoint backward.  state: the forward's final state (overwritten: it is
  * un-computed gate by gate); lam: [B][2^n] buffer.  grad_out is the upstream
  * gradient of the forward output (float [B][n] for P0/<Z>, float [B][2^n]

@@ -88,6 +88,9 @@ SIGNATURES = {
     "qg_program_workspace_bytes": (c_int64, [c_void_p, c_int64, c_int]),
     "qg_program_forward": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int,
                                    c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "qg_program_forward_timed": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int,
+                                         c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                         c_void_p]),
     "qg_program_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
                                     c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p]),

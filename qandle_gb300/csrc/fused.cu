@@ -1062,6 +1062,14 @@ int64_t qg_program_workspace_bytes(const qg_program* prog, int64_t batch, int ba
 int qg_program_forward(const qg_program* prog, const void* dev_table, void* workspace, int64_t workspace_bytes,
                        void* state, int64_t batch, int zero_init, const float* params, const float* named,
                        const void* umats, float* out, void* ckpt, void* stream) {
+    return qg_program_forward_timed(prog, dev_table, workspace, workspace_bytes, state, batch, zero_init, params,
+                                    named, umats, out, ckpt, nullptr, stream);
+}
+
+int qg_program_forward_timed(const qg_program* prog, const void* dev_table, void* workspace,
+                             int64_t workspace_bytes, void* state, int64_t batch, int zero_init, const float* params,
+                             const float* named, const void* umats, float* out, void* ckpt,
+                             void* const* pass_events, void* stream) {
     using namespace qg;
     QG_CHECK_ARG(prog && dev_table && workspace && state, "null pointer");
     QG_CHECK_ARG(batch >= 1, "batch must be >= 1");
@@ -1113,12 +1121,14 @@ int qg_program_forward(const qg_program* prog, const void* dev_table, void* work
     for (int p = 0; p < R.nfpass; ++p) {
         int zi = (p == 0) ? zero_init : 0;
         int rc;
+        if (pass_events) QG_CUDA_TRY(cudaEventRecord((cudaEvent_t)pass_events[2 * p], st));
         switch (R.tile_bits) {
             case 13: rc = launch_fwd_pass<13>(dpass, dops, p, A, zi, demb, tiles, st); break;
             case 12: rc = launch_fwd_pass<12>(dpass, dops, p, A, zi, demb, tiles, st); break;
             default: rc = launch_fwd_pass<11>(dpass, dops, p, A, zi, demb, tiles, st); break;
         }
         if (rc) return rc;
+        if (pass_events) QG_CUDA_TRY(cudaEventRecord((cudaEvent_t)pass_events[2 * p + 1], st));
     }
     if (p0) {
         k_p0_finalize<<<grid_for(batch * R.n, 128), 128, 0, st>>>(dpass + (R.nfpass - 1), A.p0part, out, batch, R.n,

@@ -242,15 +242,15 @@ def _out_shape(measure, out, n, unbatched):
 
 
 class _FusedRun(torch.autograd.Function):
+    # grad mode is off inside forward: the caller decides whether to keep the
+    # final state for the backward (`prog` is the training or inference plan)
     @staticmethod
-    def forward(ctx, ex, state_in, params, named, umats, batch, zero_init):
-        prog = ex.program(training=torch.is_grad_enabled() and any(
-            t is not None and t.requires_grad for t in (state_in, params, named)))
+    def forward(ctx, ex, prog, state_in, params, named, umats, batch, zero_init):
         return ex.run_forward(ctx, prog, state_in, params, named, umats, batch, zero_init)
 
     @staticmethod
     def backward(ctx, gout):
-        return ctx.ex.run_backward(ctx, gout)
+        return (None,) + ctx.ex.run_backward(ctx, gout)
 
 
 class FusedExecutor:
@@ -286,7 +286,10 @@ class FusedExecutor:
             _lib.require_cuda_state(state)
         inp = _Inputs(self.lowered, state, kwargs, dev)
         zero_init = 1 if (state is None and not self._has_embedding()) else 0
-        out = _FusedRun.apply(self, state, inp.params, inp.named, inp.umats, inp.batch, zero_init)
+        training = torch.is_grad_enabled() and any(
+            t is not None and t.requires_grad for t in (state, inp.params, inp.named))
+        out = _FusedRun.apply(self, self.program(training), state, inp.params, inp.named, inp.umats,
+                              inp.batch, zero_init)
         return _out_shape(self.lowered.measure, out, self.n, inp.unbatched)
 
     def _has_embedding(self) -> bool:
@@ -355,7 +358,7 @@ class FusedExecutor:
         ws = prog.workspace(B, True, dev)
         dparams = torch.empty(max(1, prog.info.nparams), dtype=torch.float32, device=dev)
         dnamed = torch.empty(B, max(1, prog.info.ncols), dtype=torch.float32, device=dev)
-        need_state = ctx.needs_input_grad[1] and not prog.info.has_embedding
+        need_state = ctx.needs_input_grad[2] and not prog.info.has_embedding
         dstate = torch.empty_like(st) if need_state else None
         _lib.call("qg_program_backward", prog.handle, prog.table(dev).data_ptr(), ws.data_ptr(), ws.numel(),
                   st.data_ptr(), lam.data_ptr(), B, params.data_ptr(), named.data_ptr(), umats.data_ptr(),
@@ -370,6 +373,79 @@ class FusedExecutor:
             elif shp[0] != B:
                 gstate = dstate.sum(0, keepdim=True)
             gstate = gstate.reshape(shp)
-        gp = dparams[:params.numel()] if ctx.needs_input_grad[2] else None
-        gn = dnamed[:, :named.shape[1]].reshape(named.shape) if (ctx.needs_input_grad[3] and named.dim() == 2) else None
+        gp = dparams[:params.numel()] if ctx.needs_input_grad[3] else None
+        gn = dnamed[:, :named.shape[1]].reshape(named.shape) if (ctx.needs_input_grad[4] and named.dim() == 2) else None
         return None, gstate, gp, gn, None, None, None
+
+
+class BoundForward:
+    """Static buffers for repeated inference calls at one batch size.
+
+    ``set_inputs`` copies a call's values into the buffers, ``launch`` runs
+    the planned passes on the current stream (optionally recording an event
+    pair around every pass), and ``capture``/``replay`` put the whole forward
+    (matrix build, embedding factors, every pass, measurement) into one CUDA
+    graph so a call costs a single graph launch.
+    """
+
+    def __init__(self, ex: "FusedExecutor", batch: int, device, has_state: bool = False):
+        self.ex = ex
+        self.prog = ex.program(False)
+        self.n = ex.n
+        self.batch = batch
+        self.device = torch.device(device)
+        info = self.prog.info
+        n = self.n
+        self.state = torch.zeros(batch, 1 << n, dtype=torch.complex64, device=device)
+        m = self.prog.measure
+        if m in ("p0", "z"):
+            self.out = torch.empty(batch, n, dtype=torch.float32, device=device)
+        elif m == "probs":
+            self.out = torch.empty(batch, 1 << n, dtype=torch.float32, device=device)
+        else:
+            self.out = None
+        self.ws = self.prog.workspace(batch, False, device)
+        self.params = torch.zeros(max(1, info.nparams), dtype=torch.float32, device=device)
+        self.named = torch.zeros(batch, max(1, info.ncols), dtype=torch.float32, device=device)
+        self.umats = torch.zeros(max(1, info.numats), 2, 2, dtype=torch.complex64, device=device)
+        self.table = self.prog.table(device)
+        self.zero_init = 0 if (has_state or info.has_embedding) else 1
+        self.graph = None
+
+    def set_inputs(self, state=None, **kwargs) -> None:
+        with torch.no_grad():
+            inp = _Inputs(self.ex.lowered, state, kwargs, self.device)
+            if inp.batch != self.batch and inp.batch != 1:
+                raise ValueError(f"bound for batch {self.batch}, got {inp.batch}")
+            self.params[:inp.params.numel()].copy_(inp.params)
+            if self.ex.lowered.named_cols:
+                self.named.copy_(inp.named.expand(self.batch, -1))
+            if self.ex.lowered.umats:
+                self.umats.copy_(inp.umats)
+            if state is not None:
+                self.state.copy_(state.reshape(-1, 1 << self.n).expand(self.batch, -1))
+
+    def launch(self, events=None) -> None:
+        evp = None
+        if events is not None:
+            evp = (ctypes.c_void_p * len(events))(*[e.cuda_event for e in events])
+        _lib.call("qg_program_forward_timed", self.prog.handle, self.table.data_ptr(), self.ws.data_ptr(),
+                  self.ws.numel(), self.state.data_ptr(), self.batch, self.zero_init, self.params.data_ptr(),
+                  self.named.data_ptr(), self.umats.data_ptr(), _lib.ptr(self.out), None, evp,
+                  _lib.stream())
+
+    def capture(self) -> None:
+        s = torch.cuda.Stream(device=self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            self.launch()  # warm-up outside the graph (sets kernel attributes)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.launch()
+
+    def replay(self) -> None:
+        self.graph.replay()
+
+    def result(self) -> torch.Tensor:
+        return self.state if self.out is None else self.out

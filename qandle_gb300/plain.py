@@ -205,3 +205,125 @@ class Probs(torch.autograd.Function):
         _lib.call("qg_probs_backward", st.data_ptr(), g.data_ptr(), gin.data_ptr(), st.numel(),
                   _lib.stream())
         return gin
+
+
+def _angle_buffer(angle, device):
+    return torch.as_tensor(angle).to(device=device, dtype=torch.float32).reshape(-1).contiguous()
+
+
+def apply_rotation_(st: torch.Tensor, n: int, qubit: int, axis: int, angle) -> torch.Tensor:
+    """In-place rotation on a contiguous [B, 2^n] buffer (no autograd)."""
+    a = _angle_buffer(angle, st.device)
+    per = a.numel() > 1
+    if per and st.shape[0] == 1 and a.numel() > 1:
+        st = st.expand(a.numel(), -1).contiguous()
+    _lib.call("qg_apply_rotation", st.data_ptr(), st.shape[0], n, qubit, axis, a.data_ptr(),
+              1 if per else 0, 0, _lib.stream())
+    return st
+
+
+def run_layers_inplace(layers, state: torch.Tensor | None, n: int, kwargs: dict,
+                       initial: torch.Tensor) -> torch.Tensor:
+    """The plain form without autograd: one in-place kernel pass per gate on a
+    single working buffer (the buffer is a copy; the caller's state is not
+    modified).  Layers are the built modules of UnsplittedCircuit."""
+    st = None
+    src = initial if state is None else state
+    unbatched = src.dim() == 1
+    for mod in layers:
+        name = type(mod).__name__
+        if name == "AngleEmbeddingBuilt":
+            st = mod(None, **kwargs)
+            unbatched = st.dim() == 1
+            st = st.reshape(-1, 1 << n)
+            continue
+        if st is None:
+            _lib.require_cuda_state(src)
+            st = src.reshape(-1, 1 << n).contiguous().clone()
+        if name in ("BuiltRX", "BuiltRY", "BuiltRZ"):
+            prev = st.shape[0]
+            st = apply_rotation_(st, n, mod.qubit, mod.axis, mod.angle(**kwargs))
+            if st.shape[0] != prev:
+                unbatched = False
+        elif name == "BuiltU":
+            m = mod._m.to(st.device).contiguous()
+            _lib.call("qg_apply_matrix", st.data_ptr(), st.shape[0], n, mod.qubit, m.data_ptr(), 0,
+                      _lib.stream())
+        elif name in ("BuiltCNOT", "BuiltCZ"):
+            _lib.call(_PERM["cnot" if name == "BuiltCNOT" else "cz"], st.data_ptr(), st.shape[0], n,
+                      mod.c, mod.t, _lib.stream())
+        elif name == "BuiltSWAP":
+            if mod.a != mod.b:
+                _lib.call("qg_apply_swap", st.data_ptr(), st.shape[0], n, mod.a, mod.b, _lib.stream())
+        elif hasattr(mod, "mods"):
+            st = run_layers_inplace(list(mod.mods), st, n, kwargs, initial)
+        else:
+            # measurements: their own (out-of-place) forward ends the loop
+            return mod(st.reshape(1 << n) if unbatched else st)
+    if st is None:
+        st = src.reshape(-1, 1 << n).clone()
+    return st.reshape(1 << n) if unbatched else st
+
+
+def _flat_layers(layers):
+    out = []
+    for mod in layers:
+        if hasattr(mod, "mods"):
+            out.extend(_flat_layers(list(mod.mods)))
+        else:
+            out.append(mod)
+    return out
+
+
+def adjoint_per_gate(layers, n: int, grad_p0: torch.Tensor, state: torch.Tensor | None = None,
+                     kwargs: dict | None = None, initial: torch.Tensor | None = None) -> list:
+    """Adjoint gradient with one kernel pass per gate and state (the plain
+    form of the adjoint): forward in place, then for every gate in reverse
+    the angle gradient Im<lam|P|psi> (a reduction kernel) and the inverse
+    gate on psi and on the cotangent.  The circuit must end with
+    MeasureProbability; grad_p0 is dL/dP0 [B, n].  Returns dL/dangle for the
+    unnamed rotations in layer order.  Shares no code with the fused engine
+    and serves as its per-gate baseline."""
+    kwargs = kwargs or {}
+    flat = _flat_layers(layers)
+    gates = [m for m in flat if type(m).__name__ not in ("MeasureProbabilityBuilt",)]
+    with torch.no_grad():
+        psi = run_layers_inplace(gates, state, n, kwargs, initial if initial is not None else state)
+        psi = psi.reshape(-1, 1 << n).contiguous()
+        B = psi.shape[0]
+        g = torch.empty_like(psi)
+        gp = grad_p0.to(torch.float32).reshape(B, n).contiguous()
+        _lib.call("qg_measure_p0_backward", psi.data_ptr(), gp.data_ptr(), g.data_ptr(), B, n,
+                  _lib.stream())
+        scr = _scratch(_lib.load().qg_rotation_grad_scratch_bytes(B, n), psi.device)
+        grads = {}
+        one = torch.empty(1, dtype=torch.float32, device=psi.device)
+        for mod in reversed(gates):
+            name = type(mod).__name__
+            if name in ("BuiltRX", "BuiltRY", "BuiltRZ"):
+                a = _angle_buffer(mod.angle(**kwargs), psi.device)
+                per = a.numel() > 1
+                if not mod.named:
+                    _lib.call("qg_rotation_grad", psi.data_ptr(), g.data_ptr(), one.data_ptr(), B, n,
+                              mod.qubit, mod.axis, 0, scr.data_ptr(), scr.numel(), _lib.stream())
+                    grads[id(mod)] = one.clone()
+                for buf in (psi, g):
+                    _lib.call("qg_apply_rotation", buf.data_ptr(), B, n, mod.qubit, mod.axis, a.data_ptr(),
+                              1 if per else 0, 1, _lib.stream())
+            elif name == "BuiltU":
+                m = mod._m.to(psi.device).contiguous()
+                for buf in (psi, g):
+                    _lib.call("qg_apply_matrix", buf.data_ptr(), B, n, mod.qubit, m.data_ptr(), 1, _lib.stream())
+            elif name in ("BuiltCNOT", "BuiltCZ"):
+                for buf in (psi, g):
+                    _lib.call(_PERM["cnot" if name == "BuiltCNOT" else "cz"], buf.data_ptr(), B, n, mod.c, mod.t,
+                              _lib.stream())
+            elif name == "BuiltSWAP":
+                if mod.a != mod.b:
+                    for buf in (psi, g):
+                        _lib.call("qg_apply_swap", buf.data_ptr(), B, n, mod.a, mod.b, _lib.stream())
+            elif name == "AngleEmbeddingBuilt":
+                break
+            else:
+                raise ValueError(f"adjoint_per_gate cannot handle {name}")
+        return [grads[id(m)] for m in gates if id(m) in grads]

@@ -118,6 +118,11 @@ class UnsplittedCircuit(torch.nn.Module):
         return out
 
     def forward(self, state=None, **kwargs):
+        if not torch.is_grad_enabled() and self._all_cuda(state, kwargs):
+            # inference: one in-place kernel pass per gate on a single buffer
+            from . import plain
+
+            return plain.run_layers_inplace(list(self.layers), state, self.num_qubits, kwargs, self.state)
         if state is None:
             state = self.state
         for mod in self.layers:
@@ -126,6 +131,11 @@ class UnsplittedCircuit(torch.nn.Module):
             else:
                 state = mod(state)
         return state
+
+    def _all_cuda(self, state, kwargs) -> bool:
+        ts = [state if state is not None else self.state]
+        ts += [v for v in kwargs.values() if isinstance(v, torch.Tensor)]
+        return all(t.is_cuda for t in ts)
 
     def decompose(self) -> "UnsplittedCircuit":
         new_layers = []
