@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--sweep", action="store_true", help="fusion-width sweep k = 1..7")
     ap.add_argument("--no-extras", action="store_true", help="headline only")
     ap.add_argument("--cpu-samples", type=int, default=16, help="samples in the CPU baseline")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--n", type=int, default=20)
     ap.add_argument("--batch", type=int, default=256)
     return ap.parse_args()
@@ -374,7 +375,7 @@ def main():
             line["k_sweep"] = sweep
 
     if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(desc, args.cpu_samples)
+        line["cpu_baseline"] = None if args.no_cpu else cpu_baseline(desc, args.cpu_samples)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.barrier()

@@ -643,8 +643,10 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* pbuf0 = reinterpret_cast<float2*>(smem_raw);  // psi, lambda, psi, lambda
     float* gacc = reinterpret_cast<float*>(pbuf0 + 4 * AMPS);  // [ngrad][NT]
+    // sample (within the tile) each partial belongs to: the thread's sample
+    // bits depend on the mapping in force when the gradient op ran
+    uint8_t* gsmp = reinterpret_cast<uint8_t*>(gacc + kMaxGradPerPass * NT);  // [ngrad][NT]
     __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int s_tsample[NT];
 
     const PassDesc d = passes[pass_index];
     const int4* ops = ops_all + d.op_begin;
@@ -707,11 +709,13 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
             } else if (op.x == OP_GRAD) {
                 float gsum = grad_dispatch(op.y, psi, lam, op.z);
                 gacc[(op.w - d.grad_base) * NT + tid] = gsum;
+                gsmp[(op.w - d.grad_base) * NT + tid] = (uint8_t)tm.sample_off;
             } else if (op.x == OP_MAT && (op.w & OPF_GRAD)) {
                 int axis = (op.w >> 8) & 3;
                 int gslot = op.w >> 12;
                 float gsum = grad_dispatch(op.y, psi, lam, axis);
                 gacc[(gslot - d.grad_base) * NT + tid] = gsum;
+                gsmp[(gslot - d.grad_base) * NT + tid] = (uint8_t)tm.sample_off;
                 float2 m[4];
                 load_slot(A, op.z, op.w, g.sample + tm.sample_off, m);
                 mat_dispatch(op.y, psi, m);
@@ -721,7 +725,6 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
                 apply_op(op, lam, tm, A, g.sample + tm.sample_off, true);
             }
         }
-        s_tsample[tid] = tm.sample_off;
         __syncthreads();
         // gradient partials of this tile: per sample when samples share the tile
         if (d.ngrad > 0) {
@@ -735,7 +738,7 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
                 int gi = it / spt, s = it % spt;
                 float acc = 0.f;
                 for (int c = lane; c < NT; c += 32)
-                    if (s_tsample[c] == s) acc += gacc[gi * NT + c];
+                    if (gsmp[gi * NT + c] == s) acc += gacc[gi * NT + c];
                 for (int o2 = 16; o2 > 0; o2 >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o2);
                 if (lane == 0 && s < g.nsamples) {
                     int64_t unit = (n >= TB) ? (g.sample * tps + g.tile_in_sample) : (g.sample + s);
@@ -1030,7 +1033,7 @@ template <int TB>
 static int launch_bwd_pass(const PassDesc* dpass, const int4* dops, int p, const RunArgs& A, int store_lam,
                            int64_t tiles, cudaStream_t st) {
     constexpr int NT = 1 << (TB - 5);
-    size_t smem = 4 * (size_t(1) << TB) * sizeof(float2) + (size_t)kMaxGradPerPass * NT * sizeof(float);
+    size_t smem = 4 * (size_t(1) << TB) * sizeof(float2) + (size_t)kMaxGradPerPass * NT * (sizeof(float) + 1);
     static bool attr_set = false;
     if (!attr_set) {
         QG_CUDA_TRY(cudaFuncSetAttribute(k_bwd_pass<TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
