@@ -132,40 +132,46 @@ __device__ __forceinline__ uint32_t tile_bytes(const PassDesc& d, const TileGeo&
     return (1u << d.tile_bits) * 8u;
 }
 
-// Issue the bulk copies of one tile (one thread; the caller has armed `bar`
-// with the expected byte count through a single arrive.expect_tx).
+// The bulk copies of one tile are issued by the 32 lanes of warp 0 in
+// parallel (lane l issues runs l, l + 32, ...); for loads the caller has armed
+// `bar` with the tile's byte count through one arrive.expect_tx first.
 __device__ void issue_tile_load(const PassDesc& d, const TileGeo& g, const float2* src, float2* dst,
-                                uint64_t* bar, int n) {
+                                uint64_t* bar, int n, int lane) {
     if (n < d.tile_bits) {
-        bulk_g2s(dst, src + g.base, tile_bytes(d, g, n), bar);
+        if (lane == 0) bulk_g2s(dst, src + g.base, tile_bytes(d, g, n), bar);
         return;
     }
     int runs = 1 << (d.tile_bits - d.run_bits);
     uint32_t rb = (1u << d.run_bits) * 8u;
-    for (int r = 0; r < runs; ++r) bulk_g2s(dst + ((int64_t)r << d.run_bits), src + g.base + run_offset(d, r), rb, bar);
+    for (int r = lane; r < runs; r += 32)
+        bulk_g2s(dst + ((int64_t)r << d.run_bits), src + g.base + run_offset(d, r), rb, bar);
 }
 
-__device__ void issue_tile_store(const PassDesc& d, const TileGeo& g, float2* dstg, const float2* src, int n) {
+__device__ void issue_tile_store(const PassDesc& d, const TileGeo& g, float2* dstg, const float2* src, int n,
+                                 int lane) {
     if (n < d.tile_bits) {
         uint32_t bytes = (uint32_t)((int64_t)g.nsamples << n) * 8u;
-        bulk_s2g(dstg + g.base, src, bytes);
+        if (lane == 0) bulk_s2g(dstg + g.base, src, bytes);
         return;
     }
     int runs = 1 << (d.tile_bits - d.run_bits);
     uint32_t rb = (1u << d.run_bits) * 8u;
-    for (int r = 0; r < runs; ++r) bulk_s2g(dstg + g.base + run_offset(d, r), src + ((int64_t)r << d.run_bits), rb);
+    for (int r = lane; r < runs; r += 32)
+        bulk_s2g(dstg + g.base + run_offset(d, r), src + ((int64_t)r << d.run_bits), rb);
 }
 
 // float (probability) image of a tile: half the bytes of the state image
-__device__ void issue_tile_store_f32(const PassDesc& d, const TileGeo& g, float* dstg, const float* src, int n) {
+__device__ void issue_tile_store_f32(const PassDesc& d, const TileGeo& g, float* dstg, const float* src, int n,
+                                     int lane) {
     if (n < d.tile_bits) {
         uint32_t bytes = (uint32_t)((int64_t)g.nsamples << n) * 4u;
-        bulk_s2g(dstg + g.base, src, bytes);
+        if (lane == 0) bulk_s2g(dstg + g.base, src, bytes);
         return;
     }
     int runs = 1 << (d.tile_bits - d.run_bits);
     uint32_t rb = (1u << d.run_bits) * 4u;
-    for (int r = 0; r < runs; ++r) bulk_s2g(dstg + g.base + run_offset(d, r), src + ((int64_t)r << d.run_bits), rb);
+    for (int r = lane; r < runs; r += 32)
+        bulk_s2g(dstg + g.base + run_offset(d, r), src + ((int64_t)r << d.run_bits), rb);
 }
 
 // ----------------------------------------------------- thread mapping --
@@ -432,25 +438,28 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
     float2* buf0 = reinterpret_cast<float2*>(smem_raw);
     float2* buf1 = buf0 + AMPS;
     __shared__ __align__(8) uint64_t bars[2];
+    __shared__ PassDesc sd;
 
-    const PassDesc d = passes[pass_index];
-    const int4* ops = ops_all + d.op_begin;
     const int tid = threadIdx.x;
-    const int n = A.n;
-    const bool load_in = (d.init == INIT_LOAD) && !zero_init;
-
+    const int lane = tid & 31;
     if (tid == 0) {
+        sd = passes[pass_index];
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    const PassDesc& d = sd;
+    const int4* ops = ops_all + d.op_begin;
+    const int n = A.n;
+    const bool load_in = (d.init == INIT_LOAD) && !zero_init;
 
     int64_t t0 = blockIdx.x;
-    if (load_in && tid == 0 && t0 < num_tiles) {
+    if (load_in && tid < 32 && t0 < num_tiles) {
         TileGeo g = tile_geo(d, t0, n, A.batch);
-        mbar_expect_tx(&bars[0], tile_bytes(d, g, n));
-        issue_tile_load(d, g, A.state, buf0, &bars[0], n);
+        if (lane == 0) mbar_expect_tx(&bars[0], tile_bytes(d, g, n));
+        __syncwarp();
+        issue_tile_load(d, g, A.state, buf0, &bars[0], n, lane);
     }
     int iter = 0;
     for (int64_t t = t0; t < num_tiles; t += gridDim.x, ++iter) {
@@ -510,11 +519,12 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
         }
         // everybody has read `buf`; prefetch the next tile into the other buffer
         __syncthreads();
-        if (load_in && tid == 0 && t + gridDim.x < num_tiles) {
+        if (load_in && tid < 32 && t + gridDim.x < num_tiles) {
             bulk_wait_read0();  // stores issued from nbuf two tiles ago have read it
             TileGeo gn = tile_geo(d, t + gridDim.x, n, A.batch);
-            mbar_expect_tx(&bars[(iter + 1) & 1], tile_bytes(d, gn, n));
-            issue_tile_load(d, gn, A.state, nbuf, &bars[(iter + 1) & 1], n);
+            if (lane == 0) mbar_expect_tx(&bars[(iter + 1) & 1], tile_bytes(d, gn, n));
+            __syncwarp();
+            issue_tile_load(d, gn, A.state, nbuf, &bars[(iter + 1) & 1], n, lane);
         }
         const int64_t my_sample = g.sample + tm.sample_off;
         // ---- the gate program of this pass ----
@@ -539,15 +549,15 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
             for (int r = 0; r < 32; ++r) buf[nat_index(r, tid)] = a[r];
             fence_proxy_async();
             __syncthreads();
-            if (tid == 0) {
-                issue_tile_store(d, g, A.state, buf, n);
-                if (d.ckpt >= 0) issue_tile_store(d, g, A.ckpt + (int64_t)d.ckpt * (A.batch << n), buf, n);
+            if (tid < 32) {
+                issue_tile_store(d, g, A.state, buf, n, lane);
+                if (d.ckpt >= 0) issue_tile_store(d, g, A.ckpt + (int64_t)d.ckpt * (A.batch << n), buf, n, lane);
                 bulk_commit();
             }
         }
         if (d.epi & (EPI_PROBS | EPI_P0)) {
             if (d.epi & EPI_STORE) {
-                if (tid == 0) bulk_wait_read0();
+                if (tid < 32) bulk_wait_read0();
                 __syncthreads();
             }
             float* pb = reinterpret_cast<float*>(buf);
@@ -556,8 +566,8 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
             if (d.epi & EPI_PROBS) {
                 fence_proxy_async();
                 __syncthreads();
-                if (tid == 0) {
-                    issue_tile_store_f32(d, g, A.out, pb, n);
+                if (tid < 32) {
+                    issue_tile_store_f32(d, g, A.out, pb, n, lane);
                     bulk_commit();
                     bulk_wait_read0();
                 }
@@ -629,7 +639,7 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
         fence_proxy_async();
         __syncthreads();
     }
-    if (tid == 0) bulk_wait_all0();
+    if (tid < 32) bulk_wait_all0();
     (void)emb;
 }
 
@@ -647,10 +657,14 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
     // bits depend on the mapping in force when the gradient op ran
     uint8_t* gsmp = reinterpret_cast<uint8_t*>(gacc + kMaxGradPerPass * NT);  // [ngrad][NT]
     __shared__ __align__(8) uint64_t bars[2];
+    __shared__ PassDesc sd;
 
-    const PassDesc d = passes[pass_index];
-    const int4* ops = ops_all + d.op_begin;
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    if (tid == 0) sd = passes[pass_index];
+    __syncthreads();
+    const PassDesc& d = sd;
+    const int4* ops = ops_all + d.op_begin;
     const int n = A.n;
     const float2* psi_src = d.psi_from_ckpt >= 0 ? A.ckpt + (int64_t)d.psi_from_ckpt * (A.batch << n) : A.state;
     const bool last = (d.epi & EPI_STORE) == 0;  // final backward pass: nothing to store but lambda
@@ -663,11 +677,12 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
     }
     __syncthreads();
     int64_t t0 = blockIdx.x;
-    if (tid == 0 && t0 < num_tiles) {
+    if (tid < 32 && t0 < num_tiles) {
         TileGeo g = tile_geo(d, t0, n, A.batch);
-        mbar_expect_tx(&bars[0], 2 * tile_bytes(d, g, n));
-        issue_tile_load(d, g, psi_src, pbuf0, &bars[0], n);
-        issue_tile_load(d, g, A.lam, pbuf0 + AMPS, &bars[0], n);
+        if (lane == 0) mbar_expect_tx(&bars[0], 2 * tile_bytes(d, g, n));
+        __syncwarp();
+        issue_tile_load(d, g, psi_src, pbuf0, &bars[0], n, lane);
+        issue_tile_load(d, g, A.lam, pbuf0 + AMPS, &bars[0], n, lane);
     }
     int iter = 0;
     for (int64_t t = t0; t < num_tiles; t += gridDim.x, ++iter) {
@@ -689,12 +704,13 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
         }
         decode_map(d, NatMap<TB>::y, NatMap<TB>::z, NatMap<TB>::w, tid, g.fixed_val, tm);
         __syncthreads();
-        if (tid == 0 && t + gridDim.x < num_tiles) {
+        if (tid < 32 && t + gridDim.x < num_tiles) {
             bulk_wait_read0();
             TileGeo gn = tile_geo(d, t + gridDim.x, n, A.batch);
-            mbar_expect_tx(&bars[(iter + 1) & 1], 2 * tile_bytes(d, gn, n));
-            issue_tile_load(d, gn, psi_src, nps, &bars[(iter + 1) & 1], n);
-            issue_tile_load(d, gn, A.lam, nps + AMPS, &bars[(iter + 1) & 1], n);
+            if (lane == 0) mbar_expect_tx(&bars[(iter + 1) & 1], 2 * tile_bytes(d, gn, n));
+            __syncwarp();
+            issue_tile_load(d, gn, psi_src, nps, &bars[(iter + 1) & 1], n, lane);
+            issue_tile_load(d, gn, A.lam, nps + AMPS, &bars[(iter + 1) & 1], n, lane);
         }
         for (int o = 0; o < d.op_count; ++o) {
             int4 op = __ldg(ops + o);
@@ -755,9 +771,9 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
             }
             fence_proxy_async();
             __syncthreads();
-            if (tid == 0) {
-                issue_tile_store(d, g, A.state, ps, n);
-                issue_tile_store(d, g, A.lam, ls, n);
+            if (tid < 32) {
+                issue_tile_store(d, g, A.state, ps, n, lane);
+                issue_tile_store(d, g, A.lam, ls, n, lane);
                 bulk_commit();
             }
         } else if (store_lam_last) {
@@ -765,15 +781,15 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
             for (int r = 0; r < 32; ++r) ls[nat_index(r, tid)] = lam[r];
             fence_proxy_async();
             __syncthreads();
-            if (tid == 0) {
-                issue_tile_store(d, g, A.lam, ls, n);
+            if (tid < 32) {
+                issue_tile_store(d, g, A.lam, ls, n, lane);
                 bulk_commit();
             }
         }
         fence_proxy_async();
         __syncthreads();
     }
-    if (tid == 0) bulk_wait_all0();
+    if (tid < 32) bulk_wait_all0();
 }
 
 // ------------------------------------------------------------ helpers --
