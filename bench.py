@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="headline only")
     ap.add_argument("--cpu-samples", type=int, default=16, help="samples in the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--tile-bits", type=int, default=13)
+    ap.add_argument("--low-bits", type=int, default=6)
+    ap.add_argument("--k", type=int, default=0, help="max strided qubits per pass (0 = tile limit)")
     ap.add_argument("--n", type=int, default=20)
     ap.add_argument("--batch", type=int, default=256)
     return ap.parse_args()
@@ -201,7 +204,8 @@ def main():
     amp_step = workloads.gate_count(desc) * B * (1 << n)
 
     # ---------------- fused forward, inputs resident in HBM ----------------
-    circ = workloads.build_circuit(desc, engine="fused").to(dev)
+    opts = dict(tile_bits=args.tile_bits, low_bits=args.low_bits, max_high=args.k)
+    circ = workloads.build_circuit(desc, engine="fused", **opts).to(dev)
     kw = workloads.circuit_inputs(desc, dev)
     with torch.no_grad():
         circ(**kw)
@@ -270,10 +274,10 @@ def main():
                                "2 re-uploads, <Z> out (860 gates)",
                    "global_batch": B * world, "qubits": n, "parallelism": f"batch shards x{world}",
                    "l2": "inputs larger than L2 (2 GiB state per GPU)",
-                   "plan": prog.summary()},
+                   "plan": prog.summary(), "tile": opts},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
-                     "kernel": "k_fwd_pass<13>", "launches_per_step": P,
+                     "kernel": f"k_fwd_pass<{args.tile_bits}>", "launches_per_step": P,
                      "avg_launch_ms": avg_pass_ms, "algorithmic_bytes_per_launch": avg_bytes,
                      "middle_pass_GBps": mid_gbs},
         "clocks": clock_info,

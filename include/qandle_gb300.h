@@ -218,6 +218,33 @@ int qg_program_forward_timed(const qg_program* prog, const void* dev_table, void
                              const float* params, const float* named, const void* umats, float* out,
                              void* ckpt, void* const* pass_events, void* stream);
 
+/* ---- building blocks of a forward, for callers that interleave programs
+ * (continuous batching): prepare (matrix tables, embedding factors), one
+ * launch per pass for up to QG_MAX_JOBS independent (program, state) jobs,
+ * finish (measurement reduction). ---- */
+#define QG_MAX_JOBS 32
+
+typedef struct qg_job {
+    const qg_program* prog;
+    const void* table;        /* device tables of prog */
+    void* workspace;          /* forward workspace of this job (prepared) */
+    int64_t workspace_bytes;
+    void* state;              /* [batch][2^n] */
+    int64_t batch;
+    int32_t pass;             /* forward pass index to run */
+    int32_t zero_init;        /* pass 0 starts from |0..0> */
+    float* out;               /* measurement output (probs written by the last pass) */
+} qg_job;
+
+int qg_program_prepare(const qg_program* prog, const void* dev_table, void* workspace,
+                       int64_t workspace_bytes, int64_t batch, const float* params, const float* named,
+                       const void* umats, void* stream);
+/* One kernel launch running pass jobs[i].pass of every job.  The jobs must be
+ * independent (distinct states) and planned with the same tile_bits. */
+int qg_jobs_run_pass(const qg_job* jobs, int njobs, void* stream);
+int qg_program_finish(const qg_program* prog, const void* dev_table, void* workspace,
+                      int64_t workspace_bytes, int64_t batch, float* out, void* stream);
+
 /* Adjoint backward.  state: the forward's final state (overwritten: it is
  * un-computed gate by gate); lam: [B][2^n] buffer.  grad_out is the upstream
  * gradient of the forward output (float [B][n] for P0/<Z>, float [B][2^n]

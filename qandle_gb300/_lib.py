@@ -53,6 +53,15 @@ class PassInfo(ctypes.Structure):
         ("ops", ctypes.POINTER(ctypes.c_int32))]
 
 
+class Job(ctypes.Structure):
+    """qg_job."""
+    _fields_ = [("prog", ctypes.c_void_p), ("table", ctypes.c_void_p), ("workspace", ctypes.c_void_p),
+                ("workspace_bytes", ctypes.c_int64), ("state", ctypes.c_void_p), ("batch", ctypes.c_int64),
+                ("pass_", ctypes.c_int32), ("zero_init", ctypes.c_int32), ("out", ctypes.c_void_p)]
+
+
+MAX_JOBS = 32
+
 GATE = {"rx": 0, "ry": 1, "rz": 2, "u": 3, "cnot": 4, "cz": 5, "swap": 6, "emb": 7}
 MEASURE = {"none": 0, "state": 1, "probs": 2, "p0": 3, "z": 4}
 
@@ -91,6 +100,10 @@ SIGNATURES = {
     "qg_program_forward_timed": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int,
                                          c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                          c_void_p]),
+    "qg_program_prepare": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p,
+                                   c_void_p, c_void_p]),
+    "qg_jobs_run_pass": (c_int, [ctypes.POINTER(Job), c_int, c_void_p]),
+    "qg_program_finish": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p]),
     "qg_program_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
                                     c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p]),

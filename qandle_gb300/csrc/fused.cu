@@ -16,6 +16,8 @@
 // out = in @ M (qandle/operators.py:265-298, :368-395, :125-126).
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "common.cuh"
 #include "engine.h"
 #include "qandle_gb300.h"
@@ -181,6 +183,10 @@ struct ThreadMap {
     int thr_off;     // local-index contribution of this thread's lane/warp bits
     uint32_t tglob;  // global-bit values of this thread's qubit thread bits | tile fixed bits
     int sample_off;  // sample offset within the tile (n < TB)
+    // The swizzle is linear over GF(2) and the thread and register parts of a
+    // local index have disjoint bits, so slot(r) = sw_base ^ XOR_k(bit k of r ? sw[k] : 0).
+    int sw[5];
+    int sw_base;
 };
 
 __device__ __forceinline__ void decode_map(const PassDesc& d, int32_t y, int32_t z, int32_t w, int tid,
@@ -201,6 +207,8 @@ __device__ __forceinline__ void decode_map(const PassDesc& d, int32_t y, int32_t
     m.thr_off = off;
     m.tglob = tg;
     m.sample_off = soff;
+    for (int k = 0; k < 5; ++k) m.sw[k] = swz(1 << m.regl[k]);
+    m.sw_base = swz(off);
 }
 
 template <int K>
@@ -218,14 +226,20 @@ __device__ __forceinline__ int roff_rt(const ThreadMap& m, int r) {
     return o;
 }
 
+template <int K>
+__device__ __forceinline__ int xslot(const ThreadMap& m) {
+    return m.sw_base ^ ((K & 1) ? m.sw[0] : 0) ^ ((K & 2) ? m.sw[1] : 0) ^ ((K & 4) ? m.sw[2] : 0) ^
+           ((K & 8) ? m.sw[3] : 0) ^ ((K & 16) ? m.sw[4] : 0);
+}
+
 template <int K = 0>
 __device__ __forceinline__ void xwrite(float2* buf, const float2 (&a)[32], const ThreadMap& m) {
-    buf[swz(m.thr_off + roff<K>(m))] = a[K];
+    buf[xslot<K>(m)] = a[K];
     if constexpr (K + 1 < 32) xwrite<K + 1>(buf, a, m);
 }
 template <int K = 0>
 __device__ __forceinline__ void xread(const float2* buf, float2 (&a)[32], const ThreadMap& m) {
-    a[K] = buf[swz(m.thr_off + roff<K>(m))];
+    a[K] = buf[xslot<K>(m)];
     if constexpr (K + 1 < 32) xread<K + 1>(buf, a, m);
 }
 
@@ -265,16 +279,38 @@ __device__ __forceinline__ void diag_reg(float2 (&a)[32], float2 d0, float2 d1) 
     for (int r = 0; r < 32; ++r) a[r] = cmul(a[r], (r & (1 << P)) ? d1 : d0);
 }
 
-// X on register position P when (ctrl_reg >= 0 ? bit ctrl_reg of r : tcond)
+// X on register position P when the thread-uniform control `tcond` holds
 template <int P>
-__device__ __forceinline__ void cx_reg(float2 (&a)[32], int ctrl_reg, bool tcond) {
+__device__ __forceinline__ void cx_reg(float2 (&a)[32], int /*ctrl_reg*/, bool tcond) {
 #pragma unroll
     for (int r = 0; r < 32; ++r) {
         if (r & (1 << P)) continue;
-        bool c = ctrl_reg >= 0 ? ((r >> ctrl_reg) & 1) : tcond;
         float2 x = a[r], y = a[r | (1 << P)];
-        a[r] = c ? y : x;
-        a[r | (1 << P)] = c ? x : y;
+        a[r] = tcond ? y : x;
+        a[r | (1 << P)] = tcond ? x : y;
+    }
+}
+
+// X on register position P where register bit C of r is 1: a fixed permutation
+template <int P, int C>
+__device__ __forceinline__ void cx_rr(float2 (&a)[32]) {
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+        if ((r & (1 << P)) || !(r & (1 << C))) continue;
+        float2 t = a[r];
+        a[r] = a[r | (1 << P)];
+        a[r | (1 << P)] = t;
+    }
+}
+
+template <int P>
+__device__ __forceinline__ void cx_rr_dispatch(int c, float2 (&a)[32]) {
+    switch (c) {
+        case 0: if (P != 0) cx_rr<P, 0>(a); break;
+        case 1: if (P != 1) cx_rr<P, 1>(a); break;
+        case 2: if (P != 2) cx_rr<P, 2>(a); break;
+        case 3: if (P != 3) cx_rr<P, 3>(a); break;
+        default: if (P != 4) cx_rr<P, 4>(a); break;
     }
 }
 
@@ -386,15 +422,24 @@ __device__ __forceinline__ void apply_op(const int4 op, float2 (&a)[32], const T
             break;
         }
         case OP_CX: {
-            int cr = (op.z & LOC_REG) ? (op.z & 7) : -1;
-            bool tc = cr < 0 ? loc_bit_thread(op.z, tm.tglob) : false;
-            if (cr < 0 && !tc) break;
+            if (op.z & LOC_REG) {
+                int cr = op.z & 7;
+                switch (op.y) {
+                    case 0: cx_rr_dispatch<0>(cr, a); break;
+                    case 1: cx_rr_dispatch<1>(cr, a); break;
+                    case 2: cx_rr_dispatch<2>(cr, a); break;
+                    case 3: cx_rr_dispatch<3>(cr, a); break;
+                    default: cx_rr_dispatch<4>(cr, a); break;
+                }
+                break;
+            }
+            bool tc = loc_bit_thread(op.z, tm.tglob);
             switch (op.y) {
-                case 0: cx_reg<0>(a, cr, tc); break;
-                case 1: cx_reg<1>(a, cr, tc); break;
-                case 2: cx_reg<2>(a, cr, tc); break;
-                case 3: cx_reg<3>(a, cr, tc); break;
-                default: cx_reg<4>(a, cr, tc); break;
+                case 0: cx_reg<0>(a, -1, tc); break;
+                case 1: cx_reg<1>(a, -1, tc); break;
+                case 2: cx_reg<2>(a, -1, tc); break;
+                case 3: cx_reg<3>(a, -1, tc); break;
+                default: cx_reg<4>(a, -1, tc); break;
             }
             break;
         }
@@ -427,11 +472,37 @@ struct PassSmem {
     static constexpr int kThreads = 1 << (TB - 5);
 };
 
-// Forward pass kernel.  One persistent CTA per SM.
-template <int TB>
-__global__ void __launch_bounds__(1 << (TB - 5), 1)
-    k_fwd_pass(const PassDesc* __restrict__ passes, const int4* __restrict__ ops_all, int pass_index, RunArgs A,
-               int zero_init, const EmbedDesc* __restrict__ emb, int64_t num_tiles) {
+// One pass of one program over one state: an entry of a multi-job launch.
+struct JobDesc {
+    const PassDesc* pd;   // device pass descriptor
+    const int4* ops;      // device ops of the pass
+    RunArgs A;
+    int32_t zero_init;    // start from |0..0> instead of loading the state
+    int32_t pad;
+    int64_t tiles;
+};
+
+template <int MAXJ>
+struct JobTable {
+    int32_t njobs;
+    int32_t pad;
+    int64_t begin[MAXJ + 1];  // first global tile of each job; begin[njobs] = total
+    JobDesc job[MAXJ];
+};
+
+template <int MAXJ>
+__device__ __forceinline__ int find_job(const JobTable<MAXJ>& jt, int64_t t) {
+    int j = 0;
+    while (j + 1 < jt.njobs && t >= jt.begin[j + 1]) ++j;
+    return j;
+}
+
+// Forward pass kernel.  One persistent CTA per SM walks the tiles of every job
+// of the launch (the passes of independent programs / states, e.g. several
+// serving requests of different widths); a single-program forward is a
+// one-job launch.
+template <int TB, int MAXJ>
+__global__ void __launch_bounds__(1 << (TB - 5), (TB <= 12 ? 2 : 1)) k_fwd_pass(const __grid_constant__ JobTable<MAXJ> jt) {
     constexpr int NT = 1 << (TB - 5);
     constexpr int AMPS = 1 << TB;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -439,37 +510,64 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
     float2* buf1 = buf0 + AMPS;
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ PassDesc sd;
+    __shared__ RunArgs sa;
 
     const int tid = threadIdx.x;
     const int lane = tid & 31;
+    const int64_t total = jt.begin[jt.njobs];
     if (tid == 0) {
-        sd = passes[pass_index];
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    const PassDesc& d = sd;
-    const int4* ops = ops_all + d.op_begin;
-    const int n = A.n;
-    const bool load_in = (d.init == INIT_LOAD) && !zero_init;
+
+    // loads in flight per buffer: a buffer's mbarrier completes once per load
+    uint32_t phase[2] = {0u, 0u};
+    auto tile_loads = [&](int j) -> bool {
+        return jt.job[j].pd->init == INIT_LOAD && !jt.job[j].zero_init;
+    };
+    auto issue_prefetch = [&](int64_t t, float2* dst, uint64_t* bar) {
+        // warp 0 only
+        int j = find_job(jt, t);
+        const PassDesc& pd = *jt.job[j].pd;
+        const RunArgs& ra = jt.job[j].A;
+        TileGeo gn = tile_geo(pd, t - jt.begin[j], ra.n, ra.batch);
+        if (lane == 0) mbar_expect_tx(bar, tile_bytes(pd, gn, ra.n));
+        __syncwarp();
+        issue_tile_load(pd, gn, ra.state, dst, bar, ra.n, lane);
+    };
 
     int64_t t0 = blockIdx.x;
-    if (load_in && tid < 32 && t0 < num_tiles) {
-        TileGeo g = tile_geo(d, t0, n, A.batch);
-        if (lane == 0) mbar_expect_tx(&bars[0], tile_bytes(d, g, n));
-        __syncwarp();
-        issue_tile_load(d, g, A.state, buf0, &bars[0], n, lane);
+    if (t0 < total && tile_loads(find_job(jt, t0))) {
+        if (tid < 32) issue_prefetch(t0, buf0, &bars[0]);
     }
+    int cur_job = -1;
     int iter = 0;
-    for (int64_t t = t0; t < num_tiles; t += gridDim.x, ++iter) {
+    for (int64_t t = t0; t < total; t += gridDim.x, ++iter) {
         float2* buf = (iter & 1) ? buf1 : buf0;
         float2* nbuf = (iter & 1) ? buf0 : buf1;
-        TileGeo g = tile_geo(d, t, n, A.batch);
+        const int j = find_job(jt, t);
+        if (j != cur_job) {
+            __syncthreads();  // nobody reads the previous job's descriptors any more
+            if (tid == 0) {
+                sd = *jt.job[j].pd;
+                sa = jt.job[j].A;
+            }
+            __syncthreads();
+            cur_job = j;
+        }
+        const PassDesc& d = sd;
+        const RunArgs& A = sa;
+        const int4* ops = jt.job[j].ops;
+        const int n = A.n;
+        const bool load_in = tile_loads(j);
+        TileGeo g = tile_geo(d, t - jt.begin[j], n, A.batch);
         float2 a[32];
         ThreadMap tm;
         if (load_in) {
-            bool ok = mbar_wait(&bars[iter & 1], (iter >> 1) & 1);
+            bool ok = mbar_wait(&bars[iter & 1], phase[iter & 1] & 1);
+            ++phase[iter & 1];
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) atomicExch(A.status, QG_ETIMEOUT);
                 break;
@@ -519,14 +617,10 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
         }
         // everybody has read `buf`; prefetch the next tile into the other buffer
         __syncthreads();
-        if (load_in && tid < 32 && t + gridDim.x < num_tiles) {
+        if (tid < 32 && t + gridDim.x < total && tile_loads(find_job(jt, t + gridDim.x))) {
             bulk_wait_read0();  // stores issued from nbuf two tiles ago have read it
-            TileGeo gn = tile_geo(d, t + gridDim.x, n, A.batch);
-            if (lane == 0) mbar_expect_tx(&bars[(iter + 1) & 1], tile_bytes(d, gn, n));
-            __syncwarp();
-            issue_tile_load(d, gn, A.state, nbuf, &bars[(iter + 1) & 1], n, lane);
+            issue_prefetch(t + gridDim.x, nbuf, &bars[(iter + 1) & 1]);
         }
-        const int64_t my_sample = g.sample + tm.sample_off;
         // ---- the gate program of this pass ----
         for (int o = 0; o < d.op_count; ++o) {
             int4 op = __ldg(ops + o);
@@ -540,7 +634,6 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
                 apply_op(op, a, tm, A, g.sample + tm.sample_off, false);
             }
         }
-        (void)my_sample;
         // ---- epilogue (the planner left the natural mapping) ----
         __syncthreads();  // all exchange reads of `buf` are done
         const int64_t smp0 = g.sample;
@@ -585,12 +678,11 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
                     float v = chunk[idx];
                     tot += v;
 #pragma unroll
-                    for (int j = 0; j < 5; ++j) sj[j] += ((idx >> j) & 1) ? 0.f : v;
+                    for (int jj = 0; jj < 5; ++jj) sj[jj] += ((idx >> jj) & 1) ? 0.f : v;
                 }
-                __syncthreads();  // every chunk is read before the partial arrays overwrite nothing
                 ptot[tid] = tot;
 #pragma unroll
-                for (int j = 0; j < 5; ++j) psub[j * NT + tid] = sj[j];
+                for (int jj = 0; jj < 5; ++jj) psub[jj * NT + tid] = sj[jj];
                 __syncthreads();
                 // phase B: (sample, local bit) items
                 const int nq = d.nq_tile;
@@ -599,37 +691,37 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
                 const int items = spt * (nq + 1);
                 const int64_t tps = (n >= TB) ? (int64_t(1) << (n - TB)) : 1;
                 if (cps >= 32) {
-                    const int warp = tid >> 5, lane = tid & 31;
+                    const int warp = tid >> 5;
                     for (int it = warp; it < items; it += NT / 32) {
-                        int s = it / (nq + 1), j = it % (nq + 1);
+                        int s = it / (nq + 1), jj = it % (nq + 1);
                         float acc = 0.f;
                         for (int c = lane; c < cps; c += 32) {
                             int t2 = s * cps + c;
-                            if (j < 5) acc += psub[j * NT + t2];
-                            else if (j < nq) acc += ((t2 >> (j - 5)) & 1) ? 0.f : ptot[t2];
+                            if (jj < 5) acc += psub[jj * NT + t2];
+                            else if (jj < nq) acc += ((t2 >> (jj - 5)) & 1) ? 0.f : ptot[t2];
                             else acc += ptot[t2];
                         }
                         for (int o2 = 16; o2 > 0; o2 >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o2);
                         if (lane == 0 && s < g.nsamples) {
                             int64_t smp = smp0 + s;
                             float* dst = A.p0part + ((smp * tps + g.tile_in_sample) * (TB + 1));
-                            dst[j < nq ? j : TB] = acc;
+                            dst[jj < nq ? jj : TB] = acc;
                         }
                     }
                 } else {
                     for (int it = tid; it < items; it += NT) {
-                        int s = it / (nq + 1), j = it % (nq + 1);
+                        int s = it / (nq + 1), jj = it % (nq + 1);
                         float acc = 0.f;
                         for (int c = 0; c < cps; ++c) {
                             int t2 = s * cps + c;
-                            if (j < 5) acc += psub[j * NT + t2];
-                            else if (j < nq) acc += ((t2 >> (j - 5)) & 1) ? 0.f : ptot[t2];
+                            if (jj < 5) acc += psub[jj * NT + t2];
+                            else if (jj < nq) acc += ((t2 >> (jj - 5)) & 1) ? 0.f : ptot[t2];
                             else acc += ptot[t2];
                         }
                         if (s < g.nsamples) {
                             int64_t smp = smp0 + s;
                             float* dst = A.p0part + ((smp * tps + g.tile_in_sample) * (TB + 1));
-                            dst[j < nq ? j : TB] = acc;
+                            dst[jj < nq ? jj : TB] = acc;
                         }
                     }
                 }
@@ -640,7 +732,6 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
         __syncthreads();
     }
     if (tid < 32) bulk_wait_all0();
-    (void)emb;
 }
 
 // Backward pass kernel: psi and lambda tiles (TB = 12), gradient partials.
@@ -1029,20 +1120,44 @@ static BwdLayout bwd_layout(const ProgramRun& R, int64_t B) {
     return L;
 }
 
-template <int TB>
-static int launch_fwd_pass(const PassDesc* dpass, const int4* dops, int p, const RunArgs& A, int zero_init,
-                           const EmbedDesc* demb, int64_t tiles, cudaStream_t st) {
+template <int TB, int MAXJ>
+static int launch_fwd_jobs(const JobTable<MAXJ>& jt, cudaStream_t st) {
     constexpr int NT = 1 << (TB - 5);
     size_t smem = 2 * (size_t(1) << TB) * sizeof(float2);
     static bool attr_set = false;
     if (!attr_set) {
-        QG_CUDA_TRY(cudaFuncSetAttribute(k_fwd_pass<TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        QG_CUDA_TRY(
+            cudaFuncSetAttribute(k_fwd_pass<TB, MAXJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = true;
     }
-    int64_t grid = tiles < sm_count() ? tiles : sm_count();
-    k_fwd_pass<TB><<<(unsigned)grid, NT, smem, st>>>(dpass, dops, p, A, zero_init, demb, tiles);
+    int64_t tiles = jt.begin[jt.njobs];
+    if (tiles <= 0) return QG_OK;
+    static int per_sm = 0;
+    if (!per_sm) {
+        QG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fwd_pass<TB, MAXJ>, NT, smem));
+        if (per_sm < 1) per_sm = 1;
+    }
+    int64_t slots = (int64_t)sm_count() * per_sm;  // persistent: every resident CTA walks tiles
+    int64_t grid = tiles < slots ? tiles : slots;
+    k_fwd_pass<TB, MAXJ><<<(unsigned)grid, NT, smem, st>>>(jt);
     QG_LAUNCH_CHECK();
     return QG_OK;
+}
+
+template <int TB>
+static int launch_fwd_pass(const PassDesc* dpass, const int4* dops, const PassDesc& hpass, int p, const RunArgs& A,
+                           int zero_init, int64_t tiles, cudaStream_t st) {
+    JobTable<1> jt;
+    memset(&jt, 0, sizeof(jt));
+    jt.njobs = 1;
+    jt.begin[0] = 0;
+    jt.begin[1] = tiles;
+    jt.job[0].pd = dpass + p;
+    jt.job[0].ops = dops + hpass.op_begin;
+    jt.job[0].A = A;
+    jt.job[0].zero_init = zero_init;
+    jt.job[0].tiles = tiles;
+    return launch_fwd_jobs<TB, 1>(jt, st);
 }
 
 template <int TB>
@@ -1055,7 +1170,13 @@ static int launch_bwd_pass(const PassDesc* dpass, const int4* dops, int p, const
         QG_CUDA_TRY(cudaFuncSetAttribute(k_bwd_pass<TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = true;
     }
-    int64_t grid = tiles < sm_count() ? tiles : sm_count();
+    static int per_sm = 0;
+    if (!per_sm) {
+        QG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bwd_pass<TB>, NT, smem));
+        if (per_sm < 1) per_sm = 1;
+    }
+    int64_t slots = (int64_t)sm_count() * per_sm;
+    int64_t grid = tiles < slots ? tiles : slots;
     k_bwd_pass<TB><<<(unsigned)grid, NT, smem, st>>>(dpass, dops, p, A, store_lam, tiles);
     QG_LAUNCH_CHECK();
     return QG_OK;
@@ -1085,29 +1206,21 @@ int qg_program_forward(const qg_program* prog, const void* dev_table, void* work
                                     named, umats, out, ckpt, nullptr, stream);
 }
 
-int qg_program_forward_timed(const qg_program* prog, const void* dev_table, void* workspace,
-                             int64_t workspace_bytes, void* state, int64_t batch, int zero_init, const float* params,
-                             const float* named, const void* umats, float* out, void* ckpt,
-                             void* const* pass_events, void* stream) {
+static int fwd_args(const qg_program* prog, const void* dev_table, void* workspace, int64_t workspace_bytes,
+                    void* state, int64_t batch, float* out, void* ckpt, qg::ProgramRun& R, qg::RunArgs& A,
+                    qg::FwdLayout& L) {
     using namespace qg;
     QG_CHECK_ARG(prog && dev_table && workspace && state, "null pointer");
     QG_CHECK_ARG(batch >= 1, "batch must be >= 1");
     QG_CHECK_ARG(((uintptr_t)state & 15) == 0, "state must be 16-byte aligned");
-    ProgramRun R;
     program_run_info(prog, &R);
-    FwdLayout L = fwd_layout(R, batch);
+    L = fwd_layout(R, batch);
     QG_CHECK_ARG(workspace_bytes >= (int64_t)L.total, "workspace too small");
-    QG_CHECK_ARG(R.nparams == 0 || params, "params is null");
-    QG_CHECK_ARG(R.ncols == 0 || named, "named inputs are null");
-    QG_CHECK_ARG(R.numats == 0 || umats, "umats is null");
     bool p0 = R.measure == QG_MEASURE_P0 || R.measure == QG_MEASURE_Z;
     QG_CHECK_ARG(!(p0 || R.measure == QG_MEASURE_PROBS) || out, "out is null");
-    QG_CHECK_ARG(R.segments <= 1 || ckpt, "checkpoint buffer is null");
     QG_CHECK_ARG(!out || ((uintptr_t)out & 15) == 0, "out must be 16-byte aligned");
-    cudaStream_t st = (cudaStream_t)stream;
     char* ws = (char*)workspace;
-    const char* tab = (const char*)dev_table;
-    RunArgs A{};
+    A = RunArgs{};
     A.state = (float2*)state;
     A.ckpt = (float2*)ckpt;
     A.out = out;
@@ -1119,6 +1232,24 @@ int qg_program_forward_timed(const qg_program* prog, const void* dev_table, void
     A.batch = batch;
     A.n = R.n;
     A.nslots_ps = R.f_ps;
+    return QG_OK;
+}
+
+int qg_program_prepare(const qg_program* prog, const void* dev_table, void* workspace, int64_t workspace_bytes,
+                       int64_t batch, const float* params, const float* named, const void* umats, void* stream) {
+    using namespace qg;
+    QG_CHECK_ARG(prog && dev_table && workspace, "null pointer");
+    QG_CHECK_ARG(batch >= 1, "batch must be >= 1");
+    ProgramRun R;
+    program_run_info(prog, &R);
+    FwdLayout L = fwd_layout(R, batch);
+    QG_CHECK_ARG(workspace_bytes >= (int64_t)L.total, "workspace too small");
+    QG_CHECK_ARG(R.nparams == 0 || params, "params is null");
+    QG_CHECK_ARG(R.ncols == 0 || named, "named inputs are null");
+    QG_CHECK_ARG(R.numats == 0 || umats, "umats is null");
+    cudaStream_t st = (cudaStream_t)stream;
+    char* ws = (char*)workspace;
+    const char* tab = (const char*)dev_table;
     QG_CUDA_TRY(cudaMemsetAsync(ws + L.status, 0, 16, st));
     int64_t items = R.f_shared + (int64_t)R.f_ps * batch;
     if (items > 0) {
@@ -1133,28 +1264,97 @@ int qg_program_forward_timed(const qg_program* prog, const void* dev_table, void
                                                          batch, R.n, (float2*)(ws + L.embfac));
         QG_LAUNCH_CHECK();
     }
+    return QG_OK;
+}
+
+int qg_program_finish(const qg_program* prog, const void* dev_table, void* workspace, int64_t workspace_bytes,
+                      int64_t batch, float* out, void* stream) {
+    using namespace qg;
+    QG_CHECK_ARG(prog && dev_table && workspace, "null pointer");
+    ProgramRun R;
+    program_run_info(prog, &R);
+    FwdLayout L = fwd_layout(R, batch);
+    QG_CHECK_ARG(workspace_bytes >= (int64_t)L.total, "workspace too small");
+    bool p0 = R.measure == QG_MEASURE_P0 || R.measure == QG_MEASURE_Z;
+    if (!p0) return QG_OK;
+    QG_CHECK_ARG(out, "out is null");
+    const PassDesc* dpass = (const PassDesc*)((const char*)dev_table + R.off_fpass);
+    k_p0_finalize<<<grid_for(batch * R.n, 128), 128, 0, (cudaStream_t)stream>>>(
+        dpass + (R.nfpass - 1), (const float*)((char*)workspace + L.p0part), out, batch, R.n, R.tile_bits,
+        R.measure == QG_MEASURE_Z);
+    QG_LAUNCH_CHECK();
+    return QG_OK;
+}
+
+int qg_jobs_run_pass(const qg_job* jobs, int njobs, void* stream) {
+    using namespace qg;
+    QG_CHECK_ARG(njobs >= 0 && njobs <= QG_MAX_JOBS, "njobs must be in [0, 32]");
+    QG_CHECK_ARG(njobs == 0 || jobs, "jobs is null");
+    if (njobs == 0) return QG_OK;
+    JobTable<QG_MAX_JOBS> jt;
+    memset(&jt, 0, sizeof(jt));
+    int tb = -1;
+    int64_t acc = 0;
+    for (int i = 0; i < njobs; ++i) {
+        const qg_job& q = jobs[i];
+        ProgramRun R;
+        RunArgs A;
+        FwdLayout L;
+        int rc = fwd_args(q.prog, q.table, q.workspace, q.workspace_bytes, q.state, q.batch, q.out, nullptr, R, A, L);
+        if (rc) return rc;
+        QG_CHECK_ARG(q.pass >= 0 && q.pass < R.nfpass, "pass index out of range");
+        QG_CHECK_ARG(R.segments <= 1, "checkpointed programs run through qg_program_forward");
+        if (tb < 0) tb = R.tile_bits;
+        QG_CHECK_ARG(tb == R.tile_bits, "all jobs of one launch need the same tile_bits");
+        const char* tab = (const char*)q.table;
+        jt.job[i].pd = (const PassDesc*)(tab + R.off_fpass) + q.pass;
+        jt.job[i].ops = (const int4*)(tab + R.off_fops) + R.fpass[q.pass].op_begin;
+        jt.job[i].A = A;
+        jt.job[i].zero_init = (q.pass == 0) ? q.zero_init : 0;
+        jt.job[i].tiles = num_tiles(R.n, R.tile_bits, q.batch);
+        jt.begin[i] = acc;
+        acc += jt.job[i].tiles;
+    }
+    jt.njobs = njobs;
+    jt.begin[njobs] = acc;
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (tb) {
+        case 13: return launch_fwd_jobs<13, QG_MAX_JOBS>(jt, st);
+        case 12: return launch_fwd_jobs<12, QG_MAX_JOBS>(jt, st);
+        default: return launch_fwd_jobs<11, QG_MAX_JOBS>(jt, st);
+    }
+}
+
+int qg_program_forward_timed(const qg_program* prog, const void* dev_table, void* workspace,
+                             int64_t workspace_bytes, void* state, int64_t batch, int zero_init, const float* params,
+                             const float* named, const void* umats, float* out, void* ckpt,
+                             void* const* pass_events, void* stream) {
+    using namespace qg;
+    ProgramRun R;
+    RunArgs A;
+    FwdLayout L;
+    int rc = fwd_args(prog, dev_table, workspace, workspace_bytes, state, batch, out, ckpt, R, A, L);
+    if (rc) return rc;
+    QG_CHECK_ARG(R.segments <= 1 || ckpt, "checkpoint buffer is null");
+    rc = qg_program_prepare(prog, dev_table, workspace, workspace_bytes, batch, params, named, umats, stream);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const char* tab = (const char*)dev_table;
     const PassDesc* dpass = (const PassDesc*)(tab + R.off_fpass);
     const int4* dops = (const int4*)(tab + R.off_fops);
-    const EmbedDesc* demb = (const EmbedDesc*)(tab + R.off_embed);
     int64_t tiles = num_tiles(R.n, R.tile_bits, batch);
     for (int p = 0; p < R.nfpass; ++p) {
         int zi = (p == 0) ? zero_init : 0;
-        int rc;
         if (pass_events) QG_CUDA_TRY(cudaEventRecord((cudaEvent_t)pass_events[2 * p], st));
         switch (R.tile_bits) {
-            case 13: rc = launch_fwd_pass<13>(dpass, dops, p, A, zi, demb, tiles, st); break;
-            case 12: rc = launch_fwd_pass<12>(dpass, dops, p, A, zi, demb, tiles, st); break;
-            default: rc = launch_fwd_pass<11>(dpass, dops, p, A, zi, demb, tiles, st); break;
+            case 13: rc = launch_fwd_pass<13>(dpass, dops, R.fpass[p], p, A, zi, tiles, st); break;
+            case 12: rc = launch_fwd_pass<12>(dpass, dops, R.fpass[p], p, A, zi, tiles, st); break;
+            default: rc = launch_fwd_pass<11>(dpass, dops, R.fpass[p], p, A, zi, tiles, st); break;
         }
         if (rc) return rc;
         if (pass_events) QG_CUDA_TRY(cudaEventRecord((cudaEvent_t)pass_events[2 * p + 1], st));
     }
-    if (p0) {
-        k_p0_finalize<<<grid_for(batch * R.n, 128), 128, 0, st>>>(dpass + (R.nfpass - 1), A.p0part, out, batch, R.n,
-                                                                  R.tile_bits, R.measure == QG_MEASURE_Z);
-        QG_LAUNCH_CHECK();
-    }
-    return QG_OK;
+    return qg_program_finish(prog, dev_table, workspace, workspace_bytes, batch, out, stream);
 }
 
 int qg_program_backward(const qg_program* prog, const void* dev_table, void* workspace, int64_t workspace_bytes,
