@@ -1,0 +1,256 @@
+"""Continuous-batching serving loop for circuit evaluations.
+
+Requests are circuits from the strongly-entangling family (AngleEmbedding,
+RZ RY RZ layers, CNOT rings, <Z> out) of 4..24 qubits and any batch.  The
+loop keeps every admitted request's state, matrix tables and embedding
+factors on the device and advances all admitted requests together: each
+step is ONE multi-job launch of the fused pass kernel (qg_jobs_run_pass)
+that runs the next pass of every active request, whatever its width.  New
+requests are admitted between steps as soon as the HBM budget
+(sum of 2^n * 8 B * batch over admitted requests) has room, so requests that
+arrive while others are on the GPU join the running batch instead of
+waiting for it to drain.
+
+Each request's tiles are computed by the same code in the same order
+whatever else shares the launch, and its reductions run in a fixed order,
+so a request's result is bit-identical alone and in the mix.
+
+There is no CPU path: the loop drives the CUDA library through its C ABI.
+"""
+from __future__ import annotations
+
+import collections
+import concurrent.futures as cf
+import ctypes
+import threading
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .engine import Lowered, Program
+
+_ROT = {"rx": 0, "ry": 1, "rz": 2}
+
+
+def lower_description(desc: dict, pad_to: int = 5):
+    """Gate records and runtime values of a circuit description (see
+    qandle_gb300.workloads).  Circuits narrower than `pad_to` qubits get idle
+    qubits prepended (qubit indices shift up), which leaves <Z> of the real
+    qubits unchanged; returns (lowered, params, named [B, ncols], shift)."""
+    n = desc["n"]
+    shift = max(0, pad_to - n)
+    lo = Lowered(n + shift)
+    params, cols = [], []
+    inputs = desc.get("inputs", {})
+    for g in desc["gates"]:
+        k = g[0]
+        if k == "emb":
+            qs = [q + shift for q in g[3]]
+            lo.gates.append((_lib.GATE["emb"], _ROT[g[1]], len(qs), 1, len(lo.named_cols), len(lo.qlist)))
+            x = np.asarray(inputs[g[2]], dtype=np.float32)
+            for j in range(len(qs)):
+                lo.named_cols.append((g[2], j))
+                cols.append(x[..., j])
+            lo.qlist.extend(qs)
+        elif k in _ROT:
+            if g[3] is None:
+                lo.gates.append((_ROT[k], g[1] + shift, 0, 0, len(params), 0))
+                params.append(np.float32(g[2]))
+            else:
+                lo.gates.append((_ROT[k], g[1] + shift, 0, 1, len(lo.named_cols), 0))
+                lo.named_cols.append((g[3], None))
+                cols.append(np.asarray(inputs[g[3]], dtype=np.float32))
+        elif k in ("cnot", "cz", "swap"):
+            lo.gates.append((_lib.GATE[k], g[1] + shift, g[2] + shift, 0, 0, 0))
+        else:
+            raise ValueError(f"the serving loop does not take gate {k}")
+    lo.measure = desc.get("measure", "z")
+    B = desc["batch"] or 1
+    named = (np.stack([np.broadcast_to(c, (B,)) for c in cols], 1).astype(np.float32)
+             if cols else np.zeros((B, 1), np.float32))
+    return lo, np.asarray(params + [np.float32(0)], np.float32), named, shift
+
+
+def structure_key(lo: Lowered):
+    return (lo.n, lo.measure, tuple(lo.gates), tuple(lo.qlist))
+
+
+class _Slot:
+    __slots__ = ("req", "prog", "state", "ws", "out", "host_out", "batch", "next_pass", "bytes",
+                 "event", "params", "named", "umats", "shift")
+
+
+class Request:
+    def __init__(self, desc: dict, arrival: float | None = None):
+        self.desc = desc
+        self.arrival = time.perf_counter() if arrival is None else arrival
+        self.admitted = None
+        self.completed = None
+        self.future: cf.Future = cf.Future()
+
+    @property
+    def latency(self):
+        return None if self.completed is None else self.completed - self.arrival
+
+
+class Server:
+    """Continuous-batching executor on one device.
+
+    hbm_budget: bytes of state the admitted requests may hold together
+    (2^n * 8 B * batch each).  max_active: requests advanced per step (a
+    multiple of the 32 jobs one launch takes means several launches).
+    """
+
+    def __init__(self, device="cuda", hbm_budget: int = 64 << 30, max_active: int = 64,
+                 tile_bits: int = 13, low_bits: int = 6):
+        self.device = torch.device(device)
+        self.budget = int(hbm_budget)
+        self.max_active = max_active
+        self.opts = dict(tile_bits=tile_bits, low_bits=low_bits)
+        self.programs: dict = {}
+        self.stream = torch.cuda.Stream(device=self.device)
+        self._queue = collections.deque()
+        self._cv = threading.Condition()
+        self._stop = False
+        self._completing = collections.deque()
+        self._used = 0
+        self.steps = 0
+        self.launches = 0
+        self._worker = threading.Thread(target=self._run, daemon=True)
+        self._poller = threading.Thread(target=self._poll, daemon=True)
+        self._worker.start()
+        self._poller.start()
+
+    # -- public --
+    def submit(self, desc: dict, arrival: float | None = None) -> Request:
+        req = Request(desc, arrival)
+        need = self._state_bytes(desc)
+        if need > self.budget:
+            req.future.set_exception(MemoryError(
+                f"request needs {need} bytes of state, more than the HBM budget {self.budget}"))
+            return req
+        with self._cv:
+            self._queue.append(req)
+            self._cv.notify()
+        return req
+
+    def close(self):
+        with self._cv:
+            self._stop = True
+            self._cv.notify()
+        self._worker.join()
+        self._poller.join()
+
+    # -- internals --
+    @staticmethod
+    def _state_bytes(desc):
+        n = max(desc["n"], 5)
+        return (1 << n) * 8 * (desc["batch"] or 1)
+
+    def _program(self, lo: Lowered) -> Program:
+        key = structure_key(lo)
+        p = self.programs.get(key)
+        if p is None:
+            p = Program(lo, lo.measure, keep_state=False, **self.opts)
+            self.programs[key] = p
+        return p
+
+    def _admit(self, req: Request) -> _Slot:
+        lo, params, named, shift = lower_description(req.desc)
+        prog = self._program(lo)
+        B = req.desc["batch"] or 1
+        n = lo.n
+        s = _Slot()
+        s.req, s.prog, s.batch, s.next_pass, s.shift = req, prog, B, 0, shift
+        s.bytes = (1 << n) * 8 * B
+        dev = self.device
+        s.state = torch.empty(B, 1 << n, dtype=torch.complex64, device=dev)
+        s.ws = prog.workspace(B, False, dev)
+        s.out = torch.empty(B, n, dtype=torch.float32, device=dev)
+        s.host_out = torch.empty(B, n, dtype=torch.float32, pin_memory=True)
+        s.params = torch.from_numpy(params).pin_memory().to(dev, non_blocking=True)
+        s.named = torch.from_numpy(np.ascontiguousarray(named)).pin_memory().to(dev, non_blocking=True)
+        s.umats = torch.zeros(1, 2, 2, dtype=torch.complex64, device=dev)
+        _lib.call("qg_program_prepare", prog.handle, prog.table(dev).data_ptr(), s.ws.data_ptr(), s.ws.numel(),
+                  B, s.params.data_ptr(), s.named.data_ptr(), s.umats.data_ptr(), self.stream.cuda_stream)
+        req.admitted = time.perf_counter()
+        return s
+
+    def _run(self):
+        lib = _lib.load()
+        active: list[_Slot] = []
+        with torch.cuda.device(self.device), torch.cuda.stream(self.stream):
+            while True:
+                with self._cv:
+                    while not self._queue and not active and not self._stop:
+                        self._cv.wait()
+                    if self._stop and not self._queue and not active:
+                        break
+                    # admit against the HBM budget, oldest first
+                    while self._queue and len(active) < self.max_active:
+                        need = self._state_bytes(self._queue[0].desc)
+                        if self._used + need > self.budget:
+                            break
+                        req = self._queue.popleft()
+                        self._used += need
+                        active.append(self._admit(req))
+                if not active:
+                    continue
+                # one step: the next pass of every active request
+                for base in range(0, len(active), _lib.MAX_JOBS):
+                    chunk = active[base:base + _lib.MAX_JOBS]
+                    jobs = (_lib.Job * len(chunk))()
+                    for i, s in enumerate(chunk):
+                        jobs[i] = _lib.Job(s.prog.handle, s.prog.table(self.device).data_ptr(), s.ws.data_ptr(),
+                                           s.ws.numel(), s.state.data_ptr(), s.batch, s.next_pass, 0,
+                                           s.out.data_ptr())
+                    _lib.check(lib.qg_jobs_run_pass(jobs, len(chunk), self.stream.cuda_stream))
+                    self.launches += 1
+                self.steps += 1
+                still = []
+                for s in active:
+                    s.next_pass += 1
+                    if s.next_pass < s.prog.info.forward_passes:
+                        still.append(s)
+                        continue
+                    _lib.call("qg_program_finish", s.prog.handle, s.prog.table(self.device).data_ptr(),
+                              s.ws.data_ptr(), s.ws.numel(), s.batch, s.out.data_ptr(), self.stream.cuda_stream)
+                    s.host_out.copy_(s.out, non_blocking=True)
+                    s.event = torch.cuda.Event()
+                    s.event.record(self.stream)
+                    # stream order makes the memory reusable by later work on this stream
+                    with self._cv:
+                        self._used -= s.bytes
+                        self._completing.append(s)
+                active = still
+
+    def _poll(self):
+        while True:
+            with self._cv:
+                done = self._stop and not self._queue and not self._completing and not self._worker.is_alive()
+            if done:
+                break
+            if not self._completing:
+                time.sleep(20e-6)
+                continue
+            s = self._completing[0]
+            if s.event.query():
+                self._completing.popleft()
+                s.req.completed = time.perf_counter()
+                out = s.host_out[:, s.shift:].clone()
+                s.req.future.set_result(out)
+            else:
+                time.sleep(20e-6)
+
+
+def run_plain(desc: dict, device) -> torch.Tensor:
+    """One request through the plain per-gate form (one launch per gate): the
+    serving baseline without batching."""
+    from . import workloads
+
+    circ = workloads.build_circuit(desc, engine="plain").to(device)
+    kw = workloads.circuit_inputs(desc, device)
+    with torch.no_grad():
+        return circ(**kw)

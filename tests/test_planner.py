@@ -120,3 +120,34 @@ def test_planner_rejects_bad_programs():
     assert rc == 1 and b"out of range" in lib.qg_last_error()
     rc = lib.qg_program_create(g, 1, None, 3, None, ctypes.byref(h))
     assert rc == 1 and b"num_qubits" in lib.qg_last_error()
+
+
+def test_serving_lowering_matches_front_end():
+    from qandle_gb300 import serve
+
+    rng = np.random.default_rng(5)
+    for _ in range(6):
+        d = workloads.random_sel_request(rng, n_range=(5, 12), depth_range=(2, 5), batch_max=8)
+        lo_s, params, named, shift = serve.lower_description(d)
+        lo_f = engine.lower(workloads.build_circuit(d, engine="fused").circuit)
+        assert shift == 0
+        assert lo_s.gates == lo_f.gates and lo_s.qlist == lo_f.qlist
+        assert lo_s.named_cols == lo_f.named_cols
+        p_f = np.array([float(m.remapping(m.theta).reshape(-1)[0].detach()) for m in lo_f.param_mods])
+        assert np.array_equal(params[:len(p_f)], p_f.astype(np.float32))
+    # narrow circuits get an idle qubit 0 and keep their results
+    d = workloads.random_sel_request(rng, n_range=(4, 4), depth_range=(2, 3), batch_max=4)
+    lo_s, params, named, shift = serve.lower_description(d)
+    assert shift == 1 and lo_s.n == 5
+    prog = engine.Program(lo_s, "state", keep_state=True)
+    B = d["batch"]
+    embed = np.zeros((B, 5, 2), complex)
+    embed[:, :, 0] = 1.0
+    for j in range(4):
+        m = np.stack([emu.row_matrix(0, x) for x in named[:, j]])
+        embed[:, j + 1, 0], embed[:, j + 1, 1] = m[:, 0, 0], m[:, 0, 1]
+    st, _ = emu.run_forward(prog, 5, B, params.astype(np.float64), named.astype(np.float64), [], embed=embed)
+    z = 2 * oracle.measure_p0(st) - (np.abs(st) ** 2).sum(-1, keepdims=True)
+    d2 = dict(d)
+    d2["measure"] = "z"
+    assert np.abs(z[:, 1:] - oracle.forward(d2)).max() < 1e-9

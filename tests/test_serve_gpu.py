@@ -1,0 +1,60 @@
+"""Continuous-batching serving loop: every request's result equals the oracle,
+and is bit-identical whether it ran alone or mixed with other requests of
+other widths; oversize requests are refused; a tight budget queues work
+instead of failing."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle
+from qandle_gb300 import serve, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests(count=12, seed=11, n_range=(4, 14), depth_range=(2, 6), batch_max=64):
+    rng = np.random.default_rng(seed)
+    return [workloads.random_sel_request(rng, n_range=n_range, depth_range=depth_range, batch_max=batch_max)
+            for _ in range(count)]
+
+
+def test_mix_equals_alone_and_oracle(cuda_device):
+    reqs = _requests()
+    srv = serve.Server(cuda_device, hbm_budget=8 << 30)
+    try:
+        mixed = [srv.submit(d) for d in reqs]
+        mixed_out = [r.future.result(timeout=120) for r in mixed]
+        alone_out = []
+        for d in reqs:
+            r = srv.submit(d)
+            alone_out.append(r.future.result(timeout=120))
+    finally:
+        srv.close()
+    assert srv.steps > 0
+    for d, a, b in zip(reqs, mixed_out, alone_out):
+        assert torch.equal(a, b), d["n"]
+        ref = oracle.forward(d)
+        assert np.abs(a.numpy() - ref).max() < 1e-5, (d["n"], d["batch"])
+
+
+def test_budget_refuses_and_queues(cuda_device):
+    rng = np.random.default_rng(3)
+    big = workloads.random_sel_request(rng, n_range=(14, 14), depth_range=(2, 2), batch_max=1)
+    big["batch"] = 64
+    big["inputs"]["x"] = np.resize(big["inputs"]["x"], (64, 14)).astype(np.float32)
+    need = (1 << 14) * 8 * 64
+    srv = serve.Server(cuda_device, hbm_budget=need)  # room for one such request at a time
+    try:
+        too_big = dict(big)
+        too_big["batch"] = 65
+        too_big["inputs"] = {"x": np.resize(big["inputs"]["x"], (65, 14)).astype(np.float32)}
+        r = srv.submit(too_big)
+        with pytest.raises(MemoryError):
+            r.future.result(timeout=10)
+        rs = [srv.submit(big) for _ in range(4)]  # queued one after another
+        outs = [x.future.result(timeout=120) for x in rs]
+    finally:
+        srv.close()
+    ref = oracle.forward(big)
+    for o in outs:
+        assert np.abs(o.numpy() - ref).max() < 1e-5
