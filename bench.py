@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--tile-bits", type=int, default=13)
     ap.add_argument("--low-bits", type=int, default=6)
     ap.add_argument("--k", type=int, default=0, help="max strided qubits per pass (0 = tile limit)")
+    ap.add_argument("--reg-bits", type=int, default=5, help="amplitudes per thread = 2^reg_bits")
     ap.add_argument("--n", type=int, default=20)
     ap.add_argument("--batch", type=int, default=256)
     return ap.parse_args()
@@ -204,7 +205,7 @@ def main():
     amp_step = workloads.gate_count(desc) * B * (1 << n)
 
     # ---------------- fused forward, inputs resident in HBM ----------------
-    opts = dict(tile_bits=args.tile_bits, low_bits=args.low_bits, max_high=args.k)
+    opts = dict(tile_bits=args.tile_bits, low_bits=args.low_bits, max_high=args.k, reg_bits=args.reg_bits)
     circ = workloads.build_circuit(desc, engine="fused", **opts).to(dev)
     kw = workloads.circuit_inputs(desc, dev)
     with torch.no_grad():

@@ -157,6 +157,8 @@ typedef struct qg_plan_options {
     int32_t segments;   /* checkpoint segments: the forward stores the state at the
                            end of each segment but the last; the backward restarts
                            each segment from it */
+    int32_t reg_bits;   /* amplitudes per thread = 2^reg_bits (4 or 5): 4 halves the
+                           registers per thread and doubles the warps per tile */
 } qg_plan_options;
 
 typedef struct qg_program qg_program;

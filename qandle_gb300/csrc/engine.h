@@ -9,7 +9,9 @@ namespace qg {
 constexpr int kRegBits = 5;         // amplitudes per thread = 2^5, held in registers
 constexpr int kMaxTileBits = 13;    // forward tile: 2^13 amplitudes, 256 threads, 64 KiB
 constexpr int kMaxQubits = 30;      // fused engine limit (global bit masks are 32-bit)
-constexpr int kMaxGradPerPass = 96; // backward: gradient slots per pass (shared-memory partials)
+// backward: gradient slots per pass (their partials live in shared memory
+// beside the psi/lambda double buffer, 5 B per slot and thread)
+__host__ __device__ constexpr int max_grad_per_pass(int reg_bits) { return reg_bits == 4 ? 64 : 96; }
 
 // Device op codes (int4 per op: x = opcode, y/z/w operands).
 enum Opcode : int32_t {
@@ -94,7 +96,7 @@ struct RunArgs {
 
 // Host view of a planned program, for the launch code in fused.cu.
 struct ProgramRun {
-    int n, tile_bits, measure, keep_state, segments;
+    int n, tile_bits, reg_bits, measure, keep_state, segments;
     int nparams, ncols, numats, ngrads, has_embed;
     int nfslots, f_shared, f_ps, nbslots, b_shared, b_ps;
     int nfpass, nbpass;

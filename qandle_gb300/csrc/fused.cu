@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <type_traits>
 
 #include "common.cuh"
 #include "engine.h"
@@ -179,7 +180,7 @@ __device__ void issue_tile_store_f32(const PassDesc& d, const TileGeo& g, float*
 // ----------------------------------------------------- thread mapping --
 
 struct ThreadMap {
-    int regl[5];     // register bit k -> local bit
+    int regl[5];     // register bit k -> local bit (k < RB)
     int thr_off;     // local-index contribution of this thread's lane/warp bits
     uint32_t tglob;  // global-bit values of this thread's qubit thread bits | tile fixed bits
     int sample_off;  // sample offset within the tile (n < TB)
@@ -189,9 +190,13 @@ struct ThreadMap {
     int sw_base;
 };
 
+// Mapping encoding (OP_MAP y/z/w): y = RB register local bits (4 bits each),
+// z = 5 lane local bits, w = warp local bits | (warp-bit count << 16).
+template <int RB>
 __device__ __forceinline__ void decode_map(const PassDesc& d, int32_t y, int32_t z, int32_t w, int tid,
                                            uint32_t fixed_val, ThreadMap& m) {
-    for (int k = 0; k < 5; ++k) m.regl[k] = (y >> (4 * k)) & 15;
+#pragma unroll
+    for (int k = 0; k < RB; ++k) m.regl[k] = (y >> (4 * k)) & 15;
     int nw = (w >> 16) & 7;
     int off = 0, soff = 0;
     uint32_t tg = fixed_val;
@@ -207,21 +212,16 @@ __device__ __forceinline__ void decode_map(const PassDesc& d, int32_t y, int32_t
     m.thr_off = off;
     m.tglob = tg;
     m.sample_off = soff;
-    for (int k = 0; k < 5; ++k) m.sw[k] = swz(1 << m.regl[k]);
+#pragma unroll
+    for (int k = 0; k < RB; ++k) m.sw[k] = swz(1 << m.regl[k]);
     m.sw_base = swz(off);
 }
 
-template <int K>
-__device__ __forceinline__ int roff(const ThreadMap& m) {
-    return ((K & 1) ? (1 << m.regl[0]) : 0) + ((K & 2) ? (1 << m.regl[1]) : 0) +
-           ((K & 4) ? (1 << m.regl[2]) : 0) + ((K & 8) ? (1 << m.regl[3]) : 0) +
-           ((K & 16) ? (1 << m.regl[4]) : 0);
-}
-
+template <int RB>
 __device__ __forceinline__ int roff_rt(const ThreadMap& m, int r) {
     int o = 0;
 #pragma unroll
-    for (int k = 0; k < 5; ++k)
+    for (int k = 0; k < RB; ++k)
         if ((r >> k) & 1) o += 1 << m.regl[k];
     return o;
 }
@@ -232,58 +232,75 @@ __device__ __forceinline__ int xslot(const ThreadMap& m) {
            ((K & 8) ? m.sw[3] : 0) ^ ((K & 16) ? m.sw[4] : 0);
 }
 
-template <int K = 0>
-__device__ __forceinline__ void xwrite(float2* buf, const float2 (&a)[32], const ThreadMap& m) {
+template <int RB, int K = 0>
+__device__ __forceinline__ void xwrite(float2* buf, const float2 (&a)[1 << RB], const ThreadMap& m) {
     buf[xslot<K>(m)] = a[K];
-    if constexpr (K + 1 < 32) xwrite<K + 1>(buf, a, m);
+    if constexpr (K + 1 < (1 << RB)) xwrite<RB, K + 1>(buf, a, m);
 }
-template <int K = 0>
-__device__ __forceinline__ void xread(const float2* buf, float2 (&a)[32], const ThreadMap& m) {
+template <int RB, int K = 0>
+__device__ __forceinline__ void xread(const float2* buf, float2 (&a)[1 << RB], const ThreadMap& m) {
     a[K] = buf[xslot<K>(m)];
-    if constexpr (K + 1 < 32) xread<K + 1>(buf, a, m);
+    if constexpr (K + 1 < (1 << RB)) xread<RB, K + 1>(buf, a, m);
 }
 
-// natural mapping: lanes = local bits 0..4, registers 5..9, warps 10..
-__device__ __forceinline__ int nat_index(int r, int tid) { return (tid & 31) | (r << 5) | ((tid >> 5) << 10); }
+// Natural mapping: lanes = local bits 0..4 (32 consecutive amplitudes per
+// warp access), registers = local bits 5..5+RB-1, warps = the bits above.
+template <int RB>
+__device__ __forceinline__ int nat_index(int r, int tid) {
+    return (tid & 31) | (r << 5) | ((tid >> 5) << (5 + RB));
+}
 
-template <int TB>
+template <int TB, int RB>
 struct NatMap {
-    static constexpr int32_t y = 0x98765;
+    static constexpr int32_t regs() {
+        int32_t v = 0;
+        for (int k = 0; k < RB; ++k) v |= (5 + k) << (4 * k);
+        return v;
+    }
+    static constexpr int32_t warps() {
+        int32_t v = 0;
+        for (int k = 0; k < TB - 5 - RB; ++k) v |= (5 + RB + k) << (4 * k);
+        return v | ((TB - 5 - RB) << 16);
+    }
+    static constexpr int32_t y = regs();
     static constexpr int32_t z = 0x43210;
-    static constexpr int32_t w = (TB >= 11 ? 0xA : 0) | (TB >= 12 ? 0xB0 : 0) | (TB >= 13 ? 0xC00 : 0) |
-                                 ((TB - 10) << 16);
+    static constexpr int32_t w = warps();
 };
 
-// ---------------------------------------------------------- gate ops --
-
-template <int P>
-__device__ __forceinline__ void mat_reg(float2 (&a)[32], const float2 m[4]) {
-#pragma unroll
-    for (int r = 0; r < 32; ++r)
-        if (!(r & (1 << P))) apply_row2(a[r], a[r | (1 << P)], m);
-}
-
-__device__ __forceinline__ void mat_dispatch(int p, float2 (&a)[32], const float2 m[4]) {
+// Run f(integral_constant<P>) for the runtime register position p < RB.
+template <int RB, typename F>
+__device__ __forceinline__ void for_pos(int p, F&& f) {
     switch (p) {
-        case 0: mat_reg<0>(a, m); break;
-        case 1: mat_reg<1>(a, m); break;
-        case 2: mat_reg<2>(a, m); break;
-        case 3: mat_reg<3>(a, m); break;
-        default: mat_reg<4>(a, m); break;
+        case 0: f(std::integral_constant<int, 0>{}); break;
+        case 1: f(std::integral_constant<int, 1>{}); break;
+        case 2: f(std::integral_constant<int, 2>{}); break;
+        case 3: f(std::integral_constant<int, 3>{}); break;
+        default:
+            if constexpr (RB > 4) f(std::integral_constant<int, 4>{});
+            break;
     }
 }
 
-template <int P>
-__device__ __forceinline__ void diag_reg(float2 (&a)[32], float2 d0, float2 d1) {
+// ---------------------------------------------------------- gate ops --
+
+template <int P, int RB>
+__device__ __forceinline__ void mat_reg(float2 (&a)[1 << RB], const float2 m[4]) {
 #pragma unroll
-    for (int r = 0; r < 32; ++r) a[r] = cmul(a[r], (r & (1 << P)) ? d1 : d0);
+    for (int r = 0; r < (1 << RB); ++r)
+        if (!(r & (1 << P))) apply_row2(a[r], a[r | (1 << P)], m);
+}
+
+template <int P, int RB>
+__device__ __forceinline__ void diag_reg(float2 (&a)[1 << RB], float2 d0, float2 d1) {
+#pragma unroll
+    for (int r = 0; r < (1 << RB); ++r) a[r] = cmul(a[r], (r & (1 << P)) ? d1 : d0);
 }
 
 // X on register position P when the thread-uniform control `tcond` holds
-template <int P>
-__device__ __forceinline__ void cx_reg(float2 (&a)[32], int /*ctrl_reg*/, bool tcond) {
+template <int P, int RB>
+__device__ __forceinline__ void cx_reg(float2 (&a)[1 << RB], bool tcond) {
 #pragma unroll
-    for (int r = 0; r < 32; ++r) {
+    for (int r = 0; r < (1 << RB); ++r) {
         if (r & (1 << P)) continue;
         float2 x = a[r], y = a[r | (1 << P)];
         a[r] = tcond ? y : x;
@@ -292,10 +309,10 @@ __device__ __forceinline__ void cx_reg(float2 (&a)[32], int /*ctrl_reg*/, bool t
 }
 
 // X on register position P where register bit C of r is 1: a fixed permutation
-template <int P, int C>
-__device__ __forceinline__ void cx_rr(float2 (&a)[32]) {
+template <int P, int C, int RB>
+__device__ __forceinline__ void cx_rr(float2 (&a)[1 << RB]) {
 #pragma unroll
-    for (int r = 0; r < 32; ++r) {
+    for (int r = 0; r < (1 << RB); ++r) {
         if ((r & (1 << P)) || !(r & (1 << C))) continue;
         float2 t = a[r];
         a[r] = a[r | (1 << P)];
@@ -303,21 +320,10 @@ __device__ __forceinline__ void cx_rr(float2 (&a)[32]) {
     }
 }
 
-template <int P>
-__device__ __forceinline__ void cx_rr_dispatch(int c, float2 (&a)[32]) {
-    switch (c) {
-        case 0: if (P != 0) cx_rr<P, 0>(a); break;
-        case 1: if (P != 1) cx_rr<P, 1>(a); break;
-        case 2: if (P != 2) cx_rr<P, 2>(a); break;
-        case 3: if (P != 3) cx_rr<P, 3>(a); break;
-        default: if (P != 4) cx_rr<P, 4>(a); break;
-    }
-}
-
-template <int P0, int P1>
-__device__ __forceinline__ void swap_reg(float2 (&a)[32]) {
+template <int P0, int P1, int RB>
+__device__ __forceinline__ void swap_reg(float2 (&a)[1 << RB]) {
 #pragma unroll
-    for (int r = 0; r < 32; ++r) {
+    for (int r = 0; r < (1 << RB); ++r) {
         if ((r & (1 << P0)) && !(r & (1 << P1))) {
             int s = r ^ (1 << P0) ^ (1 << P1);
             float2 t = a[r];
@@ -327,38 +333,16 @@ __device__ __forceinline__ void swap_reg(float2 (&a)[32]) {
     }
 }
 
-template <int P0>
-__device__ __forceinline__ void swap_dispatch1(int p1, float2 (&a)[32]) {
-    switch (p1) {
-        case 0: swap_reg<P0, 0>(a); break;
-        case 1: swap_reg<P0, 1>(a); break;
-        case 2: swap_reg<P0, 2>(a); break;
-        case 3: swap_reg<P0, 3>(a); break;
-        default: swap_reg<P0, 4>(a); break;
-    }
-}
-
-__device__ __forceinline__ void swap_dispatch(int p0, int p1, float2 (&a)[32]) {
-    if (p0 == p1) return;
-    switch (p0) {
-        case 0: swap_dispatch1<0>(p1, a); break;
-        case 1: swap_dispatch1<1>(p1, a); break;
-        case 2: swap_dispatch1<2>(p1, a); break;
-        case 3: swap_dispatch1<3>(p1, a); break;
-        default: swap_dispatch1<4>(p1, a); break;
-    }
-}
-
 __device__ __forceinline__ bool loc_bit_thread(int32_t loc, uint32_t tglob) {
     return (tglob >> (loc & 31)) & 1;
 }
 
 // Im( conj(l0) (P p)_0 + conj(l1) (P p)_1 ) summed over the pairs of position P
-template <int P>
-__device__ __forceinline__ float grad_reg(const float2 (&psi)[32], const float2 (&lam)[32], int axis) {
+template <int P, int RB>
+__device__ __forceinline__ float grad_reg(const float2 (&psi)[1 << RB], const float2 (&lam)[1 << RB], int axis) {
     float acc = 0.f;
 #pragma unroll
-    for (int r = 0; r < 32; ++r) {
+    for (int r = 0; r < (1 << RB); ++r) {
         if (r & (1 << P)) continue;
         float2 p0 = psi[r], p1 = psi[r | (1 << P)];
         apply_pauli(axis, p0, p1);
@@ -368,14 +352,17 @@ __device__ __forceinline__ float grad_reg(const float2 (&psi)[32], const float2 
     return acc;
 }
 
-__device__ __forceinline__ float grad_dispatch(int p, const float2 (&psi)[32], const float2 (&lam)[32], int axis) {
-    switch (p) {
-        case 0: return grad_reg<0>(psi, lam, axis);
-        case 1: return grad_reg<1>(psi, lam, axis);
-        case 2: return grad_reg<2>(psi, lam, axis);
-        case 3: return grad_reg<3>(psi, lam, axis);
-        default: return grad_reg<4>(psi, lam, axis);
-    }
+template <int RB>
+__device__ __forceinline__ void mat_dispatch(int p, float2 (&a)[1 << RB], const float2 m[4]) {
+    for_pos<RB>(p, [&](auto P) { mat_reg<decltype(P)::value, RB>(a, m); });
+}
+
+template <int RB>
+__device__ __forceinline__ float grad_dispatch(int p, const float2 (&psi)[1 << RB], const float2 (&lam)[1 << RB],
+                                               int axis) {
+    float g = 0.f;
+    for_pos<RB>(p, [&](auto P) { g = grad_reg<decltype(P)::value, RB>(psi, lam, axis); });
+    return g;
 }
 
 __device__ __forceinline__ void load_slot(const RunArgs& A, int32_t slot, int32_t flags, int64_t sample,
@@ -394,53 +381,41 @@ __device__ __forceinline__ void load_slot(const RunArgs& A, int32_t slot, int32_
 }
 
 // Apply one non-map op to a register set.
-__device__ __forceinline__ void apply_op(const int4 op, float2 (&a)[32], const ThreadMap& tm, const RunArgs& A,
-                                         int64_t sample, bool dagger_slots) {
+template <int RB>
+__device__ __forceinline__ void apply_op(const int4 op, float2 (&a)[1 << RB], const ThreadMap& tm,
+                                         const RunArgs& A, int64_t sample) {
     switch (op.x) {
         case OP_MAT: {
             float2 m[4];
             load_slot(A, op.z, op.w, sample, m);
-            mat_dispatch(op.y, a, m);
+            mat_dispatch<RB>(op.y, a, m);
             break;
         }
         case OP_DIAG: {
             float2 m[4];
             load_slot(A, op.z, op.w, sample, m);
             if (op.y & LOC_REG) {
-                switch (op.y & 7) {
-                    case 0: diag_reg<0>(a, m[0], m[3]); break;
-                    case 1: diag_reg<1>(a, m[0], m[3]); break;
-                    case 2: diag_reg<2>(a, m[0], m[3]); break;
-                    case 3: diag_reg<3>(a, m[0], m[3]); break;
-                    default: diag_reg<4>(a, m[0], m[3]); break;
-                }
+                for_pos<RB>(op.y & 7, [&](auto P) { diag_reg<decltype(P)::value, RB>(a, m[0], m[3]); });
             } else {
                 float2 d = loc_bit_thread(op.y, tm.tglob) ? m[3] : m[0];
 #pragma unroll
-                for (int r = 0; r < 32; ++r) a[r] = cmul(a[r], d);
+                for (int r = 0; r < (1 << RB); ++r) a[r] = cmul(a[r], d);
             }
             break;
         }
         case OP_CX: {
             if (op.z & LOC_REG) {
                 int cr = op.z & 7;
-                switch (op.y) {
-                    case 0: cx_rr_dispatch<0>(cr, a); break;
-                    case 1: cx_rr_dispatch<1>(cr, a); break;
-                    case 2: cx_rr_dispatch<2>(cr, a); break;
-                    case 3: cx_rr_dispatch<3>(cr, a); break;
-                    default: cx_rr_dispatch<4>(cr, a); break;
-                }
+                for_pos<RB>(op.y, [&](auto P) {
+                    for_pos<RB>(cr, [&](auto C) {
+                        if constexpr (decltype(P)::value != decltype(C)::value)
+                            cx_rr<decltype(P)::value, decltype(C)::value, RB>(a);
+                    });
+                });
                 break;
             }
             bool tc = loc_bit_thread(op.z, tm.tglob);
-            switch (op.y) {
-                case 0: cx_reg<0>(a, -1, tc); break;
-                case 1: cx_reg<1>(a, -1, tc); break;
-                case 2: cx_reg<2>(a, -1, tc); break;
-                case 3: cx_reg<3>(a, -1, tc); break;
-                default: cx_reg<4>(a, -1, tc); break;
-            }
+            for_pos<RB>(op.y, [&](auto P) { cx_reg<decltype(P)::value, RB>(a, tc); });
             break;
         }
         case OP_CZ: {
@@ -451,17 +426,22 @@ __device__ __forceinline__ void apply_op(const int4 op, float2 (&a)[32], const T
             if (!(t0 && t1)) break;
             uint32_t need = (r0 >= 0 ? (1u << r0) : 0u) | (r1 >= 0 ? (1u << r1) : 0u);
 #pragma unroll
-            for (int r = 0; r < 32; ++r)
+            for (int r = 0; r < (1 << RB); ++r)
                 if (((uint32_t)r & need) == need) a[r] = make_float2(-a[r].x, -a[r].y);
             break;
         }
         case OP_SWAP:
-            swap_dispatch(op.y, op.z, a);
+            if (op.y != op.z)
+                for_pos<RB>(op.y, [&](auto P0) {
+                    for_pos<RB>(op.z, [&](auto P1) {
+                        if constexpr (decltype(P0)::value != decltype(P1)::value)
+                            swap_reg<decltype(P0)::value, decltype(P1)::value, RB>(a);
+                    });
+                });
             break;
         default:
             break;
     }
-    (void)dagger_slots;
 }
 
 // --------------------------------------------------------- the pass --
@@ -501,9 +481,17 @@ __device__ __forceinline__ int find_job(const JobTable<MAXJ>& jt, int64_t t) {
 // of the launch (the passes of independent programs / states, e.g. several
 // serving requests of different widths); a single-program forward is a
 // one-job launch.
-template <int TB, int MAXJ>
-__global__ void __launch_bounds__(1 << (TB - 5), (TB <= 12 ? 2 : 1)) k_fwd_pass(const __grid_constant__ JobTable<MAXJ> jt) {
-    constexpr int NT = 1 << (TB - 5);
+// Resident CTAs per SM the register budget allows: 32 amplitudes per thread
+// (RB = 5) take up to 255 registers, 16 (RB = 4) up to 128.
+template <int TB, int RB>
+constexpr int min_blocks() {
+    return 65536 / ((1 << (TB - RB)) * (RB == 5 ? 256 : 128));
+}
+
+template <int TB, int RB, int MAXJ>
+__global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
+    k_fwd_pass(const __grid_constant__ JobTable<MAXJ> jt) {
+    constexpr int NT = 1 << (TB - RB);
     constexpr int AMPS = 1 << TB;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* buf0 = reinterpret_cast<float2*>(smem_raw);
@@ -563,7 +551,7 @@ __global__ void __launch_bounds__(1 << (TB - 5), (TB <= 12 ? 2 : 1)) k_fwd_pass(
         const int n = A.n;
         const bool load_in = tile_loads(j);
         TileGeo g = tile_geo(d, t - jt.begin[j], n, A.batch);
-        float2 a[32];
+        float2 a[1 << RB];
         ThreadMap tm;
         if (load_in) {
             bool ok = mbar_wait(&bars[iter & 1], phase[iter & 1] & 1);
@@ -573,27 +561,27 @@ __global__ void __launch_bounds__(1 << (TB - 5), (TB <= 12 ? 2 : 1)) k_fwd_pass(
                 break;
             }
 #pragma unroll
-            for (int r = 0; r < 32; ++r) a[r] = buf[nat_index(r, tid)];
-            decode_map(d, NatMap<TB>::y, NatMap<TB>::z, NatMap<TB>::w, tid, g.fixed_val, tm);
+            for (int r = 0; r < (1 << RB); ++r) a[r] = buf[nat_index<RB>(r, tid)];
+            decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
         } else {
             if (d.init == INIT_EMBED)
-                decode_map(d, d.init_map[0], d.init_map[1], d.init_map[2], tid, g.fixed_val, tm);
+                decode_map<RB>(d, d.init_map[0], d.init_map[1], d.init_map[2], tid, g.fixed_val, tm);
             else
-                decode_map(d, NatMap<TB>::y, NatMap<TB>::z, NatMap<TB>::w, tid, g.fixed_val, tm);
+                decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
             int64_t smp = g.sample + tm.sample_off;
             if (d.init == INIT_EMBED && smp < A.batch) {
                 // amplitude = prod over qubits of the per-sample factor of its bit
                 const float2* fac = A.embfac + smp * n * 2;
                 float2 c = make_float2(1.f, 0.f);
                 uint32_t regmask = 0;
-                for (int k = 0; k < 5; ++k) regmask |= 1u << d.gbit[tm.regl[k]];
+                for (int k = 0; k < RB; ++k) regmask |= 1u << d.gbit[tm.regl[k]];
                 for (int b = 0; b < n; ++b) {
                     if (regmask & (1u << b)) continue;
                     c = cmul(c, fac[2 * (n - 1 - b) + ((tm.tglob >> b) & 1)]);
                 }
                 a[0] = c;
 #pragma unroll
-                for (int k = 0; k < 5; ++k) {
+                for (int k = 0; k < RB; ++k) {
                     int b = d.gbit[tm.regl[k]];
                     float2 f0 = fac[2 * (n - 1 - b)], f1 = fac[2 * (n - 1 - b) + 1];
 #pragma unroll
@@ -604,13 +592,13 @@ __global__ void __launch_bounds__(1 << (TB - 5), (TB <= 12 ? 2 : 1)) k_fwd_pass(
                 }
             } else if (d.init == INIT_EMBED) {
 #pragma unroll
-                for (int r = 0; r < 32; ++r) a[r] = make_float2(0.f, 0.f);
+                for (int r = 0; r < (1 << RB); ++r) a[r] = make_float2(0.f, 0.f);
             } else {
                 // |0..0>: amplitude 1 where every qubit bit (in and outside the tile) is 0
                 const int qmask = (1 << d.nq_tile) - 1;
 #pragma unroll
-                for (int r = 0; r < 32; ++r) {
-                    bool origin = g.fixed_val == 0 && ((tm.thr_off + roff_rt(tm, r)) & qmask) == 0;
+                for (int r = 0; r < (1 << RB); ++r) {
+                    bool origin = g.fixed_val == 0 && ((tm.thr_off + roff_rt<RB>(tm, r)) & qmask) == 0;
                     a[r] = make_float2(origin ? 1.f : 0.f, 0.f);
                 }
             }
@@ -626,12 +614,12 @@ __global__ void __launch_bounds__(1 << (TB - 5), (TB <= 12 ? 2 : 1)) k_fwd_pass(
             int4 op = __ldg(ops + o);
             if (op.x == OP_MAP) {
                 __syncthreads();
-                xwrite(buf, a, tm);
+                xwrite<RB>(buf, a, tm);
                 __syncthreads();
-                decode_map(d, op.y, op.z, op.w, tid, g.fixed_val, tm);
-                xread(buf, a, tm);
+                decode_map<RB>(d, op.y, op.z, op.w, tid, g.fixed_val, tm);
+                xread<RB>(buf, a, tm);
             } else {
-                apply_op(op, a, tm, A, g.sample + tm.sample_off, false);
+                apply_op<RB>(op, a, tm, A, g.sample + tm.sample_off);
             }
         }
         // ---- epilogue (the planner left the natural mapping) ----
@@ -639,7 +627,7 @@ __global__ void __launch_bounds__(1 << (TB - 5), (TB <= 12 ? 2 : 1)) k_fwd_pass(
         const int64_t smp0 = g.sample;
         if (d.epi & EPI_STORE) {
 #pragma unroll
-            for (int r = 0; r < 32; ++r) buf[nat_index(r, tid)] = a[r];
+            for (int r = 0; r < (1 << RB); ++r) buf[nat_index<RB>(r, tid)] = a[r];
             fence_proxy_async();
             __syncthreads();
             if (tid < 32) {
@@ -655,7 +643,7 @@ __global__ void __launch_bounds__(1 << (TB - 5), (TB <= 12 ? 2 : 1)) k_fwd_pass(
             }
             float* pb = reinterpret_cast<float*>(buf);
 #pragma unroll
-            for (int r = 0; r < 32; ++r) pb[nat_index(r, tid)] = a[r].x * a[r].x + a[r].y * a[r].y;
+            for (int r = 0; r < (1 << RB); ++r) pb[nat_index<RB>(r, tid)] = a[r].x * a[r].x + a[r].y * a[r].y;
             if (d.epi & EPI_PROBS) {
                 fence_proxy_async();
                 __syncthreads();
@@ -667,26 +655,29 @@ __global__ void __launch_bounds__(1 << (TB - 5), (TB <= 12 ? 2 : 1)) k_fwd_pass(
             }
             __syncthreads();
             if (d.epi & EPI_P0) {
-                // phase A: thread t owns the 32 consecutive probabilities of chunk t
+                // phase A: thread t owns the 2^RB consecutive probabilities of chunk t
+                constexpr int CH = 1 << RB;
                 float* ptot = pb + AMPS;          // [NT]
-                float* psub = ptot + NT;          // [5][NT]
-                const float* chunk = pb + tid * 32;
-                float tot = 0.f, sj[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+                float* psub = ptot + NT;          // [RB][NT]
+                const float* chunk = pb + tid * CH;
+                float tot = 0.f, sj[RB];
 #pragma unroll
-                for (int k = 0; k < 32; ++k) {
-                    int idx = (k + tid) & 31;  // rotated start: conflict-free across lanes
+                for (int jj = 0; jj < RB; ++jj) sj[jj] = 0.f;
+#pragma unroll
+                for (int k = 0; k < CH; ++k) {
+                    int idx = (k + tid) & (CH - 1);  // rotated start spreads the banks
                     float v = chunk[idx];
                     tot += v;
 #pragma unroll
-                    for (int jj = 0; jj < 5; ++jj) sj[jj] += ((idx >> jj) & 1) ? 0.f : v;
+                    for (int jj = 0; jj < RB; ++jj) sj[jj] += ((idx >> jj) & 1) ? 0.f : v;
                 }
                 ptot[tid] = tot;
 #pragma unroll
-                for (int jj = 0; jj < 5; ++jj) psub[jj * NT + tid] = sj[jj];
+                for (int jj = 0; jj < RB; ++jj) psub[jj * NT + tid] = sj[jj];
                 __syncthreads();
                 // phase B: (sample, local bit) items
                 const int nq = d.nq_tile;
-                const int cps = 1 << (nq - 5);            // chunks (threads) per sample
+                const int cps = 1 << (nq - RB);           // chunks (threads) per sample
                 const int spt = NT / cps;                 // samples per tile
                 const int items = spt * (nq + 1);
                 const int64_t tps = (n >= TB) ? (int64_t(1) << (n - TB)) : 1;
@@ -697,8 +688,8 @@ __global__ void __launch_bounds__(1 << (TB - 5), (TB <= 12 ? 2 : 1)) k_fwd_pass(
                         float acc = 0.f;
                         for (int c = lane; c < cps; c += 32) {
                             int t2 = s * cps + c;
-                            if (jj < 5) acc += psub[jj * NT + t2];
-                            else if (jj < nq) acc += ((t2 >> (jj - 5)) & 1) ? 0.f : ptot[t2];
+                            if (jj < RB) acc += psub[jj * NT + t2];
+                            else if (jj < nq) acc += ((t2 >> (jj - RB)) & 1) ? 0.f : ptot[t2];
                             else acc += ptot[t2];
                         }
                         for (int o2 = 16; o2 > 0; o2 >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o2);
@@ -714,8 +705,8 @@ __global__ void __launch_bounds__(1 << (TB - 5), (TB <= 12 ? 2 : 1)) k_fwd_pass(
                         float acc = 0.f;
                         for (int c = 0; c < cps; ++c) {
                             int t2 = s * cps + c;
-                            if (jj < 5) acc += psub[jj * NT + t2];
-                            else if (jj < nq) acc += ((t2 >> (jj - 5)) & 1) ? 0.f : ptot[t2];
+                            if (jj < RB) acc += psub[jj * NT + t2];
+                            else if (jj < nq) acc += ((t2 >> (jj - RB)) & 1) ? 0.f : ptot[t2];
                             else acc += ptot[t2];
                         }
                         if (s < g.nsamples) {
@@ -735,18 +726,18 @@ __global__ void __launch_bounds__(1 << (TB - 5), (TB <= 12 ? 2 : 1)) k_fwd_pass(
 }
 
 // Backward pass kernel: psi and lambda tiles (TB = 12), gradient partials.
-template <int TB>
-__global__ void __launch_bounds__(1 << (TB - 5), 1)
+template <int TB, int RB>
+__global__ void __launch_bounds__(1 << (TB - RB), 1)
     k_bwd_pass(const PassDesc* __restrict__ passes, const int4* __restrict__ ops_all, int pass_index, RunArgs A,
                int store_lam_last, int64_t num_tiles) {
-    constexpr int NT = 1 << (TB - 5);
+    constexpr int NT = 1 << (TB - RB);
     constexpr int AMPS = 1 << TB;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* pbuf0 = reinterpret_cast<float2*>(smem_raw);  // psi, lambda, psi, lambda
     float* gacc = reinterpret_cast<float*>(pbuf0 + 4 * AMPS);  // [ngrad][NT]
     // sample (within the tile) each partial belongs to: the thread's sample
     // bits depend on the mapping in force when the gradient op ran
-    uint8_t* gsmp = reinterpret_cast<uint8_t*>(gacc + kMaxGradPerPass * NT);  // [ngrad][NT]
+    uint8_t* gsmp = reinterpret_cast<uint8_t*>(gacc + max_grad_per_pass(RB) * NT);  // [ngrad][NT]
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ PassDesc sd;
 
@@ -781,7 +772,7 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
         float2* ls = ps + AMPS;
         float2* nps = pbuf0 + ((iter + 1) & 1) * 2 * AMPS;
         TileGeo g = tile_geo(d, t, n, A.batch);
-        float2 psi[32], lam[32];
+        float2 psi[1 << RB], lam[1 << RB];
         ThreadMap tm;
         bool ok = mbar_wait(&bars[iter & 1], (iter >> 1) & 1);
         if (__syncthreads_or(!ok)) {
@@ -789,11 +780,11 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
             break;
         }
 #pragma unroll
-        for (int r = 0; r < 32; ++r) {
-            psi[r] = ps[nat_index(r, tid)];
-            lam[r] = ls[nat_index(r, tid)];
+        for (int r = 0; r < (1 << RB); ++r) {
+            psi[r] = ps[nat_index<RB>(r, tid)];
+            lam[r] = ls[nat_index<RB>(r, tid)];
         }
-        decode_map(d, NatMap<TB>::y, NatMap<TB>::z, NatMap<TB>::w, tid, g.fixed_val, tm);
+        decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
         __syncthreads();
         if (tid < 32 && t + gridDim.x < num_tiles) {
             bulk_wait_read0();
@@ -807,29 +798,29 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
             int4 op = __ldg(ops + o);
             if (op.x == OP_MAP) {
                 __syncthreads();
-                xwrite(ps, psi, tm);
-                xwrite(ls, lam, tm);
+                xwrite<RB>(ps, psi, tm);
+                xwrite<RB>(ls, lam, tm);
                 __syncthreads();
-                decode_map(d, op.y, op.z, op.w, tid, g.fixed_val, tm);
-                xread(ps, psi, tm);
-                xread(ls, lam, tm);
+                decode_map<RB>(d, op.y, op.z, op.w, tid, g.fixed_val, tm);
+                xread<RB>(ps, psi, tm);
+                xread<RB>(ls, lam, tm);
             } else if (op.x == OP_GRAD) {
-                float gsum = grad_dispatch(op.y, psi, lam, op.z);
+                float gsum = grad_dispatch<RB>(op.y, psi, lam, op.z);
                 gacc[(op.w - d.grad_base) * NT + tid] = gsum;
                 gsmp[(op.w - d.grad_base) * NT + tid] = (uint8_t)tm.sample_off;
             } else if (op.x == OP_MAT && (op.w & OPF_GRAD)) {
                 int axis = (op.w >> 8) & 3;
                 int gslot = op.w >> 12;
-                float gsum = grad_dispatch(op.y, psi, lam, axis);
+                float gsum = grad_dispatch<RB>(op.y, psi, lam, axis);
                 gacc[(gslot - d.grad_base) * NT + tid] = gsum;
                 gsmp[(gslot - d.grad_base) * NT + tid] = (uint8_t)tm.sample_off;
                 float2 m[4];
                 load_slot(A, op.z, op.w, g.sample + tm.sample_off, m);
-                mat_dispatch(op.y, psi, m);
-                mat_dispatch(op.y, lam, m);
+                mat_dispatch<RB>(op.y, psi, m);
+                mat_dispatch<RB>(op.y, lam, m);
             } else {
-                apply_op(op, psi, tm, A, g.sample + tm.sample_off, true);
-                apply_op(op, lam, tm, A, g.sample + tm.sample_off, true);
+                apply_op<RB>(op, psi, tm, A, g.sample + tm.sample_off);
+                apply_op<RB>(op, lam, tm, A, g.sample + tm.sample_off);
             }
         }
         __syncthreads();
@@ -856,9 +847,9 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
         // store psi and lambda (natural mapping)
         if (d.epi & EPI_STORE) {
 #pragma unroll
-            for (int r = 0; r < 32; ++r) {
-                ps[nat_index(r, tid)] = psi[r];
-                ls[nat_index(r, tid)] = lam[r];
+            for (int r = 0; r < (1 << RB); ++r) {
+                ps[nat_index<RB>(r, tid)] = psi[r];
+                ls[nat_index<RB>(r, tid)] = lam[r];
             }
             fence_proxy_async();
             __syncthreads();
@@ -869,7 +860,7 @@ __global__ void __launch_bounds__(1 << (TB - 5), 1)
             }
         } else if (store_lam_last) {
 #pragma unroll
-            for (int r = 0; r < 32; ++r) ls[nat_index(r, tid)] = lam[r];
+            for (int r = 0; r < (1 << RB); ++r) ls[nat_index<RB>(r, tid)] = lam[r];
             fence_proxy_async();
             __syncthreads();
             if (tid < 32) {
@@ -1120,34 +1111,49 @@ static BwdLayout bwd_layout(const ProgramRun& R, int64_t B) {
     return L;
 }
 
-template <int TB, int MAXJ>
+template <int TB, int RB, int MAXJ>
 static int launch_fwd_jobs(const JobTable<MAXJ>& jt, cudaStream_t st) {
-    constexpr int NT = 1 << (TB - 5);
+    constexpr int NT = 1 << (TB - RB);
     size_t smem = 2 * (size_t(1) << TB) * sizeof(float2);
     static bool attr_set = false;
     if (!attr_set) {
         QG_CUDA_TRY(
-            cudaFuncSetAttribute(k_fwd_pass<TB, MAXJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            cudaFuncSetAttribute(k_fwd_pass<TB, RB, MAXJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = true;
     }
     int64_t tiles = jt.begin[jt.njobs];
     if (tiles <= 0) return QG_OK;
     static int per_sm = 0;
     if (!per_sm) {
-        QG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fwd_pass<TB, MAXJ>, NT, smem));
+        QG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fwd_pass<TB, RB, MAXJ>, NT, smem));
         if (per_sm < 1) per_sm = 1;
     }
     int64_t slots = (int64_t)sm_count() * per_sm;  // persistent: every resident CTA walks tiles
     int64_t grid = tiles < slots ? tiles : slots;
-    k_fwd_pass<TB, MAXJ><<<(unsigned)grid, NT, smem, st>>>(jt);
+    k_fwd_pass<TB, RB, MAXJ><<<(unsigned)grid, NT, smem, st>>>(jt);
     QG_LAUNCH_CHECK();
     return QG_OK;
 }
 
-template <int TB>
+// Launch a job table on the kernel instantiated for (tile_bits, reg_bits).
+static int launch_fwd_table(const JobTable<QG_MAX_JOBS>& jt, int tb, int rb, cudaStream_t st) {
+    if (rb == 4) {
+        switch (tb) {
+            case 13: return launch_fwd_jobs<13, 4, QG_MAX_JOBS>(jt, st);
+            case 12: return launch_fwd_jobs<12, 4, QG_MAX_JOBS>(jt, st);
+            default: return launch_fwd_jobs<11, 4, QG_MAX_JOBS>(jt, st);
+        }
+    }
+    switch (tb) {
+        case 13: return launch_fwd_jobs<13, 5, QG_MAX_JOBS>(jt, st);
+        case 12: return launch_fwd_jobs<12, 5, QG_MAX_JOBS>(jt, st);
+        default: return launch_fwd_jobs<11, 5, QG_MAX_JOBS>(jt, st);
+    }
+}
+
 static int launch_fwd_pass(const PassDesc* dpass, const int4* dops, const PassDesc& hpass, int p, const RunArgs& A,
-                           int zero_init, int64_t tiles, cudaStream_t st) {
-    JobTable<1> jt;
+                           int zero_init, int64_t tiles, int tb, int rb, cudaStream_t st) {
+    static thread_local JobTable<QG_MAX_JOBS> jt;  // host staging; copied into the launch parameters
     memset(&jt, 0, sizeof(jt));
     jt.njobs = 1;
     jt.begin[0] = 0;
@@ -1157,29 +1163,45 @@ static int launch_fwd_pass(const PassDesc* dpass, const int4* dops, const PassDe
     jt.job[0].A = A;
     jt.job[0].zero_init = zero_init;
     jt.job[0].tiles = tiles;
-    return launch_fwd_jobs<TB, 1>(jt, st);
+    return launch_fwd_table(jt, tb, rb, st);
 }
 
-template <int TB>
+template <int TB, int RB>
 static int launch_bwd_pass(const PassDesc* dpass, const int4* dops, int p, const RunArgs& A, int store_lam,
                            int64_t tiles, cudaStream_t st) {
-    constexpr int NT = 1 << (TB - 5);
-    size_t smem = 4 * (size_t(1) << TB) * sizeof(float2) + (size_t)kMaxGradPerPass * NT * (sizeof(float) + 1);
+    constexpr int NT = 1 << (TB - RB);
+    size_t smem = 4 * (size_t(1) << TB) * sizeof(float2) + (size_t)max_grad_per_pass(RB) * NT * (sizeof(float) + 1);
     static bool attr_set = false;
     if (!attr_set) {
-        QG_CUDA_TRY(cudaFuncSetAttribute(k_bwd_pass<TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        QG_CUDA_TRY(cudaFuncSetAttribute(k_bwd_pass<TB, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = true;
     }
     static int per_sm = 0;
     if (!per_sm) {
-        QG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bwd_pass<TB>, NT, smem));
+        QG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bwd_pass<TB, RB>, NT, smem));
         if (per_sm < 1) per_sm = 1;
     }
     int64_t slots = (int64_t)sm_count() * per_sm;
     int64_t grid = tiles < slots ? tiles : slots;
-    k_bwd_pass<TB><<<(unsigned)grid, NT, smem, st>>>(dpass, dops, p, A, store_lam, tiles);
+    k_bwd_pass<TB, RB><<<(unsigned)grid, NT, smem, st>>>(dpass, dops, p, A, store_lam, tiles);
     QG_LAUNCH_CHECK();
     return QG_OK;
+}
+
+static int launch_bwd(const PassDesc* dpass, const int4* dops, int p, const RunArgs& A, int store_lam,
+                      int64_t tiles, int tb, int rb, cudaStream_t st) {
+    if (rb == 4) {
+        switch (tb) {
+            case 12: return launch_bwd_pass<12, 4>(dpass, dops, p, A, store_lam, tiles, st);
+            case 11: return launch_bwd_pass<11, 4>(dpass, dops, p, A, store_lam, tiles, st);
+            default: return launch_bwd_pass<10, 4>(dpass, dops, p, A, store_lam, tiles, st);
+        }
+    }
+    switch (tb) {
+        case 12: return launch_bwd_pass<12, 5>(dpass, dops, p, A, store_lam, tiles, st);
+        case 11: return launch_bwd_pass<11, 5>(dpass, dops, p, A, store_lam, tiles, st);
+        default: return launch_bwd_pass<10, 5>(dpass, dops, p, A, store_lam, tiles, st);
+    }
 }
 
 static int64_t num_tiles(int n, int tb, int64_t B) {
@@ -1291,9 +1313,9 @@ int qg_jobs_run_pass(const qg_job* jobs, int njobs, void* stream) {
     QG_CHECK_ARG(njobs >= 0 && njobs <= QG_MAX_JOBS, "njobs must be in [0, 32]");
     QG_CHECK_ARG(njobs == 0 || jobs, "jobs is null");
     if (njobs == 0) return QG_OK;
-    JobTable<QG_MAX_JOBS> jt;
+    static thread_local JobTable<QG_MAX_JOBS> jt;  // host staging of the launch parameters
     memset(&jt, 0, sizeof(jt));
-    int tb = -1;
+    int tb = -1, rb = 5;
     int64_t acc = 0;
     for (int i = 0; i < njobs; ++i) {
         const qg_job& q = jobs[i];
@@ -1304,8 +1326,9 @@ int qg_jobs_run_pass(const qg_job* jobs, int njobs, void* stream) {
         if (rc) return rc;
         QG_CHECK_ARG(q.pass >= 0 && q.pass < R.nfpass, "pass index out of range");
         QG_CHECK_ARG(R.segments <= 1, "checkpointed programs run through qg_program_forward");
-        if (tb < 0) tb = R.tile_bits;
-        QG_CHECK_ARG(tb == R.tile_bits, "all jobs of one launch need the same tile_bits");
+        if (tb < 0) tb = R.tile_bits, rb = R.reg_bits;
+        QG_CHECK_ARG(tb == R.tile_bits && rb == R.reg_bits,
+                     "all jobs of one launch need the same tile_bits and reg_bits");
         const char* tab = (const char*)q.table;
         jt.job[i].pd = (const PassDesc*)(tab + R.off_fpass) + q.pass;
         jt.job[i].ops = (const int4*)(tab + R.off_fops) + R.fpass[q.pass].op_begin;
@@ -1317,12 +1340,7 @@ int qg_jobs_run_pass(const qg_job* jobs, int njobs, void* stream) {
     }
     jt.njobs = njobs;
     jt.begin[njobs] = acc;
-    cudaStream_t st = (cudaStream_t)stream;
-    switch (tb) {
-        case 13: return launch_fwd_jobs<13, QG_MAX_JOBS>(jt, st);
-        case 12: return launch_fwd_jobs<12, QG_MAX_JOBS>(jt, st);
-        default: return launch_fwd_jobs<11, QG_MAX_JOBS>(jt, st);
-    }
+    return launch_fwd_table(jt, tb, rb, (cudaStream_t)stream);
 }
 
 int qg_program_forward_timed(const qg_program* prog, const void* dev_table, void* workspace,
@@ -1346,11 +1364,7 @@ int qg_program_forward_timed(const qg_program* prog, const void* dev_table, void
     for (int p = 0; p < R.nfpass; ++p) {
         int zi = (p == 0) ? zero_init : 0;
         if (pass_events) QG_CUDA_TRY(cudaEventRecord((cudaEvent_t)pass_events[2 * p], st));
-        switch (R.tile_bits) {
-            case 13: rc = launch_fwd_pass<13>(dpass, dops, R.fpass[p], p, A, zi, tiles, st); break;
-            case 12: rc = launch_fwd_pass<12>(dpass, dops, R.fpass[p], p, A, zi, tiles, st); break;
-            default: rc = launch_fwd_pass<11>(dpass, dops, R.fpass[p], p, A, zi, tiles, st); break;
-        }
+        rc = launch_fwd_pass(dpass, dops, R.fpass[p], p, A, zi, tiles, R.tile_bits, R.reg_bits, st);
         if (rc) return rc;
         if (pass_events) QG_CUDA_TRY(cudaEventRecord((cudaEvent_t)pass_events[2 * p + 1], st));
     }
@@ -1404,12 +1418,7 @@ int qg_program_backward(const qg_program* prog, const void* dev_table, void* wor
     int64_t tiles = num_tiles(R.n, tb, batch);
     for (int p = 0; p < R.nbpass; ++p) {
         int store_lam = (p + 1 == R.nbpass) && dstate != nullptr;
-        int rc;
-        switch (tb) {
-            case 12: rc = launch_bwd_pass<12>(dpass, dops, p, A, store_lam, tiles, st); break;
-            case 11: rc = launch_bwd_pass<11>(dpass, dops, p, A, store_lam, tiles, st); break;
-            default: rc = launch_bwd_pass<10>(dpass, dops, p, A, store_lam, tiles, st); break;
-        }
+        int rc = launch_bwd(dpass, dops, p, A, store_lam, tiles, tb, R.reg_bits, st);
         if (rc) return rc;
     }
     int64_t fitems = R.nparams + (int64_t)R.ncols * batch;

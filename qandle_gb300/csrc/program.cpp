@@ -196,14 +196,19 @@ int32_t pack4(const int* v, int count) {
 }
 
 struct Mapping {
-    int reg[5], lane[5], warp[3];
-    int nwarp;
+    int reg[5], lane[5], warp[4];
+    int nreg, nwarp;
+    Mapping() {
+        for (int k = 0; k < 5; ++k) reg[k] = lane[k] = -1;
+        for (int k = 0; k < 4; ++k) warp[k] = 0;
+        nreg = nwarp = 0;
+    }
     bool operator==(const Mapping& o) const {
         return !memcmp(reg, o.reg, sizeof(reg)) && !memcmp(lane, o.lane, sizeof(lane)) &&
-               !memcmp(warp, o.warp, sizeof(warp)) && nwarp == o.nwarp;
+               !memcmp(warp, o.warp, sizeof(warp)) && nwarp == o.nwarp && nreg == o.nreg;
     }
     void encode(int32_t out[3]) const {
-        out[0] = pack4(reg, 5);
+        out[0] = pack4(reg, nreg);
         out[1] = pack4(lane, 5);
         out[2] = pack4(warp, nwarp) | (nwarp << 16);
     }
@@ -211,22 +216,25 @@ struct Mapping {
 
 // The mapping used to move a tile between shared memory (natural order) and
 // registers: lanes = local bits 0..4 (32 consecutive amplitudes per warp
-// access), registers = local bits 5..9, warps = local bits 10.. .
-Mapping natural_mapping(int tb) {
+// access), registers = local bits 5..5+rb-1, warps = the bits above.
+Mapping natural_mapping(int tb, int rb) {
     Mapping m;
-    for (int k = 0; k < 5; ++k) m.lane[k] = k, m.reg[k] = 5 + k;
-    m.nwarp = tb - 10;
-    for (int k = 0; k < 3; ++k) m.warp[k] = k < m.nwarp ? 10 + k : 0;
+    m.nreg = rb;
+    for (int k = 0; k < 5; ++k) m.lane[k] = k;
+    for (int k = 0; k < rb; ++k) m.reg[k] = 5 + k;
+    m.nwarp = tb - 5 - rb;
+    for (int k = 0; k < m.nwarp; ++k) m.warp[k] = 5 + rb + k;
     return m;
 }
 
 // Register set R (local bits) -> full mapping.  Lanes take non-register bits
 // whose shared-memory swizzle images are independent (bank-conflict-free
 // exchanges); warps take the rest.
-Mapping mapping_for(uint32_t R, int tb) {
+Mapping mapping_for(uint32_t R, int tb, int rb) {
     Mapping m;
+    m.nreg = rb;
     int r = 0;
-    for (int b = 0; b < tb && r < 5; ++b)
+    for (int b = 0; b < tb && r < rb; ++b)
         if (R & (1u << b)) m.reg[r++] = b;
     std::vector<int> rest;
     for (int b = 0; b < tb; ++b)
@@ -248,7 +256,6 @@ Mapping mapping_for(uint32_t R, int tb) {
     m.nwarp = 0;
     for (int b : rest)
         if (std::find(lanes.begin(), lanes.end(), b) == lanes.end()) m.warp[m.nwarp++] = b;
-    for (int k = m.nwarp; k < 3; ++k) m.warp[k] = 0;
     return m;
 }
 
@@ -310,9 +317,10 @@ void emit_pass(Program& P, PassPlan& pp, const std::vector<LGate>& G, bool backw
     for (int j = 0; j < d.nq_tile; ++j) g2l[d.gbit[j]] = j;
     uint32_t qubit_local = (d.nq_tile >= 32) ? 0xffffffffu : ((1u << d.nq_tile) - 1);
 
-    Mapping nat = natural_mapping(tb);
+    const int rb = P.opt.reg_bits;
+    Mapping nat = natural_mapping(tb, rb);
     uint32_t natR = 0;
-    for (int k = 0; k < 5; ++k) natR |= 1u << nat.reg[k];
+    for (int k = 0; k < rb; ++k) natR |= 1u << nat.reg[k];
     bool nat_ok = (natR & ~qubit_local) == 0;  // natural registers are all qubit bits
 
     d.op_begin = (int)ops.size() / 4;
@@ -326,13 +334,13 @@ void emit_pass(Program& P, PassPlan& pp, const std::vector<LGate>& G, bool backw
     auto loc_of = [&](int gbit, const Mapping& mp) -> int32_t {
         int l = g2l[gbit];
         if (l >= 0)
-            for (int k = 0; k < 5; ++k)
+            for (int k = 0; k < rb; ++k)
                 if (mp.reg[k] == l) return LOC_REG | k;
         return gbit;
     };
     auto regpos = [&](int gbit, const Mapping& mp) -> int {
         int l = g2l[gbit];
-        for (int k = 0; k < 5; ++k)
+        for (int k = 0; k < rb; ++k)
             if (mp.reg[k] == l) return k;
         return -1;
     };
@@ -359,17 +367,17 @@ void emit_pass(Program& P, PassPlan& pp, const std::vector<LGate>& G, bool backw
             Selector s;
             s.S = 0;
             s.addable = qubit_local;
-            s.max_add = 5;
+            s.max_add = rb;
             s.backward = backward;
             s.remap = local_remap;
             placed = s.run(pending, G);
             uint32_t R = s.S;
             // fill to 5 register bits: prefer the natural registers, then low qubit bits
-            for (int k = 0; k < 5 && popc(R) < 5; ++k)
+            for (int k = 0; k < rb && popc(R) < rb; ++k)
                 if (nat_ok && !(R & (1u << nat.reg[k]))) R |= 1u << nat.reg[k];
-            for (int b = 0; b < tb && popc(R) < 5; ++b)
+            for (int b = 0; b < tb && popc(R) < rb; ++b)
                 if ((qubit_local & (1u << b)) && !(R & (1u << b))) R |= 1u << b;
-            Mapping nm = (R == natR) ? nat : mapping_for(R, tb);
+            Mapping nm = (R == natR) ? nat : mapping_for(R, tb, rb);
             if (!have_map) {
                 // zero / embedding init: produce this mapping directly
                 nm.encode(d.init_map);
@@ -499,7 +507,7 @@ void plan_segment(Program& P, const std::vector<LGate>& G, std::vector<int> pend
     while (!pending.empty()) {
         Selector s;
         s.backward = backward;
-        if (backward) s.max_grad = kMaxGradPerPass;
+        if (backward) s.max_grad = max_grad_per_pass(P.opt.reg_bits);
         if (n <= tb) {
             s.S = (n >= 32) ? 0xffffffffu : ((1u << n) - 1);
             s.addable = 0;
@@ -842,6 +850,7 @@ void program_run_info(const void* prog, ProgramRun* r) {
     const Program& P = *reinterpret_cast<const Program*>(prog);
     r->n = P.n;
     r->tile_bits = P.opt.tile_bits;
+    r->reg_bits = P.opt.reg_bits;
     r->measure = P.opt.measure;
     r->keep_state = P.opt.keep_state;
     r->segments = P.nsegments;
@@ -887,6 +896,7 @@ void qg_plan_options_default(qg_plan_options* o) {
     o->measure = QG_MEASURE_STATE;
     o->keep_state = 0;
     o->segments = 1;
+    o->reg_bits = 5;
 }
 
 int qg_program_create(const qg_gate* gates, int ngates, const int32_t* qlist, int n,
@@ -904,6 +914,9 @@ int qg_program_create(const qg_gate* gates, int ngates, const int32_t* qlist, in
     if (o.low_bits < 4 || o.low_bits > o.tile_bits - 1)
         return qg::set_error("low_bits must be in [4, tile_bits - 1]"), QG_EINVAL;
     if (o.max_high < 0) return qg::set_error("max_high must be >= 0"), QG_EINVAL;
+    if (o.reg_bits != 4 && o.reg_bits != 5) return qg::set_error("reg_bits must be 4 or 5"), QG_EINVAL;
+    if (o.tile_bits - 5 - o.reg_bits < 0 || o.tile_bits - 5 - o.reg_bits > 4)
+        return qg::set_error("tile_bits - reg_bits must leave 0..4 warp bits"), QG_EINVAL;
     if (o.segments < 1) o.segments = 1;
     std::unique_ptr<Program> P(new Program());
     P->n = n;

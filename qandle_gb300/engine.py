@@ -99,11 +99,12 @@ class Program:
     """A planned gate program: host handle plus device copies of its tables."""
 
     def __init__(self, lowered: Lowered, measure: str, keep_state: bool, tile_bits: int = 13,
-                 low_bits: int = 6, max_high: int = 0, segments: int = 1):
+                 low_bits: int = 6, max_high: int = 0, segments: int = 1, reg_bits: int = 5):
         lib = _lib.load()
         self.n = lowered.n
         self.measure = measure
         self.keep_state = keep_state
+        self.reg_bits = reg_bits
         gates = (_lib.Gate * max(1, len(lowered.gates)))()
         for i, g in enumerate(lowered.gates):
             gates[i] = _lib.Gate(*g)
@@ -114,6 +115,7 @@ class Program:
         opt.measure = _lib.MEASURE[measure]
         opt.keep_state = 1 if keep_state else 0
         opt.segments = segments
+        opt.reg_bits = reg_bits
         handle = ctypes.c_void_p()
         _lib.check(lib.qg_program_create(gates, len(lowered.gates), ctypes.cast(ql, ctypes.c_void_p),
                                          self.n, ctypes.byref(opt), ctypes.byref(handle)))
@@ -257,11 +259,11 @@ class FusedExecutor:
     """Runs a built circuit through the fused engine (used by Circuit)."""
 
     def __init__(self, circuit, tile_bits: int = 13, low_bits: int = 6, max_high: int = 0,
-                 checkpoint_segments: int = 1):
+                 checkpoint_segments: int = 1, reg_bits: int = 5):
         self.circuit = circuit
         self.n = circuit.num_qubits
         self.lowered = lower(circuit)
-        self.options = dict(tile_bits=tile_bits, low_bits=low_bits, max_high=max_high)
+        self.options = dict(tile_bits=tile_bits, low_bits=low_bits, max_high=max_high, reg_bits=reg_bits)
         self.checkpoint_segments = checkpoint_segments
         self._programs = {}
 

@@ -15,7 +15,6 @@ LOC_REG = 0x100
 OPF_PER_SAMPLE, OPF_GRAD = 1, 2
 INIT_LOAD, INIT_ZERO, INIT_EMBED = 0, 1, 2
 EPI_STORE, EPI_PROBS, EPI_P0 = 1, 2, 4
-NAT_REGS = [5, 6, 7, 8, 9]
 
 
 def row_matrix(kind, theta):
@@ -179,7 +178,7 @@ def run_forward(prog, n, B, params, named, umats, state=None, embed=None):
             regl = _decode(pd["init_map"][0])
         else:
             T = np.where(valid, st.reshape(-1)[np.maximum(idx, 0)], 0)
-            regl = list(NAT_REGS)
+            regl = list(range(5, 5 + prog.reg_bits))
         for op in pd["ops"]:
             if op[0] == OP_MAP:
                 regl = _decode(op[1])
@@ -207,7 +206,7 @@ def run_backward(prog, n, B, params, named, umats, psi, lam, ckpts, grad_targets
         samples = np.where(valid, idx >> n, -1)
         T = np.where(valid, src.reshape(-1)[np.maximum(idx, 0)], 0)
         L = np.where(valid, lam.reshape(-1)[np.maximum(idx, 0)], 0)
-        regl = list(NAT_REGS)
+        regl = list(range(5, 5 + prog.reg_bits))
         for op in pd["ops"]:
             if op[0] == OP_MAP:
                 regl = _decode(op[1])

@@ -53,7 +53,7 @@ CASES = {
     "plain_n12": lambda: workloads.plain_small(n=12, batch=5, layers=3),
 }
 OPTS = [dict(), dict(tile_bits=12, low_bits=4, max_high=2), dict(tile_bits=11, low_bits=5, max_high=1),
-        dict(tile_bits=13, low_bits=7, max_high=6)]
+        dict(tile_bits=13, low_bits=7, max_high=6), dict(reg_bits=4), dict(tile_bits=12, reg_bits=4)]
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
@@ -116,6 +116,7 @@ def _grad_case(desc, dev, opts, weights_seed=3):
 @pytest.mark.parametrize("case,opts", [
     ("brick_n10", dict()), ("brick_n14", dict()), ("brick_n16", dict(checkpoint_segments=3)),
     ("sel_n9", dict()), ("sel_n14", dict(checkpoint_segments=2)), ("sel_n15", dict(tile_bits=12, low_bits=4)),
+    ("brick_n13", dict(reg_bits=4)), ("sel_n8", dict(reg_bits=4, checkpoint_segments=2)),
 ])
 def test_fused_adjoint_vs_oracle(cuda_device, case, opts):
     kind, nq = case.split("_n")

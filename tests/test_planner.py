@@ -45,7 +45,8 @@ CASES = [
     ("plain_n8", lambda: workloads.plain_small(n=8, batch=5, layers=2)),
 ]
 OPTS = [dict(tile_bits=13, low_bits=6, max_high=0), dict(tile_bits=12, low_bits=4, max_high=2),
-        dict(tile_bits=11, low_bits=5, max_high=1), dict(tile_bits=13, low_bits=8, max_high=3)]
+        dict(tile_bits=11, low_bits=5, max_high=1), dict(tile_bits=13, low_bits=8, max_high=3),
+        dict(tile_bits=13, low_bits=6, reg_bits=4), dict(tile_bits=12, low_bits=5, reg_bits=4)]
 
 
 @pytest.mark.parametrize("case", [c[0] for c in CASES])
@@ -64,14 +65,15 @@ def test_forward_plan_matches_oracle(case, oi):
     assert prog.info.forward_passes >= 1
 
 
+@pytest.mark.parametrize("rb", [5, 4])
 @pytest.mark.parametrize("case", ["sel_n10", "brick_n14", "deep_n14", "sel_n15"])
-def test_backward_plan_matches_oracle(case):
+def test_backward_plan_matches_oracle(case, rb):
     desc = dict(CASES)[case]()
     desc["measure"] = "p0"
     n, B = desc["n"], desc["batch"]
     circ = workloads.build_circuit(desc, engine="fused")
     lo = engine.lower(circ.circuit)
-    prog = engine.Program(lo, "p0", keep_state=True, segments=3, tile_bits=13, low_bits=5)
+    prog = engine.Program(lo, "p0", keep_state=True, segments=3, tile_bits=13, low_bits=5, reg_bits=rb)
     params, named, umats, embed = _runtime(lo, desc, B)
     st, ck = emu.run_forward(prog, n, B, params, named, umats, embed=embed)
     w = np.linspace(-1.0, 1.0, B * n).reshape(B, n)
