@@ -92,7 +92,14 @@ struct RunArgs {
     int64_t batch;
     int32_t n;
     int32_t nslots_ps;        // P
+    int32_t nslots_shared;    // S
+    int32_t pad_;
 };
+
+// Shared-memory copies the pass kernels keep of the current pass's op list
+// and of the shared matrix table (longer lists / tables stay in global memory).
+constexpr int kSmemOps = 512;
+constexpr int kSmemMats = 256;
 
 // Host view of a planned program, for the launch code in fused.cu.
 struct ProgramRun {

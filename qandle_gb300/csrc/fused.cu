@@ -365,15 +365,22 @@ __device__ __forceinline__ float grad_dispatch(int p, const float2 (&psi)[1 << R
     return g;
 }
 
-__device__ __forceinline__ void load_slot(const RunArgs& A, int32_t slot, int32_t flags, int64_t sample,
-                                          float2 m[4]) {
-    // lanes of a partial tile past the last sample compute on garbage that is
-    // never stored; keep their table reads inside the table
-    if (sample >= A.batch) sample = A.batch - 1;
-    const float4* src = (flags & OPF_PER_SAMPLE)
-                            ? reinterpret_cast<const float4*>(A.mats_ps + (sample * A.nslots_ps + slot) * 4)
-                            : reinterpret_cast<const float4*>(A.mats + (int64_t)slot * 4);
-    float4 u = __ldg(src), v = __ldg(src + 1);
+__device__ __forceinline__ void load_slot(const RunArgs& A, const float4* smats, int32_t slot, int32_t flags,
+                                          int64_t sample, float2 m[4]) {
+    float4 u, v;
+    if (!(flags & OPF_PER_SAMPLE) && slot < kSmemMats) {
+        u = smats[2 * slot];
+        v = smats[2 * slot + 1];
+    } else {
+        // lanes of a partial tile past the last sample compute on garbage that
+        // is never stored; keep their table reads inside the table
+        if (sample >= A.batch) sample = A.batch - 1;
+        const float4* src = (flags & OPF_PER_SAMPLE)
+                                ? reinterpret_cast<const float4*>(A.mats_ps + (sample * A.nslots_ps + slot) * 4)
+                                : reinterpret_cast<const float4*>(A.mats + (int64_t)slot * 4);
+        u = __ldg(src);
+        v = __ldg(src + 1);
+    }
     m[0] = make_float2(u.x, u.y);
     m[1] = make_float2(u.z, u.w);
     m[2] = make_float2(v.x, v.y);
@@ -383,17 +390,17 @@ __device__ __forceinline__ void load_slot(const RunArgs& A, int32_t slot, int32_
 // Apply one non-map op to a register set.
 template <int RB>
 __device__ __forceinline__ void apply_op(const int4 op, float2 (&a)[1 << RB], const ThreadMap& tm,
-                                         const RunArgs& A, int64_t sample) {
+                                         const RunArgs& A, const float4* smats, int64_t sample) {
     switch (op.x) {
         case OP_MAT: {
             float2 m[4];
-            load_slot(A, op.z, op.w, sample, m);
+            load_slot(A, smats, op.z, op.w, sample, m);
             mat_dispatch<RB>(op.y, a, m);
             break;
         }
         case OP_DIAG: {
             float2 m[4];
-            load_slot(A, op.z, op.w, sample, m);
+            load_slot(A, smats, op.z, op.w, sample, m);
             if (op.y & LOC_REG) {
                 for_pos<RB>(op.y & 7, [&](auto P) { diag_reg<decltype(P)::value, RB>(a, m[0], m[3]); });
             } else {
@@ -496,6 +503,8 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* buf0 = reinterpret_cast<float2*>(smem_raw);
     float2* buf1 = buf0 + AMPS;
+    int4* s_ops = reinterpret_cast<int4*>(buf1 + AMPS);             // [kSmemOps]
+    float4* s_mats = reinterpret_cast<float4*>(s_ops + kSmemOps);   // [kSmemMats][2]
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ PassDesc sd;
     __shared__ RunArgs sa;
@@ -542,6 +551,13 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
                 sd = *jt.job[j].pd;
                 sa = jt.job[j].A;
             }
+            // the pass's op list and the shared matrix table, staged once per job
+            const int4* gops = jt.job[j].ops;
+            const int nops = jt.job[j].pd->op_count;
+            for (int i = tid; i < nops && i < kSmemOps; i += NT) s_ops[i] = __ldg(gops + i);
+            const int nm = jt.job[j].A.nslots_shared < kSmemMats ? jt.job[j].A.nslots_shared : kSmemMats;
+            const float4* gm = reinterpret_cast<const float4*>(jt.job[j].A.mats);
+            for (int i = tid; i < 2 * nm; i += NT) s_mats[i] = __ldg(gm + i);
             __syncthreads();
             cur_job = j;
         }
@@ -611,7 +627,7 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
         }
         // ---- the gate program of this pass ----
         for (int o = 0; o < d.op_count; ++o) {
-            int4 op = __ldg(ops + o);
+            int4 op = o < kSmemOps ? s_ops[o] : __ldg(ops + o);
             if (op.x == OP_MAP) {
                 __syncthreads();
                 xwrite<RB>(buf, a, tm);
@@ -619,7 +635,7 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
                 decode_map<RB>(d, op.y, op.z, op.w, tid, g.fixed_val, tm);
                 xread<RB>(buf, a, tm);
             } else {
-                apply_op<RB>(op, a, tm, A, g.sample + tm.sample_off);
+                apply_op<RB>(op, a, tm, A, s_mats, g.sample + tm.sample_off);
             }
         }
         // ---- epilogue (the planner left the natural mapping) ----
@@ -734,7 +750,9 @@ __global__ void __launch_bounds__(1 << (TB - RB), 1)
     constexpr int AMPS = 1 << TB;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* pbuf0 = reinterpret_cast<float2*>(smem_raw);  // psi, lambda, psi, lambda
-    float* gacc = reinterpret_cast<float*>(pbuf0 + 4 * AMPS);  // [ngrad][NT]
+    int4* s_ops = reinterpret_cast<int4*>(pbuf0 + 4 * AMPS);         // [kSmemOps]
+    float4* s_mats = reinterpret_cast<float4*>(s_ops + kSmemOps);     // [kSmemMats][2]
+    float* gacc = reinterpret_cast<float*>(s_mats + 2 * kSmemMats);  // [ngrad][NT]
     // sample (within the tile) each partial belongs to: the thread's sample
     // bits depend on the mapping in force when the gradient op ran
     uint8_t* gsmp = reinterpret_cast<uint8_t*>(gacc + max_grad_per_pass(RB) * NT);  // [ngrad][NT]
@@ -747,6 +765,12 @@ __global__ void __launch_bounds__(1 << (TB - RB), 1)
     __syncthreads();
     const PassDesc& d = sd;
     const int4* ops = ops_all + d.op_begin;
+    for (int i = tid; i < d.op_count && i < kSmemOps; i += NT) s_ops[i] = __ldg(ops + i);
+    {
+        const int nm = A.nslots_shared < kSmemMats ? A.nslots_shared : kSmemMats;
+        const float4* gm = reinterpret_cast<const float4*>(A.mats);
+        for (int i = tid; i < 2 * nm; i += NT) s_mats[i] = __ldg(gm + i);
+    }
     const int n = A.n;
     const float2* psi_src = d.psi_from_ckpt >= 0 ? A.ckpt + (int64_t)d.psi_from_ckpt * (A.batch << n) : A.state;
     const bool last = (d.epi & EPI_STORE) == 0;  // final backward pass: nothing to store but lambda
@@ -795,7 +819,7 @@ __global__ void __launch_bounds__(1 << (TB - RB), 1)
             issue_tile_load(d, gn, A.lam, nps + AMPS, &bars[(iter + 1) & 1], n, lane);
         }
         for (int o = 0; o < d.op_count; ++o) {
-            int4 op = __ldg(ops + o);
+            int4 op = o < kSmemOps ? s_ops[o] : __ldg(ops + o);
             if (op.x == OP_MAP) {
                 __syncthreads();
                 xwrite<RB>(ps, psi, tm);
@@ -815,12 +839,12 @@ __global__ void __launch_bounds__(1 << (TB - RB), 1)
                 gacc[(gslot - d.grad_base) * NT + tid] = gsum;
                 gsmp[(gslot - d.grad_base) * NT + tid] = (uint8_t)tm.sample_off;
                 float2 m[4];
-                load_slot(A, op.z, op.w, g.sample + tm.sample_off, m);
+                load_slot(A, s_mats, op.z, op.w, g.sample + tm.sample_off, m);
                 mat_dispatch<RB>(op.y, psi, m);
                 mat_dispatch<RB>(op.y, lam, m);
             } else {
-                apply_op<RB>(op, psi, tm, A, g.sample + tm.sample_off);
-                apply_op<RB>(op, lam, tm, A, g.sample + tm.sample_off);
+                apply_op<RB>(op, psi, tm, A, s_mats, g.sample + tm.sample_off);
+                apply_op<RB>(op, lam, tm, A, s_mats, g.sample + tm.sample_off);
             }
         }
         __syncthreads();
@@ -1114,7 +1138,7 @@ static BwdLayout bwd_layout(const ProgramRun& R, int64_t B) {
 template <int TB, int RB, int MAXJ>
 static int launch_fwd_jobs(const JobTable<MAXJ>& jt, cudaStream_t st) {
     constexpr int NT = 1 << (TB - RB);
-    size_t smem = 2 * (size_t(1) << TB) * sizeof(float2);
+    size_t smem = 2 * (size_t(1) << TB) * sizeof(float2) + kSmemOps * sizeof(int4) + kSmemMats * 2 * sizeof(float4);
     static bool attr_set = false;
     if (!attr_set) {
         QG_CUDA_TRY(
@@ -1170,7 +1194,8 @@ template <int TB, int RB>
 static int launch_bwd_pass(const PassDesc* dpass, const int4* dops, int p, const RunArgs& A, int store_lam,
                            int64_t tiles, cudaStream_t st) {
     constexpr int NT = 1 << (TB - RB);
-    size_t smem = 4 * (size_t(1) << TB) * sizeof(float2) + (size_t)max_grad_per_pass(RB) * NT * (sizeof(float) + 1);
+    size_t smem = 4 * (size_t(1) << TB) * sizeof(float2) + kSmemOps * sizeof(int4) + kSmemMats * 2 * sizeof(float4) +
+                  (size_t)max_grad_per_pass(RB) * NT * (sizeof(float) + 1);
     static bool attr_set = false;
     if (!attr_set) {
         QG_CUDA_TRY(cudaFuncSetAttribute(k_bwd_pass<TB, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1254,6 +1279,7 @@ static int fwd_args(const qg_program* prog, const void* dev_table, void* workspa
     A.batch = batch;
     A.n = R.n;
     A.nslots_ps = R.f_ps;
+    A.nslots_shared = R.f_shared;
     return QG_OK;
 }
 
@@ -1398,6 +1424,7 @@ int qg_program_backward(const qg_program* prog, const void* dev_table, void* wor
     A.batch = batch;
     A.n = R.n;
     A.nslots_ps = R.b_ps;
+    A.nslots_shared = R.b_shared;
     QG_CUDA_TRY(cudaMemsetAsync(ws + L.status, 0, 16, st));
     int64_t items = R.b_shared + (int64_t)R.b_ps * batch;
     if (items > 0) {
