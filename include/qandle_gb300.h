@@ -94,6 +94,19 @@ int64_t qg_measure_p0_scratch_bytes(int64_t batch, int n);
 int qg_measure_p0(const void* state, float* out, int64_t batch, int n, void* scratch,
                   int64_t scratch_bytes, void* stream);
 
+/* P0 as qg_measure_p0, for callers that cannot allocate device memory when
+ * they measure (inside CUDA graphs that must not grow allocation nodes,
+ * real-time loops without cudaMalloc stalls, hosts whose allocator owns all
+ * device memory).  No counterpart in the reference.  The partial sums live
+ * in one static device array of QG_P0_NOALLOC_MAX_PARTIALS floats (4 MiB) per
+ * device, held until exit; calls needing more
+ * (batch * (2^n / 2^min(n,12)) * (min(n,12) + 1)) return QG_ENOMEM.  The
+ * first call on a device looks up the array's address (make it before any
+ * stream capture); all calls share the array, so calls that overlap on the
+ * GPU race. */
+#define QG_P0_NOALLOC_MAX_PARTIALS (1 << 20)
+int qg_measure_p0_noalloc(const void* state, float* out, int64_t batch, int n, void* stream);
+
 /* Backward of qg_measure_p0: grad_state[b][i] = 2 * sum_q grad_p0[b][q] *
  * [bit (n-1-q) of i clear] * state[b][i]. */
 int qg_measure_p0_backward(const void* state, const float* grad_p0, void* grad_state, int64_t batch,

@@ -81,6 +81,7 @@ SIGNATURES = {
     "qg_probs_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
     "qg_measure_p0_scratch_bytes": (c_int64, [c_int64, c_int]),
     "qg_measure_p0": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_int64, c_void_p]),
+    "qg_measure_p0_noalloc": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p]),
     "qg_measure_p0_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p]),
     "qg_rotation_grad_scratch_bytes": (c_int64, [c_int64, c_int]),
     "qg_rotation_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_int, c_int, c_int,

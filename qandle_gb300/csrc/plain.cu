@@ -11,6 +11,8 @@
 // Here a gate is O(2^n) index arithmetic on the state in place.  Each thread
 // moves 16-byte float4 vectors (two complex64 amplitudes) whenever the gate's
 // lowest bit is >= 1, so a warp touches 512 contiguous bytes per access.
+#include <mutex>
+
 #include "common.cuh"
 #include "qandle_gb300.h"
 
@@ -582,3 +584,68 @@ int qg_rotation_grad(const void* out_state, const void* grad_out, float* dtheta,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------
+// P0 without caller-provided scratch.
+//
+// Some callers of this library cannot allocate device memory at the point
+// where they measure: code running inside a captured or replayed CUDA graph
+// that must not add allocation nodes, real-time loops that forbid
+// cudaMalloc/cudaFree stalls, and bindings from hosts whose allocator owns
+// all device memory and hands out no scratch.  For them the per-chunk
+// partial sums live in one fixed array that every device loading this
+// library holds until the process exits.
+//
+// - Limit: QG_P0_NOALLOC_MAX_PARTIALS floats (4 MiB).  A call needs
+//   batch * (2^n / 2^min(n, 12)) * (min(n, 12) + 1) of them and is refused
+//   beyond that.
+// - Set-up: the first call on a device looks up the array's device address
+//   (cudaGetSymbolAddress, with that device current) and caches it; make that
+//   first call before any stream capture.
+// - Sharing: every call uses the same array.  Nothing in it needs to start at
+//   zero (each block writes all its partials before the reduction reads
+//   them), but calls whose kernels overlap on the GPU (different streams,
+//   threads or graphs without ordering) race on it.
+static __device__ __align__(256) float g_p0_partials[QG_P0_NOALLOC_MAX_PARTIALS];
+
+namespace {
+std::mutex g_p0_partials_mu;
+float* g_p0_partials_ptr[256];  // per device ordinal, looked up once
+}  // namespace
+
+extern "C" int qg_measure_p0_noalloc(const void* state, float* out, int64_t batch, int n, void* stream) {
+    int rc = check_state(state, batch, n);
+    if (rc) return rc;
+    QG_CHECK_ARG(out != nullptr, "out is null");
+    if (n == 0) return QG_OK;
+    int c = n < kChunkBits ? n : kChunkBits;
+    int64_t nch = (int64_t(1) << n) >> c;
+    int64_t need = batch * nch * (c + 1);
+    if (need > (int64_t)QG_P0_NOALLOC_MAX_PARTIALS) {
+        qg::set_error("qg_measure_p0_noalloc: batch " + std::to_string(batch) + " at " + std::to_string(n) +
+                      " qubits needs " + std::to_string(need) + " partial sums, the static array holds " +
+                      std::to_string((int64_t)QG_P0_NOALLOC_MAX_PARTIALS) +
+                      "; use qg_measure_p0 with a caller-provided scratch buffer");
+        return QG_ENOMEM;
+    }
+    int dev = 0;
+    QG_CUDA_TRY(cudaGetDevice(&dev));
+    QG_CHECK_ARG(dev >= 0 && dev < 256, "device ordinal out of range");
+    float* part = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_p0_partials_mu);
+        if (!g_p0_partials_ptr[dev]) {
+            void* p = nullptr;
+            QG_CUDA_TRY(cudaGetSymbolAddress(&p, g_p0_partials));
+            g_p0_partials_ptr[dev] = (float*)p;
+        }
+        part = g_p0_partials_ptr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned grid = (unsigned)(nch * batch);
+    k_p0_partial<<<grid, kRedThreads, 0, st>>>((const float2*)state, part, n, c);
+    QG_LAUNCH_CHECK();
+    k_p0_final<<<grid_for(batch * n, 128), 128, 0, st>>>(part, out, batch, n, c, nch);
+    QG_LAUNCH_CHECK();
+    return QG_OK;
+}
