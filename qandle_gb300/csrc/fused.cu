@@ -21,6 +21,7 @@
 
 #include "common.cuh"
 #include "engine.h"
+#include "planar.cuh"
 #include "qandle_gb300.h"
 
 namespace qg {
@@ -80,10 +81,10 @@ __device__ __forceinline__ void fence_proxy_async() {
 
 // ------------------------------------------------------- tile geometry --
 
-// Swizzled shared-memory slot of local index j: the low 4 bits are XORed with
-// the 4-bit groups above them, so any 4 lane bits with distinct (bit mod 4)
-// hit distinct 8-byte bank pairs.
-__device__ __forceinline__ int swz(int j) { return j ^ (((j >> 4) ^ (j >> 8) ^ (j >> 12)) & 15); }
+// Swizzled shared-memory slot of local index j: the low 5 bits are XORed with
+// the 5-bit groups above them, so 32 lanes whose local bits have distinct
+// (bit mod 5) hit the 32 distinct 4-byte banks of a planar exchange.
+__device__ __forceinline__ int swz(int j) { return j ^ (((j >> 5) ^ (j >> 10)) & 31); }
 
 struct TileGeo {
     int64_t sample;       // first sample of the tile
@@ -451,6 +452,183 @@ __device__ __forceinline__ void apply_op(const int4 op, float2 (&a)[1 << RB], co
     }
 }
 
+// ------------------------------------------------ planar forward ops --
+
+template <int RB>
+__device__ __forceinline__ void pload_nat(PTile<RB>& t, const float2* buf, int tid) {
+#pragma unroll
+    for (int r = 0; r < (1 << RB); ++r) set_amp<RB>(t, r, buf[nat_index<RB>(r, tid)]);
+}
+
+// Natural-order store; physical register r holds logical amplitude r ^ xm.
+template <int RB>
+__device__ __forceinline__ void pstore_nat(const PTile<RB>& t, float2* buf, int tid, uint32_t xm) {
+    const int x = (int)xm << 5;
+#pragma unroll
+    for (int r = 0; r < (1 << RB); ++r) buf[nat_index<RB>(r, tid) ^ x] = get_amp<RB>(t, r);
+}
+
+template <int RB>
+__device__ __forceinline__ void pstore_probs(const PTile<RB>& t, float* pb, int tid, uint32_t xm) {
+    const int x = (int)xm << 5;
+#pragma unroll
+    for (int k = 0; k < (1 << (RB - 1)); ++k) {
+        const float2 p = vfma(t.I[k], t.I[k], vmul(t.R[k], t.R[k]));
+        pb[nat_index<RB>(2 * k, tid) ^ x] = p.x;
+        pb[nat_index<RB>(2 * k + 1, tid) ^ x] = p.y;
+    }
+}
+
+// Exchange through planar shared memory (re plane, im plane), folding the
+// pending X of the thread into the write addresses.
+template <int RB, int K = 0>
+__device__ __forceinline__ void pxwrite_k(float* plane, const PTile<RB>& t, const ThreadMap& m, int base, int amps) {
+    const int slot = base ^ ((K & 1) ? m.sw[0] : 0) ^ ((K & 2) ? m.sw[1] : 0) ^ ((K & 4) ? m.sw[2] : 0) ^
+                     ((K & 8) ? m.sw[3] : 0) ^ ((K & 16) ? m.sw[4] : 0);
+    const float2 a = get_amp<RB>(t, K);
+    plane[slot] = a.x;
+    plane[slot + amps] = a.y;
+    if constexpr (K + 1 < (1 << RB)) pxwrite_k<RB, K + 1>(plane, t, m, base, amps);
+}
+template <int RB, int K = 0>
+__device__ __forceinline__ void pxread_k(const float* plane, PTile<RB>& t, const ThreadMap& m, int amps) {
+    const int slot = m.sw_base ^ ((K & 1) ? m.sw[0] : 0) ^ ((K & 2) ? m.sw[1] : 0) ^ ((K & 4) ? m.sw[2] : 0) ^
+                     ((K & 8) ? m.sw[3] : 0) ^ ((K & 16) ? m.sw[4] : 0);
+    set_amp<RB>(t, K, make_float2(plane[slot], plane[slot + amps]));
+    if constexpr (K + 1 < (1 << RB)) pxread_k<RB, K + 1>(plane, t, m, amps);
+}
+
+template <int RB>
+__device__ __forceinline__ int xm_slot_offset(const ThreadMap& m, uint32_t xm) {
+    int o = 0;
+#pragma unroll
+    for (int k = 0; k < RB; ++k)
+        if ((xm >> k) & 1) o ^= m.sw[k];
+    return o;
+}
+
+// Apply the pending X of register bit p and clear it.
+template <int RB>
+__device__ __forceinline__ void pmaterialize(PTile<RB>& t, uint32_t& xm, int p) {
+    const bool c = (xm >> p) & 1;
+    for_pos<RB>(p, [&](auto P) { pswap_if<decltype(P)::value, RB>(t, c); });
+    xm &= ~(1u << p);
+}
+
+template <int RB>
+__device__ __forceinline__ void pnegate_mask(PTile<RB>& t, uint32_t mask) {
+    // mask has 0, 1 or 2 register bits
+    switch (mask) {
+        case 0: pnegate<0, RB>(t); break;
+        case 1: pnegate<1, RB>(t); break;
+        case 2: pnegate<2, RB>(t); break;
+        case 4: pnegate<4, RB>(t); break;
+        case 8: pnegate<8, RB>(t); break;
+        case 3: pnegate<3, RB>(t); break;
+        case 5: pnegate<5, RB>(t); break;
+        case 6: pnegate<6, RB>(t); break;
+        case 9: pnegate<9, RB>(t); break;
+        case 10: pnegate<10, RB>(t); break;
+        case 12: pnegate<12, RB>(t); break;
+        default:
+            if constexpr (RB > 4) {
+                switch (mask) {
+                    case 16: pnegate<16, RB>(t); break;
+                    case 17: pnegate<17, RB>(t); break;
+                    case 18: pnegate<18, RB>(t); break;
+                    case 20: pnegate<20, RB>(t); break;
+                    case 24: pnegate<24, RB>(t); break;
+                    default: break;
+                }
+            }
+            break;
+    }
+}
+
+// Apply one non-map op to a planar tile with pending X mask xm.
+template <int RB>
+__device__ __forceinline__ void papply_op(const int4 op, PTile<RB>& t, uint32_t& xm, const ThreadMap& tm,
+                                          const RunArgs& A, const float4* smats, int64_t sample) {
+    switch (op.x) {
+        case OP_MAT: {
+            float2 m[4];
+            load_slot(A, smats, op.z, op.w, sample, m);
+            if ((xm >> op.y) & 1) {  // X M X
+                const float2 m0 = m[0], m1 = m[1];
+                m[0] = m[3];
+                m[1] = m[2];
+                m[2] = m1;
+                m[3] = m0;
+            }
+            for_pos<RB>(op.y, [&](auto P) { pmat<decltype(P)::value, RB>(t, m); });
+            break;
+        }
+        case OP_DIAG: {
+            float2 m[4];
+            load_slot(A, smats, op.z, op.w, sample, m);
+            if (op.y & LOC_REG) {
+                const int p = op.y & 7;
+                const bool sw = (xm >> p) & 1;
+                const float2 d0 = sw ? m[3] : m[0], d1 = sw ? m[0] : m[3];
+                for_pos<RB>(p, [&](auto P) { pdiag<decltype(P)::value, RB>(t, d0, d1); });
+            } else {
+                pscale<RB>(t, loc_bit_thread(op.y, tm.tglob) ? m[3] : m[0]);
+            }
+            break;
+        }
+        case OP_CX: {
+            if (op.z & LOC_REG) {
+                const int c = op.z & 7;
+                if ((xm >> c) & 1) pmaterialize<RB>(t, xm, c);  // the control must be materialised
+                // a pending X on the target commutes with the CNOT and stays pending
+                for_pos<RB>(op.y, [&](auto P) {
+                    for_pos<RB>(c, [&](auto C) {
+                        if constexpr (decltype(P)::value != decltype(C)::value)
+                            pcx<decltype(P)::value, decltype(C)::value, RB>(t);
+                    });
+                });
+            } else {
+                xm ^= (uint32_t)loc_bit_thread(op.z, tm.tglob) << op.y;
+            }
+            break;
+        }
+        case OP_CZ: {
+            uint32_t mask = 0;
+            bool cond = true;
+            if (op.y & LOC_REG) {
+                const int p = op.y & 7;
+                if ((xm >> p) & 1) pmaterialize<RB>(t, xm, p);
+                mask |= 1u << p;
+            } else {
+                cond = cond && loc_bit_thread(op.y, tm.tglob);
+            }
+            if (op.z & LOC_REG) {
+                const int p = op.z & 7;
+                if ((xm >> p) & 1) pmaterialize<RB>(t, xm, p);
+                mask |= 1u << p;
+            } else {
+                cond = cond && loc_bit_thread(op.z, tm.tglob);
+            }
+            if (cond) pnegate_mask<RB>(t, mask);
+            break;
+        }
+        case OP_SWAP: {
+            if (op.y == op.z) break;
+            if ((xm >> op.y) & 1) pmaterialize<RB>(t, xm, op.y);
+            if ((xm >> op.z) & 1) pmaterialize<RB>(t, xm, op.z);
+            for_pos<RB>(op.y, [&](auto P0) {
+                for_pos<RB>(op.z, [&](auto P1) {
+                    if constexpr (decltype(P0)::value != decltype(P1)::value)
+                        pswapbits<decltype(P0)::value, decltype(P1)::value, RB>(t);
+                });
+            });
+            break;
+        }
+        default:
+            break;
+    }
+}
+
 // --------------------------------------------------------- the pass --
 
 template <int TB>
@@ -567,7 +745,8 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
         const int n = A.n;
         const bool load_in = tile_loads(j);
         TileGeo g = tile_geo(d, t - jt.begin[j], n, A.batch);
-        float2 a[1 << RB];
+        PTile<RB> pt;
+        uint32_t xm = 0;  // pending thread-controlled X per register bit
         ThreadMap tm;
         if (load_in) {
             bool ok = mbar_wait(&bars[iter & 1], phase[iter & 1] & 1);
@@ -576,8 +755,7 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
                 if (tid == 0) atomicExch(A.status, QG_ETIMEOUT);
                 break;
             }
-#pragma unroll
-            for (int r = 0; r < (1 << RB); ++r) a[r] = buf[nat_index<RB>(r, tid)];
+            pload_nat<RB>(pt, buf, tid);
             decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
         } else {
             if (d.init == INIT_EMBED)
@@ -595,6 +773,7 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
                     if (regmask & (1u << b)) continue;
                     c = cmul(c, fac[2 * (n - 1 - b) + ((tm.tglob >> b) & 1)]);
                 }
+                float2 a[1 << RB];
                 a[0] = c;
 #pragma unroll
                 for (int k = 0; k < RB; ++k) {
@@ -606,16 +785,18 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
                         a[r] = cmul(a[r], f0);
                     }
                 }
+#pragma unroll
+                for (int r = 0; r < (1 << RB); ++r) set_amp<RB>(pt, r, a[r]);
             } else if (d.init == INIT_EMBED) {
 #pragma unroll
-                for (int r = 0; r < (1 << RB); ++r) a[r] = make_float2(0.f, 0.f);
+                for (int r = 0; r < (1 << RB); ++r) set_amp<RB>(pt, r, make_float2(0.f, 0.f));
             } else {
                 // |0..0>: amplitude 1 where every qubit bit (in and outside the tile) is 0
                 const int qmask = (1 << d.nq_tile) - 1;
 #pragma unroll
                 for (int r = 0; r < (1 << RB); ++r) {
                     bool origin = g.fixed_val == 0 && ((tm.thr_off + roff_rt<RB>(tm, r)) & qmask) == 0;
-                    a[r] = make_float2(origin ? 1.f : 0.f, 0.f);
+                    set_amp<RB>(pt, r, make_float2(origin ? 1.f : 0.f, 0.f));
                 }
             }
         }
@@ -629,21 +810,22 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
         for (int o = 0; o < d.op_count; ++o) {
             int4 op = o < kSmemOps ? s_ops[o] : __ldg(ops + o);
             if (op.x == OP_MAP) {
+                float* plane = reinterpret_cast<float*>(buf);
                 __syncthreads();
-                xwrite<RB>(buf, a, tm);
+                pxwrite_k<RB>(plane, pt, tm, tm.sw_base ^ xm_slot_offset<RB>(tm, xm), AMPS);
+                xm = 0;
                 __syncthreads();
                 decode_map<RB>(d, op.y, op.z, op.w, tid, g.fixed_val, tm);
-                xread<RB>(buf, a, tm);
+                pxread_k<RB>(plane, pt, tm, AMPS);
             } else {
-                apply_op<RB>(op, a, tm, A, s_mats, g.sample + tm.sample_off);
+                papply_op<RB>(op, pt, xm, tm, A, s_mats, g.sample + tm.sample_off);
             }
         }
         // ---- epilogue (the planner left the natural mapping) ----
         __syncthreads();  // all exchange reads of `buf` are done
         const int64_t smp0 = g.sample;
         if (d.epi & EPI_STORE) {
-#pragma unroll
-            for (int r = 0; r < (1 << RB); ++r) buf[nat_index<RB>(r, tid)] = a[r];
+            pstore_nat<RB>(pt, buf, tid, xm);
             fence_proxy_async();
             __syncthreads();
             if (tid < 32) {
@@ -658,8 +840,7 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
                 __syncthreads();
             }
             float* pb = reinterpret_cast<float*>(buf);
-#pragma unroll
-            for (int r = 0; r < (1 << RB); ++r) pb[nat_index<RB>(r, tid)] = a[r].x * a[r].x + a[r].y * a[r].y;
+            pstore_probs<RB>(pt, pb, tid, xm);
             if (d.epi & EPI_PROBS) {
                 fence_proxy_async();
                 __syncthreads();

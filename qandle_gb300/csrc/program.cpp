@@ -242,14 +242,12 @@ Mapping mapping_for(uint32_t R, int tb, int rb) {
     std::vector<int> lanes;
     int used = 0;
     for (int b : rest) {
-        int cls = b & 3;  // swizzle image of local bit b is e_(b mod 4)
-        if ((int)lanes.size() < 4 && !(used & (1 << cls))) {
+        int cls = b % 5;  // swizzle image of local bit b is e_(b mod 5)
+        if ((int)lanes.size() < 5 && !(used & (1 << cls))) {
             lanes.push_back(b);
             used |= 1 << cls;
         }
     }
-    for (int b : rest)
-        if ((int)lanes.size() < 4 && std::find(lanes.begin(), lanes.end(), b) == lanes.end()) lanes.push_back(b);
     for (int b : rest)
         if ((int)lanes.size() < 5 && std::find(lanes.begin(), lanes.end(), b) == lanes.end()) lanes.push_back(b);
     for (int k = 0; k < 5; ++k) m.lane[k] = lanes[k];
