@@ -9,6 +9,8 @@ namespace qg {
 constexpr int kRegBits = 5;         // amplitudes per thread = 2^5, held in registers
 constexpr int kMaxTileBits = 13;    // forward tile: 2^13 amplitudes, 256 threads, 64 KiB
 constexpr int kMaxQubits = 30;      // fused engine limit (global bit masks are 32-bit)
+// register bits of the backward pass kernel (psi and lambda tiles per thread)
+constexpr int kBwdRegBits = 4;
 // backward: gradient slots per pass (their partials live in shared memory
 // beside the psi/lambda double buffer, 5 B per slot and thread)
 __host__ __device__ constexpr int max_grad_per_pass(int reg_bits) { return reg_bits == 4 ? 64 : 96; }

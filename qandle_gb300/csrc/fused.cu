@@ -507,11 +507,13 @@ __device__ __forceinline__ int xm_slot_offset(const ThreadMap& m, uint32_t xm) {
     return o;
 }
 
-// Apply the pending X of register bit p and clear it.
-template <int RB>
-__device__ __forceinline__ void pmaterialize(PTile<RB>& t, uint32_t& xm, int p) {
+// Apply the pending X of register bit p to the given tiles and clear it.
+template <int RB, int NTILE>
+__device__ __forceinline__ void pmaterialize(PTile<RB>* const (&ts)[NTILE], uint32_t& xm, int p) {
     const bool c = (xm >> p) & 1;
-    for_pos<RB>(p, [&](auto P) { pswap_if<decltype(P)::value, RB>(t, c); });
+#pragma unroll
+    for (int i = 0; i < NTILE; ++i)
+        for_pos<RB>(p, [&](auto P) { pswap_if<decltype(P)::value, RB>(*ts[i], c); });
     xm &= ~(1u << p);
 }
 
@@ -545,10 +547,12 @@ __device__ __forceinline__ void pnegate_mask(PTile<RB>& t, uint32_t mask) {
     }
 }
 
-// Apply one non-map op to a planar tile with pending X mask xm.
-template <int RB>
-__device__ __forceinline__ void papply_op(const int4 op, PTile<RB>& t, uint32_t& xm, const ThreadMap& tm,
-                                          const RunArgs& A, const float4* smats, int64_t sample) {
+// Apply one non-map op to NTILE planar tiles (psi, and lambda in the
+// backward) that share the pending X mask xm.
+template <int RB, int NTILE>
+__device__ __forceinline__ void papply_op(const int4 op, PTile<RB>* const (&ts)[NTILE], uint32_t& xm,
+                                          const ThreadMap& tm, const RunArgs& A, const float4* smats,
+                                          int64_t sample) {
     switch (op.x) {
         case OP_MAT: {
             float2 m[4];
@@ -560,7 +564,9 @@ __device__ __forceinline__ void papply_op(const int4 op, PTile<RB>& t, uint32_t&
                 m[2] = m1;
                 m[3] = m0;
             }
-            for_pos<RB>(op.y, [&](auto P) { pmat<decltype(P)::value, RB>(t, m); });
+#pragma unroll
+            for (int i = 0; i < NTILE; ++i)
+                for_pos<RB>(op.y, [&](auto P) { pmat<decltype(P)::value, RB>(*ts[i], m); });
             break;
         }
         case OP_DIAG: {
@@ -570,23 +576,29 @@ __device__ __forceinline__ void papply_op(const int4 op, PTile<RB>& t, uint32_t&
                 const int p = op.y & 7;
                 const bool sw = (xm >> p) & 1;
                 const float2 d0 = sw ? m[3] : m[0], d1 = sw ? m[0] : m[3];
-                for_pos<RB>(p, [&](auto P) { pdiag<decltype(P)::value, RB>(t, d0, d1); });
+#pragma unroll
+                for (int i = 0; i < NTILE; ++i)
+                    for_pos<RB>(p, [&](auto P) { pdiag<decltype(P)::value, RB>(*ts[i], d0, d1); });
             } else {
-                pscale<RB>(t, loc_bit_thread(op.y, tm.tglob) ? m[3] : m[0]);
+                const float2 d = loc_bit_thread(op.y, tm.tglob) ? m[3] : m[0];
+#pragma unroll
+                for (int i = 0; i < NTILE; ++i) pscale<RB>(*ts[i], d);
             }
             break;
         }
         case OP_CX: {
             if (op.z & LOC_REG) {
                 const int c = op.z & 7;
-                if ((xm >> c) & 1) pmaterialize<RB>(t, xm, c);  // the control must be materialised
+                if ((xm >> c) & 1) pmaterialize<RB, NTILE>(ts, xm, c);  // the control must be materialised
                 // a pending X on the target commutes with the CNOT and stays pending
-                for_pos<RB>(op.y, [&](auto P) {
-                    for_pos<RB>(c, [&](auto C) {
-                        if constexpr (decltype(P)::value != decltype(C)::value)
-                            pcx<decltype(P)::value, decltype(C)::value, RB>(t);
+#pragma unroll
+                for (int i = 0; i < NTILE; ++i)
+                    for_pos<RB>(op.y, [&](auto P) {
+                        for_pos<RB>(c, [&](auto C) {
+                            if constexpr (decltype(P)::value != decltype(C)::value)
+                                pcx<decltype(P)::value, decltype(C)::value, RB>(*ts[i]);
+                        });
                     });
-                });
             } else {
                 xm ^= (uint32_t)loc_bit_thread(op.z, tm.tglob) << op.y;
             }
@@ -597,36 +609,49 @@ __device__ __forceinline__ void papply_op(const int4 op, PTile<RB>& t, uint32_t&
             bool cond = true;
             if (op.y & LOC_REG) {
                 const int p = op.y & 7;
-                if ((xm >> p) & 1) pmaterialize<RB>(t, xm, p);
+                if ((xm >> p) & 1) pmaterialize<RB, NTILE>(ts, xm, p);
                 mask |= 1u << p;
             } else {
                 cond = cond && loc_bit_thread(op.y, tm.tglob);
             }
             if (op.z & LOC_REG) {
                 const int p = op.z & 7;
-                if ((xm >> p) & 1) pmaterialize<RB>(t, xm, p);
+                if ((xm >> p) & 1) pmaterialize<RB, NTILE>(ts, xm, p);
                 mask |= 1u << p;
             } else {
                 cond = cond && loc_bit_thread(op.z, tm.tglob);
             }
-            if (cond) pnegate_mask<RB>(t, mask);
+            if (cond)
+#pragma unroll
+                for (int i = 0; i < NTILE; ++i) pnegate_mask<RB>(*ts[i], mask);
             break;
         }
         case OP_SWAP: {
             if (op.y == op.z) break;
-            if ((xm >> op.y) & 1) pmaterialize<RB>(t, xm, op.y);
-            if ((xm >> op.z) & 1) pmaterialize<RB>(t, xm, op.z);
-            for_pos<RB>(op.y, [&](auto P0) {
-                for_pos<RB>(op.z, [&](auto P1) {
-                    if constexpr (decltype(P0)::value != decltype(P1)::value)
-                        pswapbits<decltype(P0)::value, decltype(P1)::value, RB>(t);
+            if ((xm >> op.y) & 1) pmaterialize<RB, NTILE>(ts, xm, op.y);
+            if ((xm >> op.z) & 1) pmaterialize<RB, NTILE>(ts, xm, op.z);
+#pragma unroll
+            for (int i = 0; i < NTILE; ++i)
+                for_pos<RB>(op.y, [&](auto P0) {
+                    for_pos<RB>(op.z, [&](auto P1) {
+                        if constexpr (decltype(P0)::value != decltype(P1)::value)
+                            pswapbits<decltype(P0)::value, decltype(P1)::value, RB>(*ts[i]);
+                    });
                 });
-            });
             break;
         }
         default:
             break;
     }
+}
+
+// Gradient partial on register bit p with the pending X folded in: the
+// physical pair order turns the generator G into X G X (= -G for Y and Z).
+template <int RB>
+__device__ __forceinline__ float pgrad_op(const PTile<RB>& ps, const PTile<RB>& ls, int p, int axis, uint32_t xm) {
+    float g = 0.f;
+    for_pos<RB>(p, [&](auto P) { g = pgrad<decltype(P)::value, RB>(ps, ls, axis); });
+    return (((xm >> p) & 1) && axis != AX_X) ? -g : g;
 }
 
 // --------------------------------------------------------- the pass --
@@ -818,7 +843,8 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
                 decode_map<RB>(d, op.y, op.z, op.w, tid, g.fixed_val, tm);
                 pxread_k<RB>(plane, pt, tm, AMPS);
             } else {
-                papply_op<RB>(op, pt, xm, tm, A, s_mats, g.sample + tm.sample_off);
+                PTile<RB>* const tiles[1] = {&pt};
+                papply_op<RB, 1>(op, tiles, xm, tm, A, s_mats, g.sample + tm.sample_off);
             }
         }
         // ---- epilogue (the planner left the natural mapping) ----
@@ -977,18 +1003,17 @@ __global__ void __launch_bounds__(1 << (TB - RB), 1)
         float2* ls = ps + AMPS;
         float2* nps = pbuf0 + ((iter + 1) & 1) * 2 * AMPS;
         TileGeo g = tile_geo(d, t, n, A.batch);
-        float2 psi[1 << RB], lam[1 << RB];
+        PTile<RB> pt, lt;
+        PTile<RB>* const tiles[2] = {&pt, &lt};
+        uint32_t xm = 0;  // pending thread-controlled X, shared by psi and lambda
         ThreadMap tm;
         bool ok = mbar_wait(&bars[iter & 1], (iter >> 1) & 1);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicExch(A.status, QG_ETIMEOUT);
             break;
         }
-#pragma unroll
-        for (int r = 0; r < (1 << RB); ++r) {
-            psi[r] = ps[nat_index<RB>(r, tid)];
-            lam[r] = ls[nat_index<RB>(r, tid)];
-        }
+        pload_nat<RB>(pt, ps, tid);
+        pload_nat<RB>(lt, ls, tid);
         decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
         __syncthreads();
         if (tid < 32 && t + gridDim.x < num_tiles) {
@@ -1003,29 +1028,28 @@ __global__ void __launch_bounds__(1 << (TB - RB), 1)
             int4 op = o < kSmemOps ? s_ops[o] : __ldg(ops + o);
             if (op.x == OP_MAP) {
                 __syncthreads();
-                xwrite<RB>(ps, psi, tm);
-                xwrite<RB>(ls, lam, tm);
+                const int base = tm.sw_base ^ xm_slot_offset<RB>(tm, xm);
+                pxwrite_k<RB>(reinterpret_cast<float*>(ps), pt, tm, base, AMPS);
+                pxwrite_k<RB>(reinterpret_cast<float*>(ls), lt, tm, base, AMPS);
+                xm = 0;
                 __syncthreads();
                 decode_map<RB>(d, op.y, op.z, op.w, tid, g.fixed_val, tm);
-                xread<RB>(ps, psi, tm);
-                xread<RB>(ls, lam, tm);
+                pxread_k<RB>(reinterpret_cast<const float*>(ps), pt, tm, AMPS);
+                pxread_k<RB>(reinterpret_cast<const float*>(ls), lt, tm, AMPS);
             } else if (op.x == OP_GRAD) {
-                float gsum = grad_dispatch<RB>(op.y, psi, lam, op.z);
+                float gsum = pgrad_op<RB>(pt, lt, op.y, op.z, xm);
                 gacc[(op.w - d.grad_base) * NT + tid] = gsum;
                 gsmp[(op.w - d.grad_base) * NT + tid] = (uint8_t)tm.sample_off;
             } else if (op.x == OP_MAT && (op.w & OPF_GRAD)) {
                 int axis = (op.w >> 8) & 3;
                 int gslot = op.w >> 12;
-                float gsum = grad_dispatch<RB>(op.y, psi, lam, axis);
+                float gsum = pgrad_op<RB>(pt, lt, op.y, axis, xm);
                 gacc[(gslot - d.grad_base) * NT + tid] = gsum;
                 gsmp[(gslot - d.grad_base) * NT + tid] = (uint8_t)tm.sample_off;
-                float2 m[4];
-                load_slot(A, s_mats, op.z, op.w, g.sample + tm.sample_off, m);
-                mat_dispatch<RB>(op.y, psi, m);
-                mat_dispatch<RB>(op.y, lam, m);
+                papply_op<RB, 2>(make_int4(OP_MAT, op.y, op.z, op.w), tiles, xm, tm, A, s_mats,
+                                 g.sample + tm.sample_off);
             } else {
-                apply_op<RB>(op, psi, tm, A, s_mats, g.sample + tm.sample_off);
-                apply_op<RB>(op, lam, tm, A, s_mats, g.sample + tm.sample_off);
+                papply_op<RB, 2>(op, tiles, xm, tm, A, s_mats, g.sample + tm.sample_off);
             }
         }
         __syncthreads();
@@ -1051,11 +1075,8 @@ __global__ void __launch_bounds__(1 << (TB - RB), 1)
         }
         // store psi and lambda (natural mapping)
         if (d.epi & EPI_STORE) {
-#pragma unroll
-            for (int r = 0; r < (1 << RB); ++r) {
-                ps[nat_index<RB>(r, tid)] = psi[r];
-                ls[nat_index<RB>(r, tid)] = lam[r];
-            }
+            pstore_nat<RB>(pt, ps, tid, xm);
+            pstore_nat<RB>(lt, ls, tid, xm);
             fence_proxy_async();
             __syncthreads();
             if (tid < 32) {
@@ -1064,8 +1085,7 @@ __global__ void __launch_bounds__(1 << (TB - RB), 1)
                 bulk_commit();
             }
         } else if (store_lam_last) {
-#pragma unroll
-            for (int r = 0; r < (1 << RB); ++r) ls[nat_index<RB>(r, tid)] = lam[r];
+            pstore_nat<RB>(lt, ls, tid, xm);
             fence_proxy_async();
             __syncthreads();
             if (tid < 32) {
@@ -1396,17 +1416,12 @@ static int launch_bwd_pass(const PassDesc* dpass, const int4* dops, int p, const
 
 static int launch_bwd(const PassDesc* dpass, const int4* dops, int p, const RunArgs& A, int store_lam,
                       int64_t tiles, int tb, int rb, cudaStream_t st) {
-    if (rb == 4) {
-        switch (tb) {
-            case 12: return launch_bwd_pass<12, 4>(dpass, dops, p, A, store_lam, tiles, st);
-            case 11: return launch_bwd_pass<11, 4>(dpass, dops, p, A, store_lam, tiles, st);
-            default: return launch_bwd_pass<10, 4>(dpass, dops, p, A, store_lam, tiles, st);
-        }
-    }
+    static_assert(kBwdRegBits == 4, "backward kernels are instantiated for 4 register bits");
+    (void)rb;
     switch (tb) {
-        case 12: return launch_bwd_pass<12, 5>(dpass, dops, p, A, store_lam, tiles, st);
-        case 11: return launch_bwd_pass<11, 5>(dpass, dops, p, A, store_lam, tiles, st);
-        default: return launch_bwd_pass<10, 5>(dpass, dops, p, A, store_lam, tiles, st);
+        case 12: return launch_bwd_pass<12, 4>(dpass, dops, p, A, store_lam, tiles, st);
+        case 11: return launch_bwd_pass<11, 4>(dpass, dops, p, A, store_lam, tiles, st);
+        default: return launch_bwd_pass<10, 4>(dpass, dops, p, A, store_lam, tiles, st);
     }
 }
 
@@ -1626,7 +1641,7 @@ int qg_program_backward(const qg_program* prog, const void* dev_table, void* wor
     int64_t tiles = num_tiles(R.n, tb, batch);
     for (int p = 0; p < R.nbpass; ++p) {
         int store_lam = (p + 1 == R.nbpass) && dstate != nullptr;
-        int rc = launch_bwd(dpass, dops, p, A, store_lam, tiles, tb, R.reg_bits, st);
+        int rc = launch_bwd(dpass, dops, p, A, store_lam, tiles, tb, kBwdRegBits, st);
         if (rc) return rc;
     }
     int64_t fitems = R.nparams + (int64_t)R.ncols * batch;

@@ -215,3 +215,65 @@ __device__ __forceinline__ void pnegate(PTile<RB>& t) {
 }
 
 }  // namespace qg
+
+namespace qg {
+
+// Im( conj(l0) (P p)_0 + conj(l1) (P p)_1 ) summed over the register-bit-P
+// pairs of psi (p) and lambda (l); P is the generator of the rotation axis.
+template <int P, int RB>
+__device__ __forceinline__ float pgrad(const PTile<RB>& ps, const PTile<RB>& ls, int axis) {
+    constexpr int H = 1 << (RB - 1);
+    float2 acc = make_float2(0.f, 0.f);
+    const float2 one = bcast(1.f), mone = bcast(-1.f);
+#pragma unroll
+    for (int k = 0; k < H; ++k) {
+        float2 p0r, p0i, p1r, p1i, l0r, l0i, l1r, l1i;
+        if constexpr (P == 0) {
+            if (k & 0) continue;
+            // pairs are the two lanes of a vector: element 0 = lane x, element 1 = lane y
+            p0r = ps.R[k];
+            p0i = ps.I[k];
+            p1r = lswap(ps.R[k]);
+            p1i = lswap(ps.I[k]);
+            l0r = ls.R[k];
+            l0i = ls.I[k];
+            l1r = lswap(ls.R[k]);
+            l1i = lswap(ls.I[k]);
+            // both lanes hold one pair seen from either side: count each pair once
+            // by weighting lane y with 0 below
+        } else {
+            constexpr int Q = 1 << (P - 1);
+            if (k & Q) continue;
+            p0r = ps.R[k];
+            p0i = ps.I[k];
+            p1r = ps.R[k | Q];
+            p1i = ps.I[k | Q];
+            l0r = ls.R[k];
+            l0i = ls.I[k];
+            l1r = ls.R[k | Q];
+            l1i = ls.I[k | Q];
+        }
+        float2 g;
+        if (axis == AX_X) {
+            // l0r p1i - l0i p1r + l1r p0i - l1i p0r
+            g = vfma(l0r, p1i, vmul(vmul(l0i, mone), p1r));
+            g = vfma(l1r, p0i, g);
+            g = vfma(vmul(l1i, mone), p0r, g);
+        } else if (axis == AX_Y) {
+            // -(l0r p1r + l0i p1i) + (l1r p0r + l1i p0i)
+            g = vfma(l1r, p0r, vmul(l1i, p0i));
+            g = vfma(vmul(l0r, mone), p1r, g);
+            g = vfma(vmul(l0i, mone), p1i, g);
+        } else {
+            // (l0r p0i - l0i p0r) - (l1r p1i - l1i p1r)
+            g = vfma(l0r, p0i, vmul(vmul(l0i, mone), p0r));
+            g = vfma(vmul(l1r, mone), p1i, g);
+            g = vfma(l1i, p1r, g);
+        }
+        if constexpr (P == 0) g.y = 0.f;
+        acc = vfma(g, one, acc);
+    }
+    return acc.x + acc.y;
+}
+
+}  // namespace qg

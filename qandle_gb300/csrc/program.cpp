@@ -315,7 +315,8 @@ void emit_pass(Program& P, PassPlan& pp, const std::vector<LGate>& G, bool backw
     for (int j = 0; j < d.nq_tile; ++j) g2l[d.gbit[j]] = j;
     uint32_t qubit_local = (d.nq_tile >= 32) ? 0xffffffffu : ((1u << d.nq_tile) - 1);
 
-    const int rb = P.opt.reg_bits;
+    // the backward holds psi and lambda, so it keeps 16 amplitudes of each per thread
+    const int rb = backward ? kBwdRegBits : P.opt.reg_bits;
     Mapping nat = natural_mapping(tb, rb);
     uint32_t natR = 0;
     for (int k = 0; k < rb; ++k) natR |= 1u << nat.reg[k];
@@ -505,7 +506,7 @@ void plan_segment(Program& P, const std::vector<LGate>& G, std::vector<int> pend
     while (!pending.empty()) {
         Selector s;
         s.backward = backward;
-        if (backward) s.max_grad = max_grad_per_pass(P.opt.reg_bits);
+        if (backward) s.max_grad = max_grad_per_pass(kBwdRegBits);
         if (n <= tb) {
             s.S = (n >= 32) ? 0xffffffffu : ((1u << n) - 1);
             s.addable = 0;

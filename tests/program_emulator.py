@@ -206,7 +206,7 @@ def run_backward(prog, n, B, params, named, umats, psi, lam, ckpts, grad_targets
         samples = np.where(valid, idx >> n, -1)
         T = np.where(valid, src.reshape(-1)[np.maximum(idx, 0)], 0)
         L = np.where(valid, lam.reshape(-1)[np.maximum(idx, 0)], 0)
-        regl = list(range(5, 5 + prog.reg_bits))
+        regl = list(range(5, 5 + 4))  # the backward keeps 16 amplitudes of psi and lambda per thread
         for op in pd["ops"]:
             if op[0] == OP_MAP:
                 regl = _decode(op[1])
