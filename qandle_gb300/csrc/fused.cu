@@ -691,6 +691,11 @@ __device__ __forceinline__ int find_job(const JobTable<MAXJ>& jt, int64_t t) {
 // of the launch (the passes of independent programs / states, e.g. several
 // serving requests of different widths); a single-program forward is a
 // one-job launch.
+// Tile buffers of the forward kernel: three (two loads in flight while one
+// tile computes), four for 2^11 tiles.  Two 2^12 CTAs with three buffers
+// each still fit one SM's shared memory.
+constexpr int fwd_stages(int tb) { return tb >= 12 ? 3 : 4; }
+
 // Resident CTAs per SM the register budget allows: 32 amplitudes per thread
 // (RB = 5) take up to 255 registers, 16 (RB = 4) up to 128.
 template <int TB, int RB>
@@ -703,12 +708,12 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
     k_fwd_pass(const __grid_constant__ JobTable<MAXJ> jt) {
     constexpr int NT = 1 << (TB - RB);
     constexpr int AMPS = 1 << TB;
+    constexpr int S = fwd_stages(TB);  // tile buffers: loads run S-1 tiles ahead
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float2* buf0 = reinterpret_cast<float2*>(smem_raw);
-    float2* buf1 = buf0 + AMPS;
-    int4* s_ops = reinterpret_cast<int4*>(buf1 + AMPS);             // [kSmemOps]
+    float2* bufs = reinterpret_cast<float2*>(smem_raw);
+    int4* s_ops = reinterpret_cast<int4*>(bufs + S * AMPS);         // [kSmemOps]
     float4* s_mats = reinterpret_cast<float4*>(s_ops + kSmemOps);   // [kSmemMats][2]
-    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ __align__(8) uint64_t bars[S];
     __shared__ PassDesc sd;
     __shared__ RunArgs sa;
 
@@ -716,14 +721,15 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
     const int lane = tid & 31;
     const int64_t total = jt.begin[jt.njobs];
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int i = 0; i < S; ++i) mbar_init(&bars[i], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 
-    // loads in flight per buffer: a buffer's mbarrier completes once per load
-    uint32_t phase[2] = {0u, 0u};
+    // loads completed per buffer: a buffer's mbarrier completes once per load
+    uint32_t phase[S];
+#pragma unroll
+    for (int i = 0; i < S; ++i) phase[i] = 0u;
     auto tile_loads = [&](int j) -> bool {
         return jt.job[j].pd->init == INIT_LOAD && !jt.job[j].zero_init;
     };
@@ -738,15 +744,18 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
         issue_tile_load(pd, gn, ra.state, dst, bar, ra.n, lane);
     };
 
-    int64_t t0 = blockIdx.x;
-    if (t0 < total && tile_loads(find_job(jt, t0))) {
-        if (tid < 32) issue_prefetch(t0, buf0, &bars[0]);
+    const int64_t t0 = blockIdx.x;
+    if (tid < 32) {
+        for (int i = 0; i < S - 1; ++i) {
+            const int64_t tp = t0 + (int64_t)i * gridDim.x;
+            if (tp < total && tile_loads(find_job(jt, tp))) issue_prefetch(tp, bufs + i * AMPS, &bars[i]);
+        }
     }
     int cur_job = -1;
     int iter = 0;
     for (int64_t t = t0; t < total; t += gridDim.x, ++iter) {
-        float2* buf = (iter & 1) ? buf1 : buf0;
-        float2* nbuf = (iter & 1) ? buf0 : buf1;
+        const int slot = iter % S;
+        float2* buf = bufs + slot * AMPS;
         const int j = find_job(jt, t);
         if (j != cur_job) {
             __syncthreads();  // nobody reads the previous job's descriptors any more
@@ -774,8 +783,8 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
         uint32_t xm = 0;  // pending thread-controlled X per register bit
         ThreadMap tm;
         if (load_in) {
-            bool ok = mbar_wait(&bars[iter & 1], phase[iter & 1] & 1);
-            ++phase[iter & 1];
+            bool ok = mbar_wait(&bars[slot], phase[slot] & 1);
+            ++phase[slot];
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) atomicExch(A.status, QG_ETIMEOUT);
                 break;
@@ -825,11 +834,16 @@ __global__ void __launch_bounds__(1 << (TB - RB), min_blocks<TB, RB>())
                 }
             }
         }
-        // everybody has read `buf`; prefetch the next tile into the other buffer
+        // everybody has read `buf`; prefetch S-1 tiles ahead into the buffer the
+        // previous tile used (its store has to have read it out first)
         __syncthreads();
-        if (tid < 32 && t + gridDim.x < total && tile_loads(find_job(jt, t + gridDim.x))) {
-            bulk_wait_read0();  // stores issued from nbuf two tiles ago have read it
-            issue_prefetch(t + gridDim.x, nbuf, &bars[(iter + 1) & 1]);
+        {
+            const int64_t tp = t + (int64_t)(S - 1) * gridDim.x;
+            const int ps = (iter + S - 1) % S;
+            if (tid < 32 && tp < total && tile_loads(find_job(jt, tp))) {
+                bulk_wait_read0();
+                issue_prefetch(tp, bufs + ps * AMPS, &bars[ps]);
+            }
         }
         // ---- the gate program of this pass ----
         for (int o = 0; o < d.op_count; ++o) {
@@ -1339,7 +1353,8 @@ static BwdLayout bwd_layout(const ProgramRun& R, int64_t B) {
 template <int TB, int RB, int MAXJ>
 static int launch_fwd_jobs(const JobTable<MAXJ>& jt, cudaStream_t st) {
     constexpr int NT = 1 << (TB - RB);
-    size_t smem = 2 * (size_t(1) << TB) * sizeof(float2) + kSmemOps * sizeof(int4) + kSmemMats * 2 * sizeof(float4);
+    size_t smem = fwd_stages(TB) * (size_t(1) << TB) * sizeof(float2) + kSmemOps * sizeof(int4) +
+                  kSmemMats * 2 * sizeof(float4);
     static bool attr_set = false;
     if (!attr_set) {
         QG_CUDA_TRY(
