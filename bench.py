@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--low-bits", type=int, default=6)
     ap.add_argument("--k", type=int, default=0, help="max strided qubits per pass (0 = tile limit)")
     ap.add_argument("--reg-bits", type=int, default=5, help="amplitudes per thread = 2^reg_bits")
+    ap.add_argument("--interpreted", action="store_true",
+                    help="run the prebuilt op interpreter instead of the per-program compiled passes")
     ap.add_argument("--n", type=int, default=20)
     ap.add_argument("--batch", type=int, default=256)
     return ap.parse_args()
@@ -205,7 +207,8 @@ def main():
     amp_step = workloads.gate_count(desc) * B * (1 << n)
 
     # ---------------- fused forward, inputs resident in HBM ----------------
-    opts = dict(tile_bits=args.tile_bits, low_bits=args.low_bits, max_high=args.k, reg_bits=args.reg_bits)
+    opts = dict(tile_bits=args.tile_bits, low_bits=args.low_bits, max_high=args.k, reg_bits=args.reg_bits,
+                compiled=not args.interpreted)
     circ = workloads.build_circuit(desc, engine="fused", **opts).to(dev)
     kw = workloads.circuit_inputs(desc, dev)
     with torch.no_grad():
@@ -278,7 +281,9 @@ def main():
                    "plan": prog.summary(), "tile": opts},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
-                     "kernel": f"k_fwd_pass<{args.tile_bits}>", "launches_per_step": P,
+                     "kernel": ("k_fwd_pass (op interpreter)" if args.interpreted else
+                                "qg_fwd_pass (compiled per pass)") + f", 2^{args.tile_bits}-amplitude tiles",
+                     "launches_per_step": P,
                      "avg_launch_ms": avg_pass_ms, "algorithmic_bytes_per_launch": avg_bytes,
                      "middle_pass_GBps": mid_gbs},
         "clocks": clock_info,

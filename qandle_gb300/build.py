@@ -38,6 +38,41 @@ def _sources():
     return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
+# Headers the run-time compiler (csrc/jit.cpp) needs, embedded in the library
+# so that it does not depend on the source tree at run time.
+JIT_HEADERS = ["devmath.cuh", "engine.h", "planar.cuh", "fwd_kernel.cuh", "jit_ops.cuh"]
+
+
+def _write_jit_headers() -> str:
+    out = os.path.join(BUILD, "jit_headers.cpp")
+    lines = ["// Generated by qandle_gb300/build.py from csrc/: the headers handed to NVRTC.",
+             "namespace qg {", f"extern const int kJitHeaderCount = {len(JIT_HEADERS)};",
+             "extern const char* const kJitHeaderNames[] = {" +
+             ", ".join(f'"{h}"' for h in JIT_HEADERS) + "};",
+             "extern const char* const kJitHeaderTexts[] = {"]
+    for h in JIT_HEADERS:
+        with open(os.path.join(CSRC, h)) as f:
+            text = f.read()
+        if ")QGJIT" in text:
+            raise RuntimeError(f"{h} contains the raw-string delimiter")
+        lines.append('R"QGJIT(' + text + ')QGJIT",')
+    lines += ["};", "}  // namespace qg", ""]
+    body = "\n".join(lines)
+    if not os.path.exists(out) or open(out).read() != body:
+        with open(out, "w") as f:
+            f.write(body)
+    return out
+
+
+def _cuda_lib_dir() -> str:
+    root = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    for cand in ("lib64", "lib"):
+        d = os.path.join(root, cand)
+        if os.path.isdir(d):
+            return d
+    return "/usr/local/cuda/lib64"
+
+
 def _digest(extra_flags) -> str:
     h = hashlib.sha256()
     files = _sources() + sorted(glob.glob(os.path.join(CSRC, "*.cuh")) +
@@ -64,7 +99,8 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-        cmd = [cc, *ARCH, *NVCC_FLAGS, *extra_flags, "-c", src, "-o", obj]
+        cmd = [cc, *ARCH, *NVCC_FLAGS, f'-DQG_CUDA_LIB_DIR="{_cuda_lib_dir()}"', *extra_flags, "-c", src,
+               "-o", obj]
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -74,11 +110,11 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
             print(r.stderr)
         return obj
 
-    srcs = _sources()
+    srcs = _sources() + [_write_jit_headers()]
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + f".tmp{os.getpid()}"
-    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
+    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -2,7 +2,9 @@
 // fused pass kernels (fused.cu).  All structs are plain data copied verbatim
 // to device memory.
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <stdint.h>
+#endif
 
 namespace qg {
 
@@ -14,6 +16,17 @@ constexpr int kBwdRegBits = 4;
 // backward: gradient slots per pass (their partials live in shared memory
 // beside the psi/lambda double buffer, 5 B per slot and thread)
 __host__ __device__ constexpr int max_grad_per_pass(int reg_bits) { return reg_bits == 4 ? 64 : 96; }
+
+// Tile buffers of the forward kernel: three (two loads in flight while one
+// tile computes), four for 2^11 tiles.  Two 2^12 CTAs with three buffers
+// each still fit one SM's shared memory.
+__host__ __device__ constexpr int fwd_stages(int tb) { return tb >= 12 ? 3 : 4; }
+
+// Resident CTAs per SM the register budget allows: 32 amplitudes per thread
+// (RB = 5) take up to 255 registers, 16 (RB = 4) up to 128.
+__host__ __device__ constexpr int fwd_min_blocks(int tb, int rb) {
+    return 65536 / ((1 << (tb - rb)) * (rb == 5 ? 256 : 128));
+}
 
 // Device op codes (int4 per op: x = opcode, y/z/w operands).
 enum Opcode : int32_t {
@@ -103,6 +116,13 @@ struct RunArgs {
 constexpr int kSmemOps = 512;
 constexpr int kSmemMats = 256;
 
+// Dynamic shared memory of the forward kernel: the tile ring, the op list and
+// the shared matrix table.
+__host__ __device__ constexpr int fwd_smem_bytes(int tb) {
+    return fwd_stages(tb) * (1 << tb) * 8 + kSmemOps * 16 + kSmemMats * 32;
+}
+
+#ifndef __CUDACC_RTC__
 // Host view of a planned program, for the launch code in fused.cu.
 struct ProgramRun {
     int n, tile_bits, reg_bits, measure, keep_state, segments;
@@ -111,9 +131,13 @@ struct ProgramRun {
     int nfpass, nbpass;
     const PassDesc* fpass;  // host copies
     const PassDesc* bpass;
+    const int32_t* fops;    // host op lists (int4 per op)
+    const int32_t* bops;
     size_t off_fpass, off_fops, off_fslot, off_fchain;
     size_t off_bpass, off_bops, off_bslot, off_bchain, off_embed, off_pcsr, off_ccsr;
 };
 void program_run_info(const void* prog, ProgramRun* out);
+#endif
+
 
 }  // namespace qg

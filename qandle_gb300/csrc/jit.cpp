@@ -1,0 +1,435 @@
+// Run-time compiled forward pass kernels.
+//
+// The op interpreter of the prebuilt forward kernel decodes every op of a
+// pass at run time: a register position becomes a switch, a CNOT between two
+// register qubits becomes register moves, and the code of every op variant
+// competes for the instruction cache.  For one program the op lists are
+// fixed, so this file writes each forward pass out as CUDA source -- the
+// shared kernel body of fwd_kernel.cuh with the pass's ops unrolled as calls
+// to jit_ops.cuh with compile-time register positions -- and compiles it for
+// sm_103a with NVRTC.  Matrices, angles and states stay run-time data, so one
+// compiled program serves every call with any batch and any parameters.
+//
+// NVRTC is opened with dlopen: without it qg_program_compile reports an
+// error and forward passes keep running on the prebuilt interpreter.  Module
+// loading and launches go through driver entry points obtained from the CUDA
+// runtime (no link-time libcuda dependency).  Compiled modules are cached
+// process-wide by (device, source text), so rebuilding an identical program
+// compiles nothing.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "common.cuh"
+#include "engine.h"
+#include "jit.h"
+#include "qandle_gb300.h"
+
+namespace qg {
+
+void program_run_info(const void* prog, ProgramRun* r);
+void* program_jit_state(const void* prog);
+void program_set_jit_state(void* prog, void* state);
+
+// headers handed to NVRTC (generated from csrc/ by build.py)
+extern const int kJitHeaderCount;
+extern const char* const kJitHeaderNames[];
+extern const char* const kJitHeaderTexts[];
+
+namespace {
+
+// ------------------------------------------------------------ NVRTC --
+
+struct Nvrtc {
+    decltype(&nvrtcCreateProgram) create = nullptr;
+    decltype(&nvrtcCompileProgram) compile = nullptr;
+    decltype(&nvrtcGetProgramLogSize) log_size = nullptr;
+    decltype(&nvrtcGetProgramLog) log = nullptr;
+    decltype(&nvrtcGetCUBINSize) cubin_size = nullptr;
+    decltype(&nvrtcGetCUBIN) cubin = nullptr;
+    decltype(&nvrtcDestroyProgram) destroy = nullptr;
+    decltype(&nvrtcGetErrorString) error_string = nullptr;
+    std::string why;  // empty when loaded
+};
+
+#ifndef QG_CUDA_LIB_DIR
+#define QG_CUDA_LIB_DIR "/usr/local/cuda/lib64"
+#endif
+
+const Nvrtc& nvrtc() {
+    static Nvrtc N;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const char* names[] = {"libnvrtc.so.13", QG_CUDA_LIB_DIR "/libnvrtc.so.13", "libnvrtc.so",
+                               QG_CUDA_LIB_DIR "/libnvrtc.so"};
+        void* h = nullptr;
+        for (const char* nm : names)
+            if ((h = dlopen(nm, RTLD_NOW | RTLD_LOCAL))) break;
+        if (!h) {
+            N.why = "libnvrtc.so.13 not found";
+            return;
+        }
+#define QG_SYM(field, name)                                          \
+    N.field = reinterpret_cast<decltype(N.field)>(dlsym(h, #name)); \
+    if (!N.field) {                                                  \
+        N.why = "libnvrtc lacks " #name;                             \
+        return;                                                      \
+    }
+        QG_SYM(create, nvrtcCreateProgram)
+        QG_SYM(compile, nvrtcCompileProgram)
+        QG_SYM(log_size, nvrtcGetProgramLogSize)
+        QG_SYM(log, nvrtcGetProgramLog)
+        QG_SYM(cubin_size, nvrtcGetCUBINSize)
+        QG_SYM(cubin, nvrtcGetCUBIN)
+        QG_SYM(destroy, nvrtcDestroyProgram)
+        QG_SYM(error_string, nvrtcGetErrorString)
+#undef QG_SYM
+    });
+    return N;
+}
+
+// ----------------------------------------------------------- driver --
+
+struct Driver {
+    decltype(&cuModuleLoadData) load = nullptr;
+    decltype(&cuModuleGetFunction) get_function = nullptr;
+    decltype(&cuFuncSetAttribute) set_attribute = nullptr;
+    decltype(&cuLaunchKernel) launch = nullptr;
+    decltype(&cuOccupancyMaxActiveBlocksPerMultiprocessor) occupancy = nullptr;
+    decltype(&cuGetErrorString) error_string = nullptr;
+    std::string why;
+};
+
+const Driver& driver() {
+    static Driver D;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFree(nullptr);  // the runtime's primary context is current from here on
+#define QG_DRV(field, name)                                                                     \
+    {                                                                                           \
+        void* fp = nullptr;                                                                     \
+        cudaDriverEntryPointQueryResult q{};                                                    \
+        if (cudaGetDriverEntryPointByVersion(#name, &fp, 12000, cudaEnableDefault, &q) !=       \
+                cudaSuccess ||                                                                  \
+            !fp) {                                                                              \
+            D.why = "driver entry point " #name " unavailable";                               \
+            return;                                                                             \
+        }                                                                                       \
+        D.field = reinterpret_cast<decltype(D.field)>(fp);                                      \
+    }
+        QG_DRV(load, cuModuleLoadData)
+        QG_DRV(get_function, cuModuleGetFunction)
+        QG_DRV(set_attribute, cuFuncSetAttribute)
+        QG_DRV(launch, cuLaunchKernel)
+        QG_DRV(occupancy, cuOccupancyMaxActiveBlocksPerMultiprocessor)
+        QG_DRV(error_string, cuGetErrorString)
+#undef QG_DRV
+    });
+    return D;
+}
+
+std::string cu_error(CUresult r) {
+    const char* s = nullptr;
+    if (driver().error_string) driver().error_string(r, &s);
+    return s ? std::string(s) : ("CUresult " + std::to_string((int)r));
+}
+
+// ------------------------------------------------------ code writer --
+
+std::string loc_bit(int32_t loc) { return "loc_bit_thread(" + std::to_string(loc) + ", tm.tglob)"; }
+
+// One forward pass as CUDA source: the shared kernel body with the pass's
+// gate program unrolled.
+std::string pass_source(const ProgramRun& R, int p) {
+    const PassDesc& d = R.fpass[p];
+    const int tb = d.tile_bits, rb = R.reg_bits;  // the launch uses the same pair
+    const int nt = 1 << (tb - rb);
+    std::ostringstream s;
+    s << "#include \"jit_ops.cuh\"\n"
+         "namespace qg {\n"
+         "struct PassOps {\n"
+         "  template <int TB, int RB>\n"
+         "  __device__ __forceinline__ static void apply(PTile<RB>& pt, uint32_t& xm, ThreadMap& tm, "
+         "const PassDesc& d, const RunArgs& A, const int4*, const int4*, const float4* s_mats, float* plane, "
+         "int64_t sample0, uint32_t fixed_val, int tid) {\n";
+    const int32_t* ops = R.fops + 4 * (size_t)d.op_begin;
+    for (int o = 0; o < d.op_count; ++o) {
+        const int32_t k = ops[4 * o], y = ops[4 * o + 1], z = ops[4 * o + 2], w = ops[4 * o + 3];
+        const std::string smp = "sample0 + tm.sample_off";
+        s << "    ";
+        switch (k) {
+            case OP_MAP:
+                s << "exchange<TB, RB>(pt, xm, tm, plane, d, " << y << ", " << z << ", " << w
+                  << ", tid, fixed_val);\n";
+                break;
+            case OP_MAT:
+                s << "jmat<" << y << ", RB>(pt, xm, A, s_mats, " << z << ", " << w << ", " << smp << ");\n";
+                break;
+            case OP_DIAG:
+                if (y & LOC_REG)
+                    s << "jdiag<" << (y & 7) << ", RB>(pt, xm, A, s_mats, " << z << ", " << w << ", " << smp
+                      << ");\n";
+                else
+                    s << "jdiag_thread<RB>(pt, " << loc_bit(y) << ", A, s_mats, " << z << ", " << w << ", " << smp
+                      << ");\n";
+                break;
+            case OP_CX:
+                if (z & LOC_REG)
+                    s << "jcx<" << y << ", " << (z & 7) << ", RB>(pt, xm);\n";
+                else
+                    s << "xm ^= (uint32_t)" << loc_bit(z) << " << " << y << ";\n";
+                break;
+            case OP_CZ: {
+                int mask = 0;
+                std::string cond;
+                for (int32_t loc : {y, z}) {
+                    if (loc & LOC_REG) {
+                        s << "jmaterialize<" << (loc & 7) << ", RB>(pt, xm); ";
+                        mask |= 1 << (loc & 7);
+                    } else {
+                        cond += (cond.empty() ? "" : " && ") + loc_bit(loc);
+                    }
+                }
+                if (cond.empty())
+                    s << "pnegate<" << mask << ", RB>(pt);\n";
+                else
+                    s << "jnegate_if<" << mask << ", RB>(pt, " << cond << ");\n";
+                break;
+            }
+            case OP_SWAP:
+                if (y != z) s << "jswap<" << y << ", " << z << ", RB>(pt, xm);\n";
+                else s << "\n";
+                break;
+            default:
+                s << "// op " << k << " has no forward form\n";
+                break;
+        }
+    }
+    s << "  }\n};\n}  // namespace qg\n"
+      << "extern \"C\" __global__ void __launch_bounds__(" << nt << ", " << fwd_min_blocks(tb, rb) << ")\n"
+      << "qg_fwd_pass(const __grid_constant__ qg::JobTable<1> jt) {\n"
+      << "  qg::fwd_pass_body<" << tb << ", " << rb << ", 1, qg::PassOps>(jt);\n}\n";
+    return s.str();
+}
+
+// ------------------------------------------------- compile and cache --
+
+struct Loaded {
+    CUmodule mod = nullptr;
+    JitKernel k;
+};
+
+std::mutex g_cache_mu;
+std::map<std::pair<int, std::string>, Loaded> g_cache;  // (device, source) -> module
+
+int compile_source(const std::string& src, std::vector<char>& cubin, std::string& err) {
+    const Nvrtc& N = nvrtc();
+    nvrtcProgram prog = nullptr;
+    nvrtcResult r = N.create(&prog, src.c_str(), "qg_pass.cu", kJitHeaderCount, kJitHeaderTexts, kJitHeaderNames);
+    if (r != NVRTC_SUCCESS) {
+        err = std::string("nvrtcCreateProgram: ") + N.error_string(r);
+        return QG_ECUDA;
+    }
+    const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo",
+                          "-DQG_RTC=1"};
+    r = N.compile(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+    if (r != NVRTC_SUCCESS) {
+        size_t n = 0;
+        N.log_size(prog, &n);
+        std::string log(n, '\0');
+        if (n) N.log(prog, &log[0]);
+        err = std::string("nvrtcCompileProgram: ") + N.error_string(r) + "\n" + log.substr(0, 4000);
+        N.destroy(&prog);
+        return QG_ECUDA;
+    }
+    size_t n = 0;
+    N.cubin_size(prog, &n);
+    cubin.resize(n);
+    N.cubin(prog, cubin.data());
+    N.destroy(&prog);
+    return QG_OK;
+}
+
+int load_cubin(const std::vector<char>& cubin, int tb, int rb, Loaded& out, std::string& err) {
+    const Driver& D = driver();
+    CUresult r = D.load(&out.mod, cubin.data());
+    if (r != CUDA_SUCCESS) {
+        err = "cuModuleLoadData: " + cu_error(r);
+        return QG_ECUDA;
+    }
+    CUfunction f = nullptr;
+    r = D.get_function(&f, out.mod, "qg_fwd_pass");
+    if (r != CUDA_SUCCESS) {
+        err = "cuModuleGetFunction: " + cu_error(r);
+        return QG_ECUDA;
+    }
+    const int smem = fwd_smem_bytes(tb);
+    r = D.set_attribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, smem);
+    if (r != CUDA_SUCCESS) {
+        err = "cuFuncSetAttribute: " + cu_error(r);
+        return QG_ECUDA;
+    }
+    int per_sm = 0;
+    r = D.occupancy(&per_sm, f, 1 << (tb - rb), (size_t)smem);
+    if (r != CUDA_SUCCESS) {
+        err = "cuOccupancyMaxActiveBlocksPerMultiprocessor: " + cu_error(r);
+        return QG_ECUDA;
+    }
+    out.k.fn = (void*)f;
+    out.k.per_sm = per_sm < 1 ? 1 : per_sm;
+    return QG_OK;
+}
+
+// Per-program state: the compiled kernel of every forward pass, per device.
+struct ProgramJit {
+    std::mutex mu;
+    std::map<int, std::vector<JitKernel>> fwd;  // device -> kernel per pass
+};
+
+}  // namespace
+
+bool jit_forward_kernel(const void* prog, int pass, JitKernel* out) {
+    ProgramJit* st = (ProgramJit*)program_jit_state(prog);
+    if (!st) return false;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    std::lock_guard<std::mutex> lk(st->mu);
+    auto it = st->fwd.find(dev);
+    if (it == st->fwd.end() || pass < 0 || pass >= (int)it->second.size()) return false;
+    *out = it->second[pass];
+    return out->fn != nullptr;
+}
+
+int jit_launch(const JitKernel& k, unsigned grid, unsigned block, size_t smem, void* stream, void** params) {
+    CUresult r = driver().launch((CUfunction)k.fn, grid, 1, 1, block, 1, 1, (unsigned)smem, (CUstream)stream,
+                                 params, nullptr);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuLaunchKernel: " + cu_error(r));
+        return QG_ECUDA;
+    }
+    return QG_OK;
+}
+
+void jit_release(void* state) { delete (ProgramJit*)state; }
+
+}  // namespace qg
+
+extern "C" {
+
+int qg_program_compile(qg_program* prog, int flags) {
+    using namespace qg;
+    if (!prog) return set_error("qg_program_compile: null pointer"), QG_EINVAL;
+    const bool load = !(flags & QG_COMPILE_NO_LOAD);
+    const Nvrtc& N = nvrtc();
+    if (!N.why.empty()) return set_error("qg_program_compile: " + N.why), QG_ECUDA;
+    int dev = -1;
+    if (load) {
+        const Driver& D = driver();
+        if (!D.why.empty()) return set_error("qg_program_compile: " + D.why), QG_ECUDA;
+        QG_CUDA_TRY(cudaGetDevice(&dev));
+    }
+    ProgramRun R;
+    program_run_info(prog, &R);
+    if (R.reg_bits != 4 && R.reg_bits != 5)
+        return set_error("qg_program_compile: reg_bits must be 4 or 5"), QG_EINVAL;
+
+    std::vector<std::string> srcs(R.nfpass);
+    for (int p = 0; p < R.nfpass; ++p) srcs[p] = pass_source(R, p);
+
+    // passes not yet in the process-wide cache compile in parallel
+    std::vector<JitKernel> kernels(R.nfpass);
+    std::vector<int> todo;
+    {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        for (int p = 0; p < R.nfpass; ++p) {
+            auto it = g_cache.find({dev, srcs[p]});
+            if (it != g_cache.end())
+                kernels[p] = it->second.k;
+            else
+                todo.push_back(p);
+        }
+    }
+    std::vector<std::vector<char>> cubins(todo.size());
+    std::vector<std::string> errs(todo.size());
+    std::vector<int> rcs(todo.size(), QG_OK);
+    {
+        unsigned hw = std::thread::hardware_concurrency();
+        size_t nthreads = std::min<size_t>(todo.size(), hw ? hw : 4);
+        std::vector<std::thread> pool;
+        std::mutex qmu;
+        size_t next = 0;
+        for (size_t t = 0; t < nthreads; ++t)
+            pool.emplace_back([&] {
+                for (;;) {
+                    size_t i;
+                    {
+                        std::lock_guard<std::mutex> lk(qmu);
+                        if (next >= todo.size()) return;
+                        i = next++;
+                    }
+                    rcs[i] = compile_source(srcs[todo[i]], cubins[i], errs[i]);
+                }
+            });
+        for (auto& th : pool) th.join();
+    }
+    for (size_t i = 0; i < todo.size(); ++i)
+        if (rcs[i]) return set_error("qg_program_compile: pass " + std::to_string(todo[i]) + ": " + errs[i]), rcs[i];
+    if (!load) return QG_OK;
+    {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        for (size_t i = 0; i < todo.size(); ++i) {
+            const int p = todo[i];
+            auto it = g_cache.find({dev, srcs[p]});
+            if (it == g_cache.end()) {
+                Loaded L;
+                std::string err;
+                int rc = load_cubin(cubins[i], R.fpass[p].tile_bits, R.reg_bits, L, err);
+                if (rc) return set_error("qg_program_compile: pass " + std::to_string(p) + ": " + err), rc;
+                it = g_cache.emplace(std::make_pair(dev, srcs[p]), L).first;
+            }
+            kernels[p] = it->second.k;
+        }
+    }
+    ProgramJit* st;
+    {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        st = (ProgramJit*)program_jit_state(prog);
+        if (!st) {
+            st = new ProgramJit();
+            program_set_jit_state(prog, st);
+        }
+    }
+    std::lock_guard<std::mutex> lk(st->mu);
+    st->fwd[dev] = kernels;
+    return QG_OK;
+}
+
+int64_t qg_program_pass_source(const qg_program* prog, int pass, char* host_out, int64_t bytes) {
+    using namespace qg;
+    if (!prog) return -1;
+    ProgramRun R;
+    program_run_info(prog, &R);
+    if (pass < 0 || pass >= R.nfpass) return -1;
+    const std::string src = pass_source(R, pass);
+    const int64_t need = (int64_t)src.size() + 1;
+    if (host_out && bytes >= need) memcpy(host_out, src.c_str(), (size_t)need);
+    return need;
+}
+
+int qg_program_compiled(const qg_program* prog) {
+    qg::JitKernel k;
+    return prog && qg::jit_forward_kernel(prog, 0, &k) ? 1 : 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,89 @@
+// Gate ops with compile-time register positions, called by the pass kernels
+// that jit.cpp generates for one program and compiles with NVRTC.
+//
+// The op interpreter (fused.cu) dispatches every op on its runtime register
+// position; here the position is a template argument, so a CNOT or SWAP
+// between register qubits is a renaming of registers that costs no
+// instruction, and consecutive gates on different qubits interleave freely.
+//
+// Pending X (planar.cuh): physical register r holds logical amplitude
+// r ^ xm.  The rules below keep xm exact without moving data:
+//   CX(c -> p), both in registers: apply the physical CX and set
+//     xm_p ^= xm_c  (X_c CX X_c = X_p CX);
+//   SWAP(a, b): apply the physical SWAP and swap bits a and b of xm;
+//   a matrix on bit p with xm_p set acts as X M X (rows and columns reversed).
+#pragma once
+#include "fwd_kernel.cuh"
+
+namespace qg {
+
+// X M X of a row-form 2x2 where c holds, else M.
+__device__ __forceinline__ void xmx_if(float2 m[4], bool c) {
+    const float2 a = m[0], b = m[1], e = m[2], f = m[3];
+    m[0] = c ? f : a;
+    m[1] = c ? e : b;
+    m[2] = c ? b : e;
+    m[3] = c ? a : f;
+}
+
+template <int P, int RB>
+__device__ __forceinline__ void jmat(PTile<RB>& pt, uint32_t xm, const RunArgs& A, const float4* s_mats, int slot,
+                                     int flags, int64_t sample) {
+    float2 m[4];
+    load_slot(A, s_mats, slot, flags, sample, m);
+    xmx_if(m, (xm >> P) & 1u);
+    pmat<P, RB>(pt, m);
+}
+
+template <int P, int RB>
+__device__ __forceinline__ void jdiag(PTile<RB>& pt, uint32_t xm, const RunArgs& A, const float4* s_mats, int slot,
+                                      int flags, int64_t sample) {
+    float2 m[4];
+    load_slot(A, s_mats, slot, flags, sample, m);
+    const bool sw = (xm >> P) & 1u;
+    pdiag<P, RB>(pt, sw ? m[3] : m[0], sw ? m[0] : m[3]);
+}
+
+// Diagonal on a thread-uniform bit: one complex factor for the whole thread.
+template <int RB>
+__device__ __forceinline__ void jdiag_thread(PTile<RB>& pt, bool bit, const RunArgs& A, const float4* s_mats,
+                                             int slot, int flags, int64_t sample) {
+    float2 m[4];
+    load_slot(A, s_mats, slot, flags, sample, m);
+    pscale<RB>(pt, bit ? m[3] : m[0]);
+}
+
+template <int P, int C, int RB>
+__device__ __forceinline__ void jcx(PTile<RB>& pt, uint32_t& xm) {
+    pcx<P, C, RB>(pt);
+    xm ^= ((xm >> C) & 1u) << P;
+}
+
+template <int P0, int P1, int RB>
+__device__ __forceinline__ void jswap(PTile<RB>& pt, uint32_t& xm) {
+    pswapbits<P0, P1, RB>(pt);
+    const uint32_t d = ((xm >> P0) ^ (xm >> P1)) & 1u;
+    xm ^= d * ((1u << P0) | (1u << P1));
+}
+
+// Apply the pending X of register bit P and clear it.
+template <int P, int RB>
+__device__ __forceinline__ void jmaterialize(PTile<RB>& pt, uint32_t& xm) {
+    pswap_if<P, RB>(pt, (xm >> P) & 1u);
+    xm &= ~(1u << P);
+}
+
+// Negate the amplitudes whose register bits in Mask are all 1, where c holds
+// (a per-thread condition: a sign multiply instead of a divergent branch).
+template <int Mask, int RB>
+__device__ __forceinline__ void jnegate_if(PTile<RB>& pt, bool c) {
+    const float s = c ? -1.f : 1.f;
+#pragma unroll
+    for (int r = 0; r < (1 << RB); ++r) {
+        if ((r & Mask) != Mask) continue;
+        const float2 a = get_amp<RB>(pt, r);
+        set_amp<RB>(pt, r, make_float2(a.x * s, a.y * s));
+    }
+}
+
+}  // namespace qg

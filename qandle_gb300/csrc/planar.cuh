@@ -15,9 +15,7 @@
 // X M X, and the next exchange or store writes every register to the slot of
 // its logical index, which costs one XOR per thread.
 #pragma once
-#include <type_traits>
-
-#include "common.cuh"
+#include "devmath.cuh"
 
 namespace qg {
 

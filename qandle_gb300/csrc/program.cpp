@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include "engine.h"
+#include "jit.h"
 #include "qandle_gb300.h"
 
 namespace qg {
@@ -297,6 +298,7 @@ struct Program {
     std::vector<unsigned char> table;
     int f_shared = 0, f_ps = 0, b_shared = 0, b_ps = 0;
     std::string stats;
+    void* jit = nullptr;  // compiled pass kernels (jit.cpp), owned by the program
 };
 
 namespace {
@@ -868,6 +870,8 @@ void program_run_info(const void* prog, ProgramRun* r) {
     r->nbpass = (int)P.bpass.size();
     r->fpass = P.fpass.data();
     r->bpass = P.bpass.data();
+    r->fops = P.fops.data();
+    r->bops = P.bops.data();
     r->off_fpass = P.off_fpass;
     r->off_fops = P.off_fops;
     r->off_fslot = P.off_fslot;
@@ -880,6 +884,9 @@ void program_run_info(const void* prog, ProgramRun* r) {
     r->off_pcsr = P.off_pcsr;
     r->off_ccsr = P.off_ccsr;
 }
+
+void* program_jit_state(const void* prog) { return reinterpret_cast<const Program*>(prog)->jit; }
+void program_set_jit_state(void* prog, void* state) { reinterpret_cast<Program*>(prog)->jit = state; }
 
 }  // namespace qg
 
@@ -932,7 +939,12 @@ int qg_program_create(const qg_gate* gates, int ngates, const int32_t* qlist, in
     return QG_OK;
 }
 
-void qg_program_destroy(qg_program* p) { delete reinterpret_cast<Program*>(p); }
+void qg_program_destroy(qg_program* p) {
+    if (!p) return;
+    Program* P = reinterpret_cast<Program*>(p);
+    qg::jit_release(P->jit);
+    delete P;
+}
 
 int qg_program_info(const qg_program* p, qg_program_info_t* info) {
     if (!p || !info) return qg::set_error("null pointer"), QG_EINVAL;

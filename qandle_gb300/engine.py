@@ -13,6 +13,7 @@ fallback.
 from __future__ import annotations
 
 import ctypes
+import os
 import threading
 
 import numpy as np
@@ -126,6 +127,7 @@ class Program:
         _lib.check(lib.qg_program_table(self.handle, host, self.info.table_bytes))
         self._table_host = torch.frombuffer(bytearray(host), dtype=torch.uint8)
         self._tables = {}
+        self._compiled = set()
         self._lock = threading.Lock()
 
     def __del__(self):
@@ -135,6 +137,41 @@ class Program:
                 _lib.load().qg_program_destroy(h)
             except Exception:
                 pass
+
+    def pass_source(self, p: int) -> str:
+        """CUDA source of compiled forward pass p (the pass's ops unrolled)."""
+        lib = _lib.load()
+        size = lib.qg_program_pass_source(self.handle, p, None, 0)
+        if size < 0:
+            raise IndexError(f"no forward pass {p}")
+        buf = ctypes.create_string_buffer(size)
+        lib.qg_program_pass_source(self.handle, p, buf, size)
+        return buf.value.decode()
+
+    def compile(self, device=None, load: bool = True) -> None:
+        """Compile the forward passes into per-pass kernels (NVRTC) for
+        ``device``; with ``load=False`` only check that they build (no GPU
+        needed).  Raises RuntimeError with the compiler's log on failure."""
+        lib = _lib.load()
+        flags = 0 if load else 1
+        if load:
+            with torch.cuda.device(device):
+                _lib.check(lib.qg_program_compile(self.handle, flags))
+        else:
+            _lib.check(lib.qg_program_compile(self.handle, flags))
+
+    def compiled(self, device) -> bool:
+        with torch.cuda.device(device):
+            return bool(_lib.load().qg_program_compiled(self.handle))
+
+    def ensure_compiled(self, device) -> None:
+        key = str(device)
+        if key in self._compiled:
+            return
+        with self._lock:
+            if key not in self._compiled:
+                self.compile(device)
+                self._compiled.add(key)
 
     def table(self, device) -> torch.Tensor:
         key = str(device)
@@ -259,8 +296,14 @@ class FusedExecutor:
     """Runs a built circuit through the fused engine (used by Circuit)."""
 
     def __init__(self, circuit, tile_bits: int = 13, low_bits: int = 6, max_high: int = 0,
-                 checkpoint_segments: int = 1, reg_bits: int = 5):
+                 checkpoint_segments: int = 1, reg_bits: int = 5, compiled: bool = None):
         self.circuit = circuit
+        # compiled = True: forward passes run as per-program kernels compiled
+        # at first use (NVRTC); False: the prebuilt op interpreter.  The
+        # default follows QG_COMPILE (on unless set to 0).
+        if compiled is None:
+            compiled = os.environ.get("QG_COMPILE", "1") != "0"
+        self.compiled = bool(compiled)
         self.n = circuit.num_qubits
         self.lowered = lower(circuit)
         self.options = dict(tile_bits=tile_bits, low_bits=low_bits, max_high=max_high, reg_bits=reg_bits)
@@ -328,6 +371,8 @@ class FusedExecutor:
         if prog.info.segments > 1:
             ckpt = torch.empty(prog.info.segments - 1, B, 1 << n, dtype=torch.complex64, device=dev)
         ws = prog.workspace(B, False, dev)
+        if self.compiled:
+            prog.ensure_compiled(dev)
         _lib.call("qg_program_forward", prog.handle, prog.table(dev).data_ptr(), ws.data_ptr(), ws.numel(),
                   st.data_ptr(), B, zero_init, params.data_ptr(), named.data_ptr(), umats.data_ptr(),
                   _lib.ptr(out), _lib.ptr(ckpt), _lib.stream())
@@ -413,6 +458,8 @@ class BoundForward:
         self.table = self.prog.table(device)
         self.zero_init = 0 if (has_state or info.has_embedding) else 1
         self.graph = None
+        if ex.compiled:
+            self.prog.ensure_compiled(self.device)
 
     def set_inputs(self, state=None, **kwargs) -> None:
         with torch.no_grad():

@@ -56,16 +56,37 @@ OPTS = [dict(), dict(tile_bits=12, low_bits=4, max_high=2), dict(tile_bits=11, l
         dict(tile_bits=13, low_bits=7, max_high=6), dict(reg_bits=4), dict(tile_bits=12, reg_bits=4)]
 
 
+@pytest.mark.parametrize("compiled", [True, False], ids=["compiled", "interpreted"])
 @pytest.mark.parametrize("case", sorted(CASES))
 @pytest.mark.parametrize("oi", range(len(OPTS)))
-def test_fused_forward_vs_oracle(cuda_device, case, oi):
+def test_fused_forward_vs_oracle(cuda_device, case, oi, compiled):
     desc = CASES[case]()
-    out = _run(desc, cuda_device, **OPTS[oi])
+    out = _run(desc, cuda_device, compiled=compiled, **OPTS[oi])
     ref = oracle.forward(desc)
     if out.shape == ref.shape[1:]:
         ref = ref[0]  # no per-sample input: the front end runs the unbatched |0..0> state
     err = np.abs(out - ref).max()
     assert err < TOL, (case, OPTS[oi], err)
+
+
+def test_compiled_kernels_run(cuda_device):
+    """The default forward runs the per-program compiled pass kernels."""
+    desc = workloads.sel_reupload(n=14, batch=3, layers=2, reupload_every=2)
+    circ = workloads.build_circuit(desc, engine="fused").to(cuda_device)
+    with torch.no_grad():
+        circ(**workloads.circuit_inputs(desc, cuda_device))
+    assert circ._executor.compiled
+    assert circ._executor.program(False).compiled(cuda_device)
+
+
+@pytest.mark.parametrize("reg_bits", [5, 4])
+def test_headline_circuit_full_width(cuda_device, reg_bits):
+    """The benchmark circuit itself (20 qubits, 10 SEL layers, re-uploads,
+    <Z>) at batch 2, compiled, against the oracle."""
+    desc = workloads.sel_reupload(n=20, batch=2)
+    out = _run(desc, cuda_device, reg_bits=reg_bits)
+    ref = oracle.forward(desc)
+    assert np.abs(out - ref).max() < TOL
 
 
 @pytest.mark.parametrize("measure", ["state", "probs", "p0", "z"])
