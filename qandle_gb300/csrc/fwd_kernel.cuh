@@ -155,6 +155,55 @@ __device__ void issue_tile_store(const PassDesc& d, const TileGeo& g, float2* ds
         bulk_s2g(dstg + g.base + run_offset(d, r), src + ((int64_t)r << d.run_bits), rb);
 }
 
+// Per-thread async copies (cp.async, 16 bytes = 2 amplitudes each) of one
+// tile's state image into dst in local-index order.  Every thread of the CTA
+// issues 2^(RB-1) copies; thread tid copies chunks tid, tid + NT, ..., so a
+// warp covers 512 contiguous bytes of a run.  Unlike one engine working
+// through a tile's runs (bulk copies), the load/store units of all warps keep
+// many small copies in flight, which scattered 512-byte runs need.  Local
+// bit 0 is global bit 0 (runs are at least 2 amplitudes), so a chunk is
+// contiguous; higher local bits add their global strides.  The caller
+// commits the copies as one group.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+template <int TB, int RB>
+__device__ __forceinline__ void thread_tile_load(const PassDesc& d, const TileGeo& g, const float2* src,
+                                                 float2* dst, int n, int tid) {
+    constexpr int NT = 1 << (TB - RB);
+    constexpr int PER = 1 << (RB - 1);  // chunks per thread
+    const float2* base = src + g.base;
+    if (n < TB) {  // whole samples: the tile image is contiguous
+        const int lim = (int)(((int64_t)g.nsamples << n) >> 1);
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+            const int c = tid + i * NT;
+            if (c < lim) cp_async16(dst + 2 * c, base + 2 * c);
+        }
+        return;
+    }
+    uint32_t thr = 0;
+#pragma unroll
+    for (int k = 0; k < TB - RB; ++k) thr |= (uint32_t)((tid >> k) & 1) << d.gbit[1 + k];
+    uint32_t st[RB - 1];
+#pragma unroll
+    for (int k = 0; k < RB - 1; ++k) st[k] = 1u << d.gbit[TB - RB + 1 + k];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        uint32_t off = thr;
+#pragma unroll
+        for (int k = 0; k < RB - 1; ++k)
+            if ((i >> k) & 1) off ^= st[k];
+        cp_async16(dst + 2 * (tid + i * NT), base + off);
+    }
+}
+
 // float (probability) image of a tile: half the bytes of the state image
 __device__ void issue_tile_store_f32(const PassDesc& d, const TileGeo& g, float* dstg, const float* src, int n,
                                      int lane) {
@@ -295,6 +344,44 @@ __device__ __forceinline__ void pstore_probs(const PTile<RB>& t, float* pb, int 
     }
 }
 
+// Store a tile in the natural mapping straight from registers to global
+// memory.  The lanes hold 32 consecutive amplitudes of a run, so a warp
+// store covers 256 contiguous bytes whenever the lanes share their pending
+// X; no shared-memory staging, so the tile's buffer is free at once.
+// Physical register r holds logical amplitude r ^ xm.  Local bits map to
+// distinct global bits, so offsets of the register part combine by XOR.
+template <int RB>
+__device__ __forceinline__ void pstore_global(const PTile<RB>& t, uint32_t xm, const PassDesc& d,
+                                              const TileGeo& g, float2* dst, int n, int tid) {
+    float2* base = dst + g.base;
+    if (n < d.tile_bits) {  // whole samples: the tile image is contiguous
+        const int64_t lim = (int64_t)g.nsamples << n;
+#pragma unroll
+        for (int r = 0; r < (1 << RB); ++r) {
+            const int j = nat_index<RB>(r ^ (int)xm, tid);
+            if (j < lim) base[j] = get_amp<RB>(t, r);
+        }
+        return;
+    }
+    uint32_t rs[RB];
+#pragma unroll
+    for (int k = 0; k < RB; ++k) rs[k] = 1u << d.gbit[5 + k];
+    uint32_t c = 0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) c |= (uint32_t)((tid >> k) & 1) << d.gbit[k];
+    for (int k = 0; k < d.tile_bits - 5 - RB; ++k) c |= (uint32_t)((tid >> (5 + k)) & 1) << d.gbit[5 + RB + k];
+#pragma unroll
+    for (int k = 0; k < RB; ++k) c ^= ((xm >> k) & 1u) ? rs[k] : 0u;
+    uint32_t off[1 << RB];
+    off[0] = c;
+#pragma unroll
+    for (int k = 0; k < RB; ++k)
+#pragma unroll
+        for (int r = 0; r < (1 << k); ++r) off[r + (1 << k)] = off[r] ^ rs[k];
+#pragma unroll
+    for (int r = 0; r < (1 << RB); ++r) base[off[r]] = get_amp<RB>(t, r);
+}
+
 // Exchange through planar shared memory (re plane, im plane), folding the
 // pending X of the thread into the write addresses.
 template <int RB, int K = 0>
@@ -376,44 +463,35 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
     float2* bufs = reinterpret_cast<float2*>(smem_raw);
     int4* s_ops = reinterpret_cast<int4*>(bufs + S * AMPS);         // [kSmemOps]
     float4* s_mats = reinterpret_cast<float4*>(s_ops + kSmemOps);   // [kSmemMats][2]
-    __shared__ __align__(8) uint64_t bars[S];
     __shared__ PassDesc sd;
     __shared__ RunArgs sa;
 
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int64_t total = jt.begin[jt.njobs];
-    if (tid == 0) {
-        for (int i = 0; i < S; ++i) mbar_init(&bars[i], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
 
-    // loads completed per buffer: a buffer's mbarrier completes once per load
-    uint32_t phase[S];
-#pragma unroll
-    for (int i = 0; i < S; ++i) phase[i] = 0u;
     auto tile_loads = [&](int j) -> bool {
         return jt.job[j].pd->init == INIT_LOAD && !jt.job[j].zero_init;
     };
-    auto issue_prefetch = [&](int64_t t, float2* dst, uint64_t* bar) {
-        // warp 0 only
-        int j = find_job(jt, t);
-        const PassDesc& pd = *jt.job[j].pd;
-        const RunArgs& ra = jt.job[j].A;
-        TileGeo gn = tile_geo(pd, t - jt.begin[j], ra.n, ra.batch);
-        if (lane == 0) mbar_expect_tx(bar, tile_bytes(pd, gn, ra.n));
-        __syncwarp();
-        issue_tile_load(pd, gn, ra.state, dst, bar, ra.n, lane);
+    // Every thread commits exactly one copy group per prefetch slot (empty
+    // when there is nothing to load), so "tile t has landed" is
+    // cp.async.wait_group S-2 followed by a CTA barrier.
+    auto issue_prefetch = [&](int64_t t, float2* dst) {
+        if (t < total) {
+            const int j = find_job(jt, t);
+            if (tile_loads(j)) {
+                const PassDesc& pd = *jt.job[j].pd;
+                const RunArgs& ra = jt.job[j].A;
+                TileGeo gn = tile_geo(pd, t - jt.begin[j], ra.n, ra.batch);
+                thread_tile_load<TB, RB>(pd, gn, ra.state, dst, ra.n, tid);
+            }
+        }
+        cp_async_commit();
     };
 
     const int64_t t0 = blockIdx.x;
-    if (tid < 32) {
-        for (int i = 0; i < S - 1; ++i) {
-            const int64_t tp = t0 + (int64_t)i * gridDim.x;
-            if (tp < total && tile_loads(find_job(jt, tp))) issue_prefetch(tp, bufs + i * AMPS, &bars[i]);
-        }
-    }
+#pragma unroll
+    for (int i = 0; i < S - 1; ++i) issue_prefetch(t0 + (int64_t)i * gridDim.x, bufs + i * AMPS);
     int cur_job = -1;
     int iter = 0;
     for (int64_t t = t0; t < total; t += gridDim.x, ++iter) {
@@ -445,13 +523,9 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         PTile<RB> pt;
         uint32_t xm = 0;  // pending thread-controlled X per register bit
         ThreadMap tm;
+        cp_async_wait<S - 2>();  // this thread's copies of tile t have landed
+        __syncthreads();         // ... and every other thread's
         if (load_in) {
-            bool ok = mbar_wait(&bars[slot], phase[slot] & 1);
-            ++phase[slot];
-            if (__syncthreads_or(!ok)) {
-                if (tid == 0) atomicExch(A.status, kStatusTimeout);
-                break;
-            }
             pload_nat<RB>(pt, buf, tid);
             decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
         } else {
@@ -497,17 +571,11 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 }
             }
         }
-        // everybody has read `buf`; prefetch S-1 tiles ahead into the buffer the
-        // previous tile used (its store has to have read it out first)
-        __syncthreads();
-        {
-            const int64_t tp = t + (int64_t)(S - 1) * gridDim.x;
-            const int ps = (iter + S - 1) % S;
-            if (tid < 32 && tp < total && tile_loads(find_job(jt, tp))) {
-                bulk_wait_read0();
-                issue_prefetch(tp, bufs + ps * AMPS, &bars[ps]);
-            }
-        }
+        // Prefetch S-1 tiles ahead into the buffer the previous tile used: the
+        // end of that tile waited for every read of it.  (The first exchange
+        // and the epilogue start with a barrier, so every thread has read
+        // `buf` before it is written again.)
+        issue_prefetch(t + (int64_t)(S - 1) * gridDim.x, bufs + ((iter + S - 1) % S) * AMPS);
         // ---- the gate program of this pass ----
         Ops::template apply<TB, RB>(pt, xm, tm, d, A, ops, s_ops, s_mats, reinterpret_cast<float*>(buf), g.sample,
                                     g.fixed_val, tid);
@@ -515,20 +583,10 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         __syncthreads();  // all exchange reads of `buf` are done
         const int64_t smp0 = g.sample;
         if (d.epi & EPI_STORE) {
-            pstore_nat<RB>(pt, buf, tid, xm);
-            fence_proxy_async();
-            __syncthreads();
-            if (tid < 32) {
-                issue_tile_store(d, g, A.state, buf, n, lane);
-                if (d.ckpt >= 0) issue_tile_store(d, g, A.ckpt + (int64_t)d.ckpt * (A.batch << n), buf, n, lane);
-                bulk_commit();
-            }
+            pstore_global<RB>(pt, xm, d, g, A.state, n, tid);
+            if (d.ckpt >= 0) pstore_global<RB>(pt, xm, d, g, A.ckpt + (int64_t)d.ckpt * (A.batch << n), n, tid);
         }
         if (d.epi & (EPI_PROBS | EPI_P0)) {
-            if (d.epi & EPI_STORE) {
-                if (tid < 32) bulk_wait_read0();
-                __syncthreads();
-            }
             float* pb = reinterpret_cast<float*>(buf);
             pstore_probs<RB>(pt, pb, tid, xm);
             if (d.epi & EPI_PROBS) {
@@ -605,7 +663,7 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 }
             }
         }
-        // make `buf` free before it receives the prefetch two tiles ahead
+        // make `buf` free before it receives the prefetch S-1 tiles ahead
         fence_proxy_async();
         __syncthreads();
     }
