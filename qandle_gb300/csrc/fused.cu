@@ -196,6 +196,9 @@ __device__ __forceinline__ float pgrad_op(const PTile<RB>& ps, const PTile<RB>& 
 // Gate program of a forward pass read from the pass's op list at run time
 // (the prebuilt kernels; the compiled pass kernels of jit.cpp unroll it).
 struct InterpOps {
+    static constexpr bool kStageOps = true;
+    template <int TB, int RB>
+    __device__ __forceinline__ static void tile_start(const RunArgs&, const TileGeo&, float4*, int) {}
     template <int TB, int RB>
     __device__ __forceinline__ static void apply(PTile<RB>& pt, uint32_t& xm, ThreadMap& tm, const PassDesc& d,
                                                  const RunArgs& A, const int4* ops, const int4* s_ops,
@@ -234,11 +237,9 @@ __global__ void __launch_bounds__(1 << (TB - RB), 1)
     // sample (within the tile) each partial belongs to: the thread's sample
     // bits depend on the mapping in force when the gradient op ran
     uint8_t* gsmp = reinterpret_cast<uint8_t*>(gacc + max_grad_per_pass(RB) * NT);  // [ngrad][NT]
-    __shared__ __align__(8) uint64_t bars[2];
     __shared__ PassDesc sd;
 
     const int tid = threadIdx.x;
-    const int lane = tid & 31;
     if (tid == 0) sd = passes[pass_index];
     __syncthreads();
     const PassDesc& d = sd;
@@ -254,20 +255,20 @@ __global__ void __launch_bounds__(1 << (TB - RB), 1)
     const bool last = (d.epi & EPI_STORE) == 0;  // final backward pass: nothing to store but lambda
     (void)last;
 
-    if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
     __syncthreads();
+    // psi and lambda of a tile arrive as one cp.async group per thread; every
+    // thread commits one group per tile (empty past the last tile), so
+    // "tile t has landed" is wait_group 0 before the next commit + a barrier
+    auto prefetch = [&](int64_t t, float2* dst) {
+        if (t < num_tiles) {
+            TileGeo gn = tile_geo(d, t, n, A.batch);
+            thread_tile_load<TB, RB>(d, gn, psi_src, dst, n, tid);
+            thread_tile_load<TB, RB>(d, gn, A.lam, dst + AMPS, n, tid);
+        }
+        cp_async_commit();
+    };
     int64_t t0 = blockIdx.x;
-    if (tid < 32 && t0 < num_tiles) {
-        TileGeo g = tile_geo(d, t0, n, A.batch);
-        if (lane == 0) mbar_expect_tx(&bars[0], 2 * tile_bytes(d, g, n));
-        __syncwarp();
-        issue_tile_load(d, g, psi_src, pbuf0, &bars[0], n, lane);
-        issue_tile_load(d, g, A.lam, pbuf0 + AMPS, &bars[0], n, lane);
-    }
+    prefetch(t0, pbuf0);
     int iter = 0;
     for (int64_t t = t0; t < num_tiles; t += gridDim.x, ++iter) {
         float2* ps = pbuf0 + (iter & 1) * 2 * AMPS;
@@ -278,23 +279,13 @@ __global__ void __launch_bounds__(1 << (TB - RB), 1)
         PTile<RB>* const tiles[2] = {&pt, &lt};
         uint32_t xm = 0;  // pending thread-controlled X, shared by psi and lambda
         ThreadMap tm;
-        bool ok = mbar_wait(&bars[iter & 1], (iter >> 1) & 1);
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) atomicExch(A.status, QG_ETIMEOUT);
-            break;
-        }
+        cp_async_wait<0>();
+        __syncthreads();
         pload_nat<RB>(pt, ps, tid);
         pload_nat<RB>(lt, ls, tid);
         decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
-        __syncthreads();
-        if (tid < 32 && t + gridDim.x < num_tiles) {
-            bulk_wait_read0();
-            TileGeo gn = tile_geo(d, t + gridDim.x, n, A.batch);
-            if (lane == 0) mbar_expect_tx(&bars[(iter + 1) & 1], 2 * tile_bytes(d, gn, n));
-            __syncwarp();
-            issue_tile_load(d, gn, psi_src, nps, &bars[(iter + 1) & 1], n, lane);
-            issue_tile_load(d, gn, A.lam, nps + AMPS, &bars[(iter + 1) & 1], n, lane);
-        }
+        // the other buffer pair held tile t - 1, whose end waited for every read
+        prefetch(t + gridDim.x, nps);
         for (int o = 0; o < d.op_count; ++o) {
             int4 op = o < kSmemOps ? s_ops[o] : __ldg(ops + o);
             if (op.x == OP_MAP) {
@@ -344,30 +335,16 @@ __global__ void __launch_bounds__(1 << (TB - RB), 1)
                 }
             }
         }
-        // store psi and lambda (natural mapping)
+        // store psi and lambda (natural mapping) straight from registers
         if (d.epi & EPI_STORE) {
-            pstore_nat<RB>(pt, ps, tid, xm);
-            pstore_nat<RB>(lt, ls, tid, xm);
-            fence_proxy_async();
-            __syncthreads();
-            if (tid < 32) {
-                issue_tile_store(d, g, A.state, ps, n, lane);
-                issue_tile_store(d, g, A.lam, ls, n, lane);
-                bulk_commit();
-            }
+            pstore_global<RB>(pt, xm, d, g, A.state, n, tid);
+            pstore_global<RB>(lt, xm, d, g, A.lam, n, tid);
         } else if (store_lam_last) {
-            pstore_nat<RB>(lt, ls, tid, xm);
-            fence_proxy_async();
-            __syncthreads();
-            if (tid < 32) {
-                issue_tile_store(d, g, A.lam, ls, n, lane);
-                bulk_commit();
-            }
+            pstore_global<RB>(lt, xm, d, g, A.lam, n, tid);
         }
-        fence_proxy_async();
-        __syncthreads();
+        __syncthreads();  // `ps` / `ls` are free for the prefetch two tiles ahead
     }
-    if (tid < 32) bulk_wait_all0();
+    cp_async_wait<0>();
 }
 
 // ------------------------------------------------------------ helpers --

@@ -504,10 +504,13 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 sd = *jt.job[j].pd;
                 sa = jt.job[j].A;
             }
-            // the pass's op list and the shared matrix table, staged once per job
-            const int4* gops = jt.job[j].ops;
-            const int nops = jt.job[j].pd->op_count;
-            for (int i = tid; i < nops && i < kSmemOps; i += NT) s_ops[i] = __ldg(gops + i);
+            // the pass's op list (when Ops reads it) and the shared matrix
+            // table, staged once per job
+            if (Ops::kStageOps) {
+                const int4* gops = jt.job[j].ops;
+                const int nops = jt.job[j].pd->op_count;
+                for (int i = tid; i < nops && i < kSmemOps; i += NT) s_ops[i] = __ldg(gops + i);
+            }
             const int nm = jt.job[j].A.nslots_shared < kSmemMats ? jt.job[j].A.nslots_shared : kSmemMats;
             const float4* gm = reinterpret_cast<const float4*>(jt.job[j].A.mats);
             for (int i = tid; i < 2 * nm; i += NT) s_mats[i] = __ldg(gm + i);
@@ -523,6 +526,9 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         PTile<RB> pt;
         uint32_t xm = 0;  // pending thread-controlled X per register bit
         ThreadMap tm;
+        // per-tile data of Ops (in the op-list area when it is not staged),
+        // published by the barrier below
+        Ops::template tile_start<TB, RB>(A, g, reinterpret_cast<float4*>(s_ops), tid);
         cp_async_wait<S - 2>();  // this thread's copies of tile t have landed
         __syncthreads();         // ... and every other thread's
         if (load_in) {

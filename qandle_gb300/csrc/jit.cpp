@@ -155,18 +155,54 @@ std::string pass_source(const ProgramRun& R, int p) {
     const PassDesc& d = R.fpass[p];
     const int tb = d.tile_bits, rb = R.reg_bits;  // the launch uses the same pair
     const int nt = 1 << (tb - rb);
+    const int32_t* ops = R.fops + 4 * (size_t)d.op_begin;
+    // With n >= TB a tile lies in one sample, so the pass's per-sample
+    // matrices are the same for the whole CTA: they are copied into shared
+    // memory (the op-list area, unused here) at each tile's start instead of
+    // being read from global memory by every thread at every op.
+    std::vector<int32_t> staged;  // per-sample slot of each staged matrix
+    std::map<int32_t, int> staged_index;
+    if (R.n >= tb) {
+        for (int o = 0; o < d.op_count; ++o) {
+            const int32_t k = ops[4 * o], z = ops[4 * o + 2], w = ops[4 * o + 3];
+            if ((k == OP_MAT || k == OP_DIAG) && (w & OPF_PER_SAMPLE) && !staged_index.count(z)) {
+                staged_index[z] = (int)staged.size();
+                staged.push_back(z);
+            }
+        }
+        const int cap = std::min(nt / 2, kSmemOps * 16 / 32);
+        if ((int)staged.size() > cap) {
+            staged.clear();
+            staged_index.clear();
+        }
+    }
     std::ostringstream s;
     s << "#include \"jit_ops.cuh\"\n"
          "namespace qg {\n"
          "struct PassOps {\n"
+         "  static constexpr bool kStageOps = false;\n"
+         "  template <int TB, int RB>\n"
+         "  __device__ __forceinline__ static void tile_start(const RunArgs& A, const TileGeo& g, float4* sm, "
+         "int tid) {\n";
+    if (!staged.empty()) {
+        s << "    if (tid < " << 2 * staged.size() << ") {\n      const int k = tid >> 1;\n      const int slot = ";
+        for (size_t i = 0; i + 1 < staged.size(); ++i) s << "k == " << i << " ? " << staged[i] << " : ";
+        s << staged.back() << ";\n"
+          << "      sm[tid] = __ldg(reinterpret_cast<const float4*>(A.mats_ps + (g.sample * A.nslots_ps + slot) * 4)"
+             " + (tid & 1));\n    }\n";
+    }
+    s << "  }\n"
          "  template <int TB, int RB>\n"
          "  __device__ __forceinline__ static void apply(PTile<RB>& pt, uint32_t& xm, ThreadMap& tm, "
-         "const PassDesc& d, const RunArgs& A, const int4*, const int4*, const float4* s_mats, float* plane, "
-         "int64_t sample0, uint32_t fixed_val, int tid) {\n";
-    const int32_t* ops = R.fops + 4 * (size_t)d.op_begin;
+         "const PassDesc& d, const RunArgs& A, const int4*, const int4* s_ops, const float4* s_mats, float* plane, "
+         "int64_t sample0, uint32_t fixed_val, int tid) {\n"
+         "    const float4* staged = reinterpret_cast<const float4*>(s_ops);\n"
+         "    (void)staged;\n";
     for (int o = 0; o < d.op_count; ++o) {
         const int32_t k = ops[4 * o], y = ops[4 * o + 1], z = ops[4 * o + 2], w = ops[4 * o + 3];
         const std::string smp = "sample0 + tm.sample_off";
+        const bool st = (k == OP_MAT || k == OP_DIAG) && (w & OPF_PER_SAMPLE) && staged_index.count(z);
+        const int si = st ? staged_index[z] : -1;
         s << "    ";
         switch (k) {
             case OP_MAP:
@@ -174,15 +210,25 @@ std::string pass_source(const ProgramRun& R, int p) {
                   << ", tid, fixed_val);\n";
                 break;
             case OP_MAT:
-                s << "jmat<" << y << ", RB>(pt, xm, A, s_mats, " << z << ", " << w << ", " << smp << ");\n";
+                if (st)
+                    s << "jmat_staged<" << y << ", RB>(pt, xm, staged, " << si << ");\n";
+                else
+                    s << "jmat<" << y << ", RB>(pt, xm, A, s_mats, " << z << ", " << w << ", " << smp << ");\n";
                 break;
             case OP_DIAG:
-                if (y & LOC_REG)
-                    s << "jdiag<" << (y & 7) << ", RB>(pt, xm, A, s_mats, " << z << ", " << w << ", " << smp
-                      << ");\n";
-                else
-                    s << "jdiag_thread<RB>(pt, " << loc_bit(y) << ", A, s_mats, " << z << ", " << w << ", " << smp
-                      << ");\n";
+                if (y & LOC_REG) {
+                    if (st)
+                        s << "jdiag_staged<" << (y & 7) << ", RB>(pt, xm, staged, " << si << ");\n";
+                    else
+                        s << "jdiag<" << (y & 7) << ", RB>(pt, xm, A, s_mats, " << z << ", " << w << ", " << smp
+                          << ");\n";
+                } else {
+                    if (st)
+                        s << "jdiag_thread_staged<RB>(pt, " << loc_bit(y) << ", staged, " << si << ");\n";
+                    else
+                        s << "jdiag_thread<RB>(pt, " << loc_bit(y) << ", A, s_mats, " << z << ", " << w << ", "
+                          << smp << ");\n";
+                }
                 break;
             case OP_CX:
                 if (z & LOC_REG)

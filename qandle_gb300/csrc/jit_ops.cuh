@@ -35,6 +35,39 @@ __device__ __forceinline__ void jmat(PTile<RB>& pt, uint32_t xm, const RunArgs& 
     pmat<P, RB>(pt, m);
 }
 
+// A matrix staged in shared memory (two float4: M00 M01 | M10 M11).
+__device__ __forceinline__ void smem_mat(const float4* sm, float2 m[4]) {
+    const float4 u = sm[0], v = sm[1];
+    m[0] = make_float2(u.x, u.y);
+    m[1] = make_float2(u.z, u.w);
+    m[2] = make_float2(v.x, v.y);
+    m[3] = make_float2(v.z, v.w);
+}
+
+// Per-sample matrix k of the tile's sample, staged at the tile's start.
+template <int P, int RB>
+__device__ __forceinline__ void jmat_staged(PTile<RB>& pt, uint32_t xm, const float4* staged, int k) {
+    float2 m[4];
+    smem_mat(staged + 2 * k, m);
+    xmx_if(m, (xm >> P) & 1u);
+    pmat<P, RB>(pt, m);
+}
+
+template <int P, int RB>
+__device__ __forceinline__ void jdiag_staged(PTile<RB>& pt, uint32_t xm, const float4* staged, int k) {
+    float2 m[4];
+    smem_mat(staged + 2 * k, m);
+    const bool sw = (xm >> P) & 1u;
+    pdiag<P, RB>(pt, sw ? m[3] : m[0], sw ? m[0] : m[3]);
+}
+
+template <int RB>
+__device__ __forceinline__ void jdiag_thread_staged(PTile<RB>& pt, bool bit, const float4* staged, int k) {
+    float2 m[4];
+    smem_mat(staged + 2 * k, m);
+    pscale<RB>(pt, bit ? m[3] : m[0]);
+}
+
 template <int P, int RB>
 __device__ __forceinline__ void jdiag(PTile<RB>& pt, uint32_t xm, const RunArgs& A, const float4* s_mats, int slot,
                                       int flags, int64_t sample) {
