@@ -3,10 +3,10 @@
 // program (jit.cpp).  Everything here is device code that needs no host
 // header, so the same text is handed to NVRTC.
 //
-// A pass walks tiles of 2^TB amplitudes: each tile is loaded by bulk async
-// copies (cp.async.bulk, completion on an mbarrier) into one of a ring of
-// shared-memory buffers, so later tiles stream in while the current one is
-// computed.  A thread holds 2^RB amplitudes in registers (planar.cuh); the
+// A pass walks tiles of 2^TB amplitudes: each tile is loaded by per-thread
+// async copies (cp.async) into one of a ring of shared-memory buffers, so
+// later tiles stream in while the current one is computed, and stored
+// straight from registers.  A thread holds 2^RB amplitudes in registers (planar.cuh); the
 // gate program of the pass runs on them (`Ops`), exchanging through the
 // tile's buffer when the register qubits change; the epilogue stores the
 // tile, its probabilities or P0 partials.
@@ -21,38 +21,6 @@ namespace qg {
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-// Bounded wait on an mbarrier phase.  Returns false if it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t addr = smem_u32(bar);
-    for (int it = 0; it < (1 << 22); ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(addr), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
 }
 
 __device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t bytes) {
@@ -119,40 +87,6 @@ __device__ __forceinline__ int64_t run_offset(const PassDesc& d, int r) {
             off += (lb < d.nq_tile) ? (int64_t(1) << d.gbit[lb]) : 0;
         }
     return off;
-}
-
-// Bytes of one tile's state image.
-__device__ __forceinline__ uint32_t tile_bytes(const PassDesc& d, const TileGeo& g, int n) {
-    if (n < d.tile_bits) return (uint32_t)((int64_t)g.nsamples << n) * 8u;
-    return (1u << d.tile_bits) * 8u;
-}
-
-// The bulk copies of one tile are issued by the 32 lanes of warp 0 in
-// parallel (lane l issues runs l, l + 32, ...); for loads the caller has armed
-// `bar` with the tile's byte count through one arrive.expect_tx first.
-__device__ void issue_tile_load(const PassDesc& d, const TileGeo& g, const float2* src, float2* dst,
-                                uint64_t* bar, int n, int lane) {
-    if (n < d.tile_bits) {
-        if (lane == 0) bulk_g2s(dst, src + g.base, tile_bytes(d, g, n), bar);
-        return;
-    }
-    int runs = 1 << (d.tile_bits - d.run_bits);
-    uint32_t rb = (1u << d.run_bits) * 8u;
-    for (int r = lane; r < runs; r += 32)
-        bulk_g2s(dst + ((int64_t)r << d.run_bits), src + g.base + run_offset(d, r), rb, bar);
-}
-
-__device__ void issue_tile_store(const PassDesc& d, const TileGeo& g, float2* dstg, const float2* src, int n,
-                                 int lane) {
-    if (n < d.tile_bits) {
-        uint32_t bytes = (uint32_t)((int64_t)g.nsamples << n) * 8u;
-        if (lane == 0) bulk_s2g(dstg + g.base, src, bytes);
-        return;
-    }
-    int runs = 1 << (d.tile_bits - d.run_bits);
-    uint32_t rb = (1u << d.run_bits) * 8u;
-    for (int r = lane; r < runs; r += 32)
-        bulk_s2g(dstg + g.base + run_offset(d, r), src + ((int64_t)r << d.run_bits), rb);
 }
 
 // Per-thread async copies (cp.async, 16 bytes = 2 amplitudes each) of one
@@ -325,14 +259,8 @@ __device__ __forceinline__ void pload_nat(PTile<RB>& t, const float2* buf, int t
     for (int r = 0; r < (1 << RB); ++r) set_amp<RB>(t, r, buf[nat_index<RB>(r, tid)]);
 }
 
-// Natural-order store; physical register r holds logical amplitude r ^ xm.
-template <int RB>
-__device__ __forceinline__ void pstore_nat(const PTile<RB>& t, float2* buf, int tid, uint32_t xm) {
-    const int x = (int)xm << 5;
-#pragma unroll
-    for (int r = 0; r < (1 << RB); ++r) buf[nat_index<RB>(r, tid) ^ x] = get_amp<RB>(t, r);
-}
-
+// Probabilities of the tile in natural order into shared memory; physical
+// register r holds logical amplitude r ^ xm.
 template <int RB>
 __device__ __forceinline__ void pstore_probs(const PTile<RB>& t, float* pb, int tid, uint32_t xm) {
     const int x = (int)xm << 5;
