@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--low-bits", type=int, default=6)
     ap.add_argument("--k", type=int, default=0, help="max strided qubits per pass (0 = tile limit)")
     ap.add_argument("--reg-bits", type=int, default=5, help="amplitudes per thread = 2^reg_bits")
+    ap.add_argument("--serving-requests", type=int, default=48, help="requests in the serving run")
+    ap.add_argument("--autotune", action="store_true",
+                    help="time the candidate plans first and run the headline with the fastest")
     ap.add_argument("--interpreted", action="store_true",
                     help="run the prebuilt op interpreter instead of the per-program compiled passes")
     ap.add_argument("--n", type=int, default=20)
@@ -209,6 +212,13 @@ def main():
     # ---------------- fused forward, inputs resident in HBM ----------------
     opts = dict(tile_bits=args.tile_bits, low_bits=args.low_bits, max_high=args.k, reg_bits=args.reg_bits,
                 compiled=not args.interpreted)
+    tuned = None
+    if args.autotune:
+        from qandle_gb300 import tune
+
+        tuned = tune.autotune(workloads.build_circuit(desc, engine="fused"), B, dev,
+                              compiled=not args.interpreted)
+        opts.update(tuned["options"])
     circ = workloads.build_circuit(desc, engine="fused", **opts).to(dev)
     kw = workloads.circuit_inputs(desc, dev)
     with torch.no_grad():
@@ -289,6 +299,9 @@ def main():
         "clocks": clock_info,
         "gpu_launches": gpu_launches,
     }
+    if tuned is not None:
+        line["autotune"] = {"options": tuned["options"], "cached": tuned["cached"],
+                            "timings_ms": [[o, round(t, 3)] for o, t in tuned["timings"]]}
 
     # ---------------- end to end through the public API ----------------
     x_host = torch.tensor(desc["inputs"]["x"]).pin_memory()
@@ -358,6 +371,14 @@ def main():
         line["adjoint"] = bench_adjoint(dev, sync_all, W)
         torch.cuda.empty_cache()
 
+        # ---------------- deep single state: 28 qubits x batch 1 ----------------
+        line["deep28"] = bench_deep(dev, sync_all, W)
+        torch.cuda.empty_cache()
+
+        # ---------------- serving: Poisson arrivals of mixed-width requests ----------------
+        line["serving"] = bench_serving(dev, args.serving_requests)
+        torch.cuda.empty_cache()
+
         # ---------------- fusion width sweep ----------------
         if args.sweep:
             sweep = {}
@@ -390,6 +411,116 @@ def main():
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def bench_deep(dev, sync_all, W):
+    """28 qubits, batch 1 (2 GiB), 50 layers of U per qubit with CNOT+SWAP
+    brickwork, |psi|^2 out: fused forward against the per-gate form."""
+    import torch
+
+    from qandle_gb300 import engine, workloads
+
+    desc = workloads.deep_u()
+    n = desc["n"]
+    amp = workloads.gate_count(desc) * (1 << n)
+    circ = workloads.build_circuit(desc, engine="fused").to(dev)
+    with torch.no_grad():
+        circ()
+    bound = engine.BoundForward(circ._executor, 1, dev)
+    bound.set_inputs()  # the circuit's U matrices
+    for _ in range(max(1, W)):
+        bound.launch()
+    sync_all()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    steps = 3
+    e0.record()
+    for _ in range(steps):
+        bound.launch()
+    e1.record()
+    sync_all()
+    fms = e0.elapsed_time(e1) / steps
+    fused_probs = bound.result().reshape(-1)
+    norm = float(fused_probs.double().sum())
+    del bound
+    circ_p = workloads.build_circuit(desc, engine="plain").to(dev)
+    with torch.no_grad():
+        sync_all()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record()
+        plain_probs = circ_p().reshape(-1)
+        p1.record()
+        sync_all()
+    pms = p0.elapsed_time(p1)
+    diff = float((plain_probs - fused_probs).abs().max())
+    return {"workload": f"deep_u: {n} qubits x batch 1, 50 layers of U + CNOT/SWAP brickwork, |psi|^2 out "
+                        f"({workloads.gate_count(desc)} gates)",
+            "plan": circ._executor.program(False).summary(),
+            "ms_per_step_fused": fms, "ms_per_step_per_gate": pms, "fused_speedup": pms / fms,
+            "amp_updates_per_s_fused": amp / (fms * 1e-3), "amp_updates_per_s_per_gate": amp / (pms * 1e-3),
+            "norm_fused": norm, "max_abs_prob_diff_fused_vs_per_gate": diff}
+
+
+def bench_serving(dev, count: int, rate: float = 2000.0, seed: int = 7):
+    """Open-loop Poisson arrivals (rate per second) of mixed strongly-
+    entangling requests: n ~ U{4..24}, depth ~ U{2..30}, batch log-uniform in
+    [1, 512], <Z> out.  The continuous-batching server against the same
+    requests served one after another in arrival order by the per-gate form
+    (one launch per gate per request)."""
+    import numpy as np
+    import torch
+
+    from qandle_gb300 import serve, workloads
+
+    rng = np.random.default_rng(seed)
+    reqs = [workloads.random_sel_request(rng) for _ in range(count)]
+    offs = np.concatenate([[0.0], np.cumsum(rng.exponential(1.0 / rate, size=count - 1))])
+    amp = float(sum(workloads.gate_count(d) * d["batch"] * (1 << d["n"]) for d in reqs))
+
+    srv = serve.Server(dev, hbm_budget=160 << 30)
+    try:
+        t0 = time.perf_counter()
+        handles = []
+        for d, o in zip(reqs, offs):
+            wait = t0 + o - time.perf_counter()
+            if wait > 0:
+                time.sleep(wait)
+            handles.append(srv.submit(d, arrival=t0 + o))
+        outs = [h.future.result(timeout=900) for h in handles]
+        t_end = max(h.completed for h in handles)
+        steps, launches = srv.steps, srv.launches
+    finally:
+        srv.close()
+    lat = np.array([h.latency for h in handles]) * 1e3
+    span = t_end - t0
+    fused = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+             "circuits_per_s": count / span, "amp_updates_per_s": amp / span, "wall_s": span,
+             "steps": steps, "launches": launches}
+    del handles
+    torch.cuda.empty_cache()
+
+    service, diff = [], 0.0
+    for i, d in enumerate(reqs):
+        torch.cuda.synchronize(dev)
+        s = time.perf_counter()
+        out = serve.run_plain(d, dev).cpu()
+        service.append(time.perf_counter() - s)
+        diff = max(diff, float((out - outs[i]).abs().max()))
+        del out
+    done, lat_p = 0.0, []
+    for o, sv in zip(offs, service):
+        done = max(done, o) + sv
+        lat_p.append((done - o) * 1e3)
+    lat_p = np.array(lat_p)
+    plain = {"p50_ms": float(np.percentile(lat_p, 50)), "p99_ms": float(np.percentile(lat_p, 99)),
+             "circuits_per_s": count / done, "amp_updates_per_s": amp / done, "wall_s": done}
+    return {"workload": f"{count} requests, Poisson {rate:g}/s, n ~ U{{4..24}}, depth ~ U{{2..30}}, "
+                        "batch log-uniform [1, 512], <Z> out (seed 7)",
+            "amp_updates": amp, "continuous_batching": fused, "per_gate_fifo": plain,
+            "throughput_ratio": fused["circuits_per_s"] / plain["circuits_per_s"],
+            "max_abs_diff_vs_per_gate": diff,
+            "note": "per-gate latencies replay the measured service times in arrival order (FIFO)"}
 
 
 def bench_adjoint(dev, sync_all, W):

@@ -8,6 +8,7 @@ There is no CPU execution path: tensors must live on a CUDA device.
 """
 # ruff: noqa: F401 F403
 from . import config, errors, remap
+from .tune import autotune
 from .operators import *
 from .embeddings import *
 from .measurements import *

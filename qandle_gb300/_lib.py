@@ -127,6 +127,15 @@ def load():
         path = _build.LIB
         if not os.path.exists(path):
             _build.build()
+        # compiled pass kernels are kept on disk beside the library unless the
+        # caller chose another place (an empty value turns the cache off)
+        if "QG_JIT_CACHE_DIR" not in os.environ:
+            cache = os.path.join(os.path.dirname(path), "jit_cache")
+            try:
+                os.makedirs(cache, exist_ok=True)
+                os.environ["QG_JIT_CACHE_DIR"] = cache
+            except OSError:
+                pass
         lib = ctypes.CDLL(path)
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(lib, name, None)

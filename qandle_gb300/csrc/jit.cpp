@@ -15,13 +15,17 @@
 // loading and launches go through driver entry points obtained from the CUDA
 // runtime (no link-time libcuda dependency).  Compiled modules are cached
 // process-wide by (device, source text), so rebuilding an identical program
-// compiles nothing.
+// compiles nothing; QG_JIT_CACHE_DIR adds a cache of cubins on disk.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <dlfcn.h>
+#include <unistd.h>
 #include <nvrtc.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <functional>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -60,6 +64,7 @@ struct Nvrtc {
     decltype(&nvrtcGetCUBIN) cubin = nullptr;
     decltype(&nvrtcDestroyProgram) destroy = nullptr;
     decltype(&nvrtcGetErrorString) error_string = nullptr;
+    decltype(&nvrtcVersion) version = nullptr;
     std::string why;  // empty when loaded
 };
 
@@ -94,6 +99,7 @@ const Nvrtc& nvrtc() {
         QG_SYM(cubin, nvrtcGetCUBIN)
         QG_SYM(destroy, nvrtcDestroyProgram)
         QG_SYM(error_string, nvrtcGetErrorString)
+        QG_SYM(version, nvrtcVersion)
 #undef QG_SYM
     });
     return N;
@@ -279,17 +285,75 @@ struct Loaded {
 std::mutex g_cache_mu;
 std::map<std::pair<int, std::string>, Loaded> g_cache;  // (device, source) -> module
 
+const char* const kOpts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "-DQG_RTC=1"};
+constexpr int kNumOpts = (int)(sizeof(kOpts) / sizeof(kOpts[0]));
+
+// Optional on-disk cache of compiled passes: QG_JIT_CACHE_DIR names a
+// directory; a pass's cubin is stored under a 64-bit FNV-1a hash of its
+// source, the headers it includes, the compile options and the NVRTC
+// version.
+std::string cache_path(const std::string& src, const char* const* opts, int nopts) {
+    const char* dir = getenv("QG_JIT_CACHE_DIR");
+    if (!dir || !*dir) return "";
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](const std::string& t) {
+        for (unsigned char ch : t) {
+            h ^= ch;
+            h *= 1099511628211ull;
+        }
+        h ^= 0xff;
+        h *= 1099511628211ull;
+    };
+    mix(src);
+    for (int i = 0; i < kJitHeaderCount; ++i) mix(kJitHeaderTexts[i]);  // the kernel body it includes
+    for (int i = 0; i < nopts; ++i) mix(opts[i]);
+    int major = 0, minor = 0;
+    if (nvrtc().version) nvrtc().version(&major, &minor);
+    mix(std::to_string(major) + "." + std::to_string(minor));
+    char name[64];
+    snprintf(name, sizeof(name), "/qg_pass_%016llx_%zu.cubin", (unsigned long long)h, src.size());
+    return std::string(dir) + name;
+}
+
+bool cache_read(const std::string& path, std::vector<char>& cubin) {
+    if (path.empty()) return false;
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) return false;
+    fseek(f, 0, SEEK_END);
+    long n = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    bool ok = n > 0;
+    if (ok) {
+        cubin.resize((size_t)n);
+        ok = fread(cubin.data(), 1, (size_t)n, f) == (size_t)n;
+    }
+    fclose(f);
+    return ok;
+}
+
+void cache_write(const std::string& path, const std::vector<char>& cubin) {
+    if (path.empty()) return;
+    const std::string tmp = path + ".tmp" + std::to_string((long long)getpid()) + "_" +
+                            std::to_string((unsigned long long)std::hash<std::thread::id>()(std::this_thread::get_id()));
+    FILE* f = fopen(tmp.c_str(), "wb");
+    if (!f) return;
+    const bool ok = fwrite(cubin.data(), 1, cubin.size(), f) == cubin.size();
+    fclose(f);
+    if (ok) rename(tmp.c_str(), path.c_str());
+    else remove(tmp.c_str());
+}
+
 int compile_source(const std::string& src, std::vector<char>& cubin, std::string& err) {
     const Nvrtc& N = nvrtc();
+    const std::string cpath = cache_path(src, kOpts, kNumOpts);
+    if (cache_read(cpath, cubin)) return QG_OK;
     nvrtcProgram prog = nullptr;
     nvrtcResult r = N.create(&prog, src.c_str(), "qg_pass.cu", kJitHeaderCount, kJitHeaderTexts, kJitHeaderNames);
     if (r != NVRTC_SUCCESS) {
         err = std::string("nvrtcCreateProgram: ") + N.error_string(r);
         return QG_ECUDA;
     }
-    const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo",
-                          "-DQG_RTC=1"};
-    r = N.compile(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+    r = N.compile(prog, kNumOpts, kOpts);
     if (r != NVRTC_SUCCESS) {
         size_t n = 0;
         N.log_size(prog, &n);
@@ -304,6 +368,7 @@ int compile_source(const std::string& src, std::vector<char>& cubin, std::string
     cubin.resize(n);
     N.cubin(prog, cubin.data());
     N.destroy(&prog);
+    cache_write(cpath, cubin);
     return QG_OK;
 }
 

@@ -582,6 +582,13 @@ static void renumber(std::vector<int32_t>& ops, const std::vector<SlotDesc>& sd)
 
 static int build_program(Program& P, const qg_gate* gates, int ngates, const int32_t* qlist) {
     const int n = P.n;
+    // SWAPs are absorbed by relabelling: perm[b] is the bit of the stored
+    // state that holds the reference's bit b.  A SWAP exchanges two entries
+    // and emits nothing; every other gate acts on the bits perm points to.
+    // At the end, SWAPs on stored bits put every bit back (at most n - 1),
+    // so the state, its probabilities and P0 come out in the caller's order.
+    int perm[32];
+    for (int b = 0; b < 32; ++b) perm[b] = b;
     // the last embedding overwrites the state: everything before it is dead
     int start = 0;
     for (int i = 0; i < ngates; ++i)
@@ -597,7 +604,7 @@ static int build_program(Program& P, const qg_gate* gates, int ngates, const int
                 if (g.src != 0 && g.src != 1) return set_error("rotation src must be 0 or 1"), QG_EINVAL;
                 l.kind = K_ROT;
                 l.axis = g.kind;
-                l.b0 = n - 1 - g.q0;
+                l.b0 = perm[n - 1 - g.q0];
                 l.src = g.src;
                 l.idx = g.idx;
                 l.diag = (g.kind == QG_GATE_RZ);
@@ -608,7 +615,7 @@ static int build_program(Program& P, const qg_gate* gates, int ngates, const int
             case QG_GATE_U:
                 if (g.q0 < 0 || g.q0 >= n) return set_error("U qubit out of range"), QG_EINVAL;
                 l.kind = K_U;
-                l.b0 = n - 1 - g.q0;
+                l.b0 = perm[n - 1 - g.q0];
                 l.idx = g.idx;
                 l.diag = (g.aux & 1) != 0;  // caller asserts the matrix is diagonal
                 P.numats = std::max(P.numats, g.idx + 1);
@@ -622,9 +629,13 @@ static int build_program(Program& P, const qg_gate* gates, int ngates, const int
                     if (g.kind == QG_GATE_SWAP) continue;  // identity (operators.py:661-671)
                     return set_error("control and target must differ"), QG_EINVAL;
                 }
-                l.kind = g.kind == QG_GATE_CNOT ? K_CNOT : (g.kind == QG_GATE_CZ ? K_CZ : K_SWAP);
-                l.b0 = n - 1 - g.q0;
-                l.b1 = n - 1 - g.q1;
+                if (g.kind == QG_GATE_SWAP) {
+                    std::swap(perm[n - 1 - g.q0], perm[n - 1 - g.q1]);
+                    continue;
+                }
+                l.kind = g.kind == QG_GATE_CNOT ? K_CNOT : K_CZ;
+                l.b0 = perm[n - 1 - g.q0];
+                l.b1 = perm[n - 1 - g.q1];
                 break;
             case QG_GATE_EMBED: {
                 if (i != start) break;
@@ -646,6 +657,17 @@ static int build_program(Program& P, const qg_gate* gates, int ngates, const int
                 return set_error("unknown gate kind"), QG_EINVAL;
         }
         P.gates.push_back(l);
+    }
+    for (int b = 0; b < n; ++b) {
+        if (perm[b] == b) continue;
+        int c = 0;
+        while (perm[c] != b) ++c;  // the reference bit now stored at bit b
+        LGate l;
+        l.kind = K_SWAP;
+        l.b0 = perm[b];
+        l.b1 = b;
+        P.gates.push_back(l);
+        std::swap(perm[b], perm[c]);
     }
     return QG_OK;
 }

@@ -61,6 +61,17 @@ class Circuit(torch.nn.Module):
             self._executor = _engine.FusedExecutor(self.circuit, **self._engine_options)
         return self._executor(state, **kwargs)
 
+    def tune(self, batch: int, device="cuda", **kwargs) -> dict:
+        """Pick the fused engine's plan options for this circuit at `batch`
+        by timing candidates on `device` (qandle_gb300.tune.autotune; the
+        answer is cached on disk) and use them from the next call on."""
+        from . import tune as _tune
+
+        res = _tune.autotune(self, batch, device, **kwargs)
+        self._engine_options = dict(self._engine_options, **res["options"])
+        self._executor = None
+        return res
+
     def to_matrix(self, **kwargs):
         return self.circuit.to_matrix(**kwargs)
 

@@ -1,0 +1,132 @@
+"""Autotuner for the fused engine's plan options.
+
+The best tile shape depends on the circuit and the batch: a 2^13 tile holds
+more qubits per pass (fewer HBM round trips), a 2^12 tile runs two CTAs per
+SM, longer contiguous runs (``low_bits``) make the loads denser but leave
+fewer tile slots for strided qubits, and 16 instead of 32 amplitudes per
+thread trade exchanges for occupancy.  ``autotune`` plans and runs each
+candidate on the device with the circuit's own structure at the given batch,
+times its forward with CUDA events, and returns the fastest option set.
+Results are kept in a JSON file keyed by the circuit's gate structure (gate
+kinds and qubits, not angles), the batch, the device and whether passes are
+compiled, so a later process gets the answer without running anything.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import threading
+import typing
+
+import torch
+
+from . import engine
+
+DEFAULT_CANDIDATES: typing.List[dict] = [
+    dict(tile_bits=13, low_bits=6, reg_bits=5),
+    dict(tile_bits=12, low_bits=6, reg_bits=5),
+    dict(tile_bits=12, low_bits=7, reg_bits=5),
+    dict(tile_bits=13, low_bits=7, reg_bits=5),
+    dict(tile_bits=12, low_bits=6, reg_bits=4),
+]
+
+_lock = threading.Lock()
+
+
+def default_cache_path() -> str:
+    env = os.environ.get("QG_TUNE_CACHE")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "tune_cache.json")
+
+
+def structure_key(lowered: "engine.Lowered") -> str:
+    """Hash of what the plan depends on: width, measurement, and per gate its
+    kind, qubits and whether its angle is per sample.  Angle values and
+    matrix entries do not change the plan."""
+    h = hashlib.sha256()
+    h.update(f"n={lowered.n};m={lowered.measure};".encode())
+    for g in lowered.gates:  # (kind, q0, q1, src, idx, aux); aux marks diagonal U
+        kind, q0, q1, src, aux = g[0], g[1], g[2], g[3], g[5]
+        h.update(f"{kind},{q0},{q1},{src},{aux};".encode())
+    h.update(("q" + ",".join(str(q) for q in lowered.qlist)).encode())
+    return h.hexdigest()[:32]
+
+
+def _key(lowered, batch: int, device, compiled: bool) -> str:
+    name = torch.cuda.get_device_name(device) if torch.cuda.is_available() else "cpu"
+    return f"{structure_key(lowered)}|B={batch}|{name}|{'compiled' if compiled else 'interpreted'}"
+
+
+def _load(path: str) -> dict:
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(path: str, key: str, entry: dict) -> None:
+    with _lock:
+        data = _load(path)
+        data[key] = entry
+        os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+        tmp = f"{path}.tmp{os.getpid()}"
+        with open(tmp, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+
+
+def time_candidate(circuit, batch: int, device, options: dict, reps: int = 3, compiled: bool = True) -> float:
+    """Milliseconds of one forward of `circuit` at `batch` with the plan
+    `options` (inputs resident on the device, after one warm-up).  Angles,
+    matrices and named inputs stay zero: the kernels' work does not depend on
+    their values."""
+    ex = engine.FusedExecutor(circuit, compiled=compiled, **options)
+    bound = engine.BoundForward(ex, batch, device)
+    bound.launch()
+    torch.cuda.synchronize(device)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        bound.launch()
+    e1.record()
+    torch.cuda.synchronize(device)
+    return e0.elapsed_time(e1) / reps
+
+
+def autotune(circuit, batch: int, device="cuda", candidates: typing.Optional[typing.List[dict]] = None,
+             cache_path: typing.Optional[str] = None, reps: int = 3, compiled: bool = True,
+             timer: typing.Optional[typing.Callable[[dict], float]] = None) -> dict:
+    """Fastest plan options for `circuit` (a qandle_gb300.Circuit or its
+    built UnsplittedCircuit) at `batch` on `device`.
+
+    Returns {"options": {...}, "ms": best time, "timings": [(options, ms)],
+    "cached": bool}.  Candidates that the planner rejects for this circuit
+    are skipped.  `timer` replaces the device timing (tests)."""
+    built = getattr(circuit, "circuit", circuit)
+    if built.num_qubits < 5:  # runs on the per-gate kernels: nothing to tune
+        return {"options": {}, "ms": None, "timings": [], "cached": False}
+    lowered = engine.lower(built)
+    device = torch.device(device)
+    path = cache_path or default_cache_path()
+    key = _key(lowered, batch, device, compiled)
+    hit = _load(path).get(key)
+    if hit is not None:
+        return dict(hit, cached=True)
+    cands = candidates or DEFAULT_CANDIDATES
+    timings = []
+    for opt in cands:
+        try:
+            ms = timer(opt) if timer is not None else time_candidate(built, batch, device, opt, reps, compiled)
+        except RuntimeError:
+            continue
+        timings.append((dict(opt), float(ms)))
+    if not timings:
+        raise RuntimeError("no candidate plan could be run for this circuit")
+    best = min(timings, key=lambda t: t[1])
+    entry = {"options": best[0], "ms": best[1], "timings": timings}
+    _store(path, key, entry)
+    return dict(entry, cached=False)

@@ -194,3 +194,39 @@ def test_fused_matches_plain(cuda_device):
     a = _run(desc, cuda_device, engine="fused")
     b = _run(desc, cuda_device, engine="plain")
     assert np.abs(a - b).max() < TOL
+
+
+def test_deep_28_qubits(cuda_device):
+    """The 28-qubit, batch-1 deep circuit (50 layers of U with CNOT+SWAP
+    brickwork, 2 GiB state): the full run keeps the norm and agrees with the
+    per-gate form; the same circuit restricted to qubits 0..19 matches the
+    complex128 oracle."""
+    desc = workloads.deep_u(n=28, batch=1, layers=50)
+    circ = workloads.build_circuit(desc, engine="fused").to(cuda_device)
+    with torch.no_grad():
+        probs = circ().reshape(-1)
+    assert abs(float(probs.double().sum()) - 1.0) < 1e-4
+    circ_p = workloads.build_circuit(desc, engine="plain").to(cuda_device)
+    with torch.no_grad():
+        probs_p = circ_p().reshape(-1)
+    assert float((probs - probs_p).abs().max()) < TOL
+    del probs, probs_p
+    pre = workloads.restrict(desc, 20)
+    out = _run(pre, cuda_device)
+    ref = oracle.forward(pre)
+    if out.shape == ref.shape[1:]:
+        ref = ref[0]
+    assert np.abs(out - ref).max() < TOL
+
+
+def test_autotune_on_device(cuda_device, tmp_path):
+    """Circuit.tune times real candidate plans, keeps the fastest, and the
+    tuned circuit still matches the oracle."""
+    desc = workloads.sel_reupload(n=14, batch=8, layers=2, reupload_every=2)
+    circ = workloads.build_circuit(desc, engine="fused").to(cuda_device)
+    cands = [dict(tile_bits=13, low_bits=6), dict(tile_bits=12, low_bits=6)]
+    res = circ.tune(8, cuda_device, candidates=cands, cache_path=str(tmp_path / "tune.json"))
+    assert res["options"] in cands and res["ms"] > 0 and len(res["timings"]) == 2
+    with torch.no_grad():
+        out = circ(**workloads.circuit_inputs(desc, cuda_device)).cpu().numpy()
+    assert np.abs(out - oracle.forward(desc)).max() < TOL
