@@ -212,24 +212,30 @@ int qg_program_grad_targets(const qg_program* prog, int32_t* out, int64_t cap);
  * caller copies them to device memory once and passes that pointer below. */
 int qg_program_table(const qg_program* prog, void* host_out, int64_t bytes);
 
-/* Compile the forward passes of `prog` for the current device: each pass's op
- * list is unrolled into its own kernel (NVRTC, sm_103a).  Afterwards
- * qg_program_forward / qg_program_forward_timed on this device launch the
- * compiled kernels instead of the op interpreter; results agree with the
- * interpreter within float rounding.  Identical passes compile once per
+/* Compile the passes of `prog` for the current device: each pass's op list is
+ * unrolled into its own kernel (NVRTC, sm_103a).  Afterwards
+ * qg_program_forward / qg_program_forward_timed (and qg_program_backward,
+ * with QG_COMPILE_BACKWARD) on this device launch the compiled kernels
+ * instead of the op interpreter; results agree with the interpreter within
+ * float rounding.  Identical passes compile once per
  * process.  Returns QG_ECUDA with the compiler log in qg_last_error() when
  * NVRTC is missing or fails; the interpreter then stays in use.  No
  * counterpart in the reference, whose layers run one dense matmul each
  * (qandle/qcircuit.py:163-174). */
 int qg_program_compile(qg_program* prog, int flags);
 /* flags: QG_COMPILE_NO_LOAD compiles every pass and discards the result (no
- * device needed: a host-side check that the program's kernels build). */
+ * device needed: a host-side check that the program's kernels build);
+ * QG_COMPILE_BACKWARD also compiles the backward passes, which
+ * qg_program_backward then launches. */
 #define QG_COMPILE_NO_LOAD 1
-/* 1 if compiled forward kernels are active for `prog` on the current device. */
+#define QG_COMPILE_BACKWARD 2
+/* 0: nothing compiled for `prog` on the current device; 1: forward passes;
+ * 3: forward and backward passes. */
 int qg_program_compiled(const qg_program* prog);
-/* The CUDA source of compiled forward pass `pass` (NUL-terminated) into
- * host_out; returns the bytes needed including the NUL, or -1. */
-int64_t qg_program_pass_source(const qg_program* prog, int pass, char* host_out, int64_t bytes);
+/* The CUDA source of compiled forward (backward = 0) or backward pass `pass`
+ * (NUL-terminated) into host_out; returns the bytes needed including the
+ * NUL, or -1. */
+int64_t qg_program_pass_source(const qg_program* prog, int backward, int pass, char* host_out, int64_t bytes);
 
 /* Workspace bytes for a forward (backward = 0) or backward run at `batch`. */
 int64_t qg_program_workspace_bytes(const qg_program* prog, int64_t batch, int backward);

@@ -92,7 +92,7 @@ SIGNATURES = {
     "qg_program_destroy": (None, [c_void_p]),
     "qg_program_compile": (c_int, [c_void_p, c_int]),
     "qg_program_compiled": (c_int, [c_void_p]),
-    "qg_program_pass_source": (c_int64, [c_void_p, c_int, c_void_p, c_int64]),
+    "qg_program_pass_source": (c_int64, [c_void_p, c_int, c_int, c_void_p, c_int64]),
     "qg_program_info": (c_int, [c_void_p, ctypes.POINTER(ProgramInfo)]),
     "qg_program_pass": (c_int, [c_void_p, c_int, c_int, ctypes.POINTER(PassInfo)]),
     "qg_program_table": (c_int, [c_void_p, c_void_p, c_int64]),

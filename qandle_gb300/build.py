@@ -40,7 +40,7 @@ def _sources():
 
 # Headers the run-time compiler (csrc/jit.cpp) needs, embedded in the library
 # so that it does not depend on the source tree at run time.
-JIT_HEADERS = ["devmath.cuh", "engine.h", "planar.cuh", "fwd_kernel.cuh", "jit_ops.cuh"]
+JIT_HEADERS = ["devmath.cuh", "engine.h", "planar.cuh", "fwd_kernel.cuh", "bwd_kernel.cuh", "jit_ops.cuh"]
 
 
 def _write_jit_headers() -> str:

@@ -122,6 +122,13 @@ __host__ __device__ constexpr int fwd_smem_bytes(int tb) {
     return fwd_stages(tb) * (1 << tb) * 8 + kSmemOps * 16 + kSmemMats * 32;
 }
 
+// Dynamic shared memory of the backward kernel: psi and lambda double
+// buffers, the op list, the shared matrix table, the gradient partials and
+// their sample tags.
+__host__ __device__ constexpr int bwd_smem_bytes(int tb, int rb) {
+    return 4 * (1 << tb) * 8 + kSmemOps * 16 + kSmemMats * 32 + max_grad_per_pass(rb) * (1 << (tb - rb)) * 5;
+}
+
 #ifndef __CUDACC_RTC__
 // Host view of a planned program, for the launch code in fused.cu.
 struct ProgramRun {

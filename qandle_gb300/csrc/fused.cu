@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "engine.h"
+#include "bwd_kernel.cuh"
 #include "fwd_kernel.cuh"
 #include "jit.h"
 #include "planar.cuh"
@@ -222,129 +223,43 @@ __global__ void __launch_bounds__(1 << (TB - RB), fwd_min_blocks(TB, RB))
     fwd_pass_body<TB, RB, MAXJ, InterpOps>(jt);
 }
 
-// Backward pass kernel: psi and lambda tiles (TB = 12), gradient partials.
+// Gate program of a backward pass read from the pass's op list at run time.
+struct BwdInterpOps {
+    static constexpr bool kStageOps = true;
+    template <int TB, int RB>
+    __device__ __forceinline__ static void apply(PTile<RB>& pt, PTile<RB>& lt, uint32_t& xm, ThreadMap& tm,
+                                                 const PassDesc& d, const RunArgs& A, const int4* ops,
+                                                 const int4* s_ops, const float4* s_mats, float* pp, float* lp,
+                                                 int64_t sample0, uint32_t fixed_val, int tid, float* gacc,
+                                                 uint8_t* gsmp) {
+        constexpr int NT = 1 << (TB - RB);
+        PTile<RB>* const tiles[2] = {&pt, &lt};
+        for (int o = 0; o < d.op_count; ++o) {
+            int4 op = o < kSmemOps ? s_ops[o] : __ldg(ops + o);
+            if (op.x == OP_MAP) {
+                exchange2<TB, RB>(pt, lt, xm, tm, pp, lp, d, op.y, op.z, op.w, tid, fixed_val);
+            } else if (op.x == OP_GRAD) {
+                grad_record<NT>(gacc, gsmp, op.w - d.grad_base, tid, pgrad_op<RB>(pt, lt, op.y, op.z, xm),
+                                tm.sample_off);
+            } else if (op.x == OP_MAT && (op.w & OPF_GRAD)) {
+                const int axis = (op.w >> 8) & 3;
+                const int gslot = op.w >> 12;
+                grad_record<NT>(gacc, gsmp, gslot - d.grad_base, tid, pgrad_op<RB>(pt, lt, op.y, axis, xm),
+                                tm.sample_off);
+                papply_op<RB, 2>(make_int4(OP_MAT, op.y, op.z, op.w), tiles, xm, tm, A, s_mats,
+                                 sample0 + tm.sample_off);
+            } else {
+                papply_op<RB, 2>(op, tiles, xm, tm, A, s_mats, sample0 + tm.sample_off);
+            }
+        }
+    }
+};
+
 template <int TB, int RB>
 __global__ void __launch_bounds__(1 << (TB - RB), 1)
     k_bwd_pass(const PassDesc* __restrict__ passes, const int4* __restrict__ ops_all, int pass_index, RunArgs A,
                int store_lam_last, int64_t num_tiles) {
-    constexpr int NT = 1 << (TB - RB);
-    constexpr int AMPS = 1 << TB;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    float2* pbuf0 = reinterpret_cast<float2*>(smem_raw);  // psi, lambda, psi, lambda
-    int4* s_ops = reinterpret_cast<int4*>(pbuf0 + 4 * AMPS);         // [kSmemOps]
-    float4* s_mats = reinterpret_cast<float4*>(s_ops + kSmemOps);     // [kSmemMats][2]
-    float* gacc = reinterpret_cast<float*>(s_mats + 2 * kSmemMats);  // [ngrad][NT]
-    // sample (within the tile) each partial belongs to: the thread's sample
-    // bits depend on the mapping in force when the gradient op ran
-    uint8_t* gsmp = reinterpret_cast<uint8_t*>(gacc + max_grad_per_pass(RB) * NT);  // [ngrad][NT]
-    __shared__ PassDesc sd;
-
-    const int tid = threadIdx.x;
-    if (tid == 0) sd = passes[pass_index];
-    __syncthreads();
-    const PassDesc& d = sd;
-    const int4* ops = ops_all + d.op_begin;
-    for (int i = tid; i < d.op_count && i < kSmemOps; i += NT) s_ops[i] = __ldg(ops + i);
-    {
-        const int nm = A.nslots_shared < kSmemMats ? A.nslots_shared : kSmemMats;
-        const float4* gm = reinterpret_cast<const float4*>(A.mats);
-        for (int i = tid; i < 2 * nm; i += NT) s_mats[i] = __ldg(gm + i);
-    }
-    const int n = A.n;
-    const float2* psi_src = d.psi_from_ckpt >= 0 ? A.ckpt + (int64_t)d.psi_from_ckpt * (A.batch << n) : A.state;
-    const bool last = (d.epi & EPI_STORE) == 0;  // final backward pass: nothing to store but lambda
-    (void)last;
-
-    __syncthreads();
-    // psi and lambda of a tile arrive as one cp.async group per thread; every
-    // thread commits one group per tile (empty past the last tile), so
-    // "tile t has landed" is wait_group 0 before the next commit + a barrier
-    auto prefetch = [&](int64_t t, float2* dst) {
-        if (t < num_tiles) {
-            TileGeo gn = tile_geo(d, t, n, A.batch);
-            thread_tile_load<TB, RB>(d, gn, psi_src, dst, n, tid);
-            thread_tile_load<TB, RB>(d, gn, A.lam, dst + AMPS, n, tid);
-        }
-        cp_async_commit();
-    };
-    int64_t t0 = blockIdx.x;
-    prefetch(t0, pbuf0);
-    int iter = 0;
-    for (int64_t t = t0; t < num_tiles; t += gridDim.x, ++iter) {
-        float2* ps = pbuf0 + (iter & 1) * 2 * AMPS;
-        float2* ls = ps + AMPS;
-        float2* nps = pbuf0 + ((iter + 1) & 1) * 2 * AMPS;
-        TileGeo g = tile_geo(d, t, n, A.batch);
-        PTile<RB> pt, lt;
-        PTile<RB>* const tiles[2] = {&pt, &lt};
-        uint32_t xm = 0;  // pending thread-controlled X, shared by psi and lambda
-        ThreadMap tm;
-        cp_async_wait<0>();
-        __syncthreads();
-        pload_nat<RB>(pt, ps, tid);
-        pload_nat<RB>(lt, ls, tid);
-        decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
-        // the other buffer pair held tile t - 1, whose end waited for every read
-        prefetch(t + gridDim.x, nps);
-        for (int o = 0; o < d.op_count; ++o) {
-            int4 op = o < kSmemOps ? s_ops[o] : __ldg(ops + o);
-            if (op.x == OP_MAP) {
-                __syncthreads();
-                const int base = tm.sw_base ^ xm_slot_offset<RB>(tm, xm);
-                pxwrite_k<RB>(reinterpret_cast<float*>(ps), pt, tm, base, AMPS);
-                pxwrite_k<RB>(reinterpret_cast<float*>(ls), lt, tm, base, AMPS);
-                xm = 0;
-                __syncthreads();
-                decode_map<RB>(d, op.y, op.z, op.w, tid, g.fixed_val, tm);
-                pxread_k<RB>(reinterpret_cast<const float*>(ps), pt, tm, AMPS);
-                pxread_k<RB>(reinterpret_cast<const float*>(ls), lt, tm, AMPS);
-            } else if (op.x == OP_GRAD) {
-                float gsum = pgrad_op<RB>(pt, lt, op.y, op.z, xm);
-                gacc[(op.w - d.grad_base) * NT + tid] = gsum;
-                gsmp[(op.w - d.grad_base) * NT + tid] = (uint8_t)tm.sample_off;
-            } else if (op.x == OP_MAT && (op.w & OPF_GRAD)) {
-                int axis = (op.w >> 8) & 3;
-                int gslot = op.w >> 12;
-                float gsum = pgrad_op<RB>(pt, lt, op.y, axis, xm);
-                gacc[(gslot - d.grad_base) * NT + tid] = gsum;
-                gsmp[(gslot - d.grad_base) * NT + tid] = (uint8_t)tm.sample_off;
-                papply_op<RB, 2>(make_int4(OP_MAT, op.y, op.z, op.w), tiles, xm, tm, A, s_mats,
-                                 g.sample + tm.sample_off);
-            } else {
-                papply_op<RB, 2>(op, tiles, xm, tm, A, s_mats, g.sample + tm.sample_off);
-            }
-        }
-        __syncthreads();
-        // gradient partials of this tile: per sample when samples share the tile
-        if (d.ngrad > 0) {
-            const int nq = d.nq_tile;
-            const int spt = (nq < TB) ? (1 << (TB - nq)) : 1;
-            const int64_t tps = (n >= TB) ? (int64_t(1) << (n - TB)) : 1;
-            const int64_t units = (n >= TB) ? A.batch * tps : A.batch;
-            const int items = d.ngrad * spt;
-            const int warp = tid >> 5, lane = tid & 31;
-            for (int it = warp; it < items; it += NT / 32) {
-                int gi = it / spt, s = it % spt;
-                float acc = 0.f;
-                for (int c = lane; c < NT; c += 32)
-                    if (gsmp[gi * NT + c] == s) acc += gacc[gi * NT + c];
-                for (int o2 = 16; o2 > 0; o2 >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o2);
-                if (lane == 0 && s < g.nsamples) {
-                    int64_t unit = (n >= TB) ? (g.sample * tps + g.tile_in_sample) : (g.sample + s);
-                    A.gradpart[(int64_t)(d.grad_base + gi) * units + unit] = acc;
-                }
-            }
-        }
-        // store psi and lambda (natural mapping) straight from registers
-        if (d.epi & EPI_STORE) {
-            pstore_global<RB>(pt, xm, d, g, A.state, n, tid);
-            pstore_global<RB>(lt, xm, d, g, A.lam, n, tid);
-        } else if (store_lam_last) {
-            pstore_global<RB>(lt, xm, d, g, A.lam, n, tid);
-        }
-        __syncthreads();  // `ps` / `ls` are free for the prefetch two tiles ahead
-    }
-    cp_async_wait<0>();
+    bwd_pass_body<TB, RB, BwdInterpOps>(passes, ops_all, pass_index, A, store_lam_last, num_tiles);
 }
 
 // ------------------------------------------------------------ helpers --
@@ -664,8 +579,7 @@ template <int TB, int RB>
 static int launch_bwd_pass(const PassDesc* dpass, const int4* dops, int p, const RunArgs& A, int store_lam,
                            int64_t tiles, cudaStream_t st) {
     constexpr int NT = 1 << (TB - RB);
-    size_t smem = 4 * (size_t(1) << TB) * sizeof(float2) + kSmemOps * sizeof(int4) + kSmemMats * 2 * sizeof(float4) +
-                  (size_t)max_grad_per_pass(RB) * NT * (sizeof(float) + 1);
+    size_t smem = bwd_smem_bytes(TB, RB);
     static bool attr_set = false;
     if (!attr_set) {
         QG_CUDA_TRY(cudaFuncSetAttribute(k_bwd_pass<TB, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -681,6 +595,20 @@ static int launch_bwd_pass(const PassDesc* dpass, const int4* dops, int p, const
     k_bwd_pass<TB, RB><<<(unsigned)grid, NT, smem, st>>>(dpass, dops, p, A, store_lam, tiles);
     QG_LAUNCH_CHECK();
     return QG_OK;
+}
+
+// Launch of a backward pass kernel compiled for this program (jit.cpp).
+static int launch_bwd_compiled(const JitKernel& k, const PassDesc* dpass, const int4* dops, int p, const RunArgs& A,
+                               int store_lam, int64_t tiles, int tb, cudaStream_t st) {
+    if (tiles <= 0) return QG_OK;
+    const int rb = kBwdRegBits;
+    int64_t slots = (int64_t)sm_count() * k.per_sm;
+    int64_t grid = tiles < slots ? tiles : slots;
+    RunArgs a = A;
+    int pass = p, sl = store_lam;
+    int64_t nt = tiles;
+    void* params[] = {(void*)&dpass, (void*)&dops, &pass, &a, &sl, &nt};
+    return jit_launch(k, (unsigned)grid, 1u << (tb - rb), (size_t)bwd_smem_bytes(tb, rb), st, params);
 }
 
 static int launch_bwd(const PassDesc* dpass, const int4* dops, int p, const RunArgs& A, int store_lam,
@@ -914,7 +842,10 @@ int qg_program_backward(const qg_program* prog, const void* dev_table, void* wor
     int64_t tiles = num_tiles(R.n, tb, batch);
     for (int p = 0; p < R.nbpass; ++p) {
         int store_lam = (p + 1 == R.nbpass) && dstate != nullptr;
-        int rc = launch_bwd(dpass, dops, p, A, store_lam, tiles, tb, kBwdRegBits, st);
+        JitKernel jk;
+        int rc = jit_backward_kernel(prog, p, &jk)
+                     ? launch_bwd_compiled(jk, dpass, dops, p, A, store_lam, tiles, tb, st)
+                     : launch_bwd(dpass, dops, p, A, store_lam, tiles, tb, kBwdRegBits, st);
         if (rc) return rc;
     }
     int64_t fitems = R.nparams + (int64_t)R.ncols * batch;

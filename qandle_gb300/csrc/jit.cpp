@@ -275,6 +275,91 @@ std::string pass_source(const ProgramRun& R, int p) {
     return s.str();
 }
 
+// One backward pass as CUDA source: the shared backward body with the pass's
+// ops unrolled on psi and lambda, gradient partials at compile-time slots.
+std::string bwd_pass_source(const ProgramRun& R, int p) {
+    const PassDesc& d = R.bpass[p];
+    const int tb = d.tile_bits, rb = kBwdRegBits;
+    const int nt = 1 << (tb - rb);
+    const int32_t* ops = R.bops + 4 * (size_t)d.op_begin;
+    std::ostringstream s;
+    s << "#include \"jit_ops.cuh\"\n"
+         "namespace qg {\n"
+         "struct BwdPassOps {\n"
+         "  static constexpr bool kStageOps = false;\n"
+         "  template <int TB, int RB>\n"
+         "  __device__ __forceinline__ static void apply(PTile<RB>& pt, PTile<RB>& lt, uint32_t& xm, ThreadMap& tm, "
+         "const PassDesc& d, const RunArgs& A, const int4*, const int4*, const float4* s_mats, float* pp, float* lp, "
+         "int64_t sample0, uint32_t fixed_val, int tid, float* gacc, uint8_t* gsmp) {\n"
+         "    constexpr int NT = 1 << (TB - RB);\n";
+    for (int o = 0; o < d.op_count; ++o) {
+        const int32_t k = ops[4 * o], y = ops[4 * o + 1], z = ops[4 * o + 2], w = ops[4 * o + 3];
+        const std::string smp = "sample0 + tm.sample_off";
+        s << "    ";
+        switch (k) {
+            case OP_MAP:
+                s << "exchange2<TB, RB>(pt, lt, xm, tm, pp, lp, d, " << y << ", " << z << ", " << w
+                  << ", tid, fixed_val);\n";
+                break;
+            case OP_GRAD:
+                s << "jgrad<" << y << ", RB, NT>(pt, lt, xm, " << z << ", gacc, gsmp, " << (w - d.grad_base)
+                  << ", tid, tm.sample_off);\n";
+                break;
+            case OP_MAT:
+                if (w & OPF_GRAD)
+                    s << "jgrad<" << y << ", RB, NT>(pt, lt, xm, " << ((w >> 8) & 3) << ", gacc, gsmp, "
+                      << ((w >> 12) - d.grad_base) << ", tid, tm.sample_off); ";
+                s << "jmat2<" << y << ", RB>(pt, lt, xm, A, s_mats, " << z << ", " << w << ", " << smp << ");\n";
+                break;
+            case OP_DIAG:
+                if (y & LOC_REG)
+                    s << "jdiag2<" << (y & 7) << ", RB>(pt, lt, xm, A, s_mats, " << z << ", " << w << ", " << smp
+                      << ");\n";
+                else
+                    s << "jdiag_thread2<RB>(pt, lt, " << loc_bit(y) << ", A, s_mats, " << z << ", " << w << ", "
+                      << smp << ");\n";
+                break;
+            case OP_CX:
+                if (z & LOC_REG)
+                    s << "jcx2<" << y << ", " << (z & 7) << ", RB>(pt, lt, xm);\n";
+                else
+                    s << "xm ^= (uint32_t)" << loc_bit(z) << " << " << y << ";\n";
+                break;
+            case OP_CZ: {
+                int mask = 0;
+                std::string cond;
+                for (int32_t loc : {y, z}) {
+                    if (loc & LOC_REG) {
+                        s << "jmaterialize2<" << (loc & 7) << ", RB>(pt, lt, xm); ";
+                        mask |= 1 << (loc & 7);
+                    } else {
+                        cond += (cond.empty() ? "" : " && ") + loc_bit(loc);
+                    }
+                }
+                if (cond.empty())
+                    s << "jnegate2<" << mask << ", RB>(pt, lt);\n";
+                else
+                    s << "jnegate_if2<" << mask << ", RB>(pt, lt, " << cond << ");\n";
+                break;
+            }
+            case OP_SWAP:
+                if (y != z) s << "jswap2<" << y << ", " << z << ", RB>(pt, lt, xm);\n";
+                else s << "\n";
+                break;
+            default:
+                s << "// op " << k << " has no backward form\n";
+                break;
+        }
+    }
+    s << "  }\n};\n}  // namespace qg\n"
+      << "extern \"C\" __global__ void __launch_bounds__(" << nt << ", 1)\n"
+      << "qg_bwd_pass(const qg::PassDesc* __restrict__ passes, const int4* __restrict__ ops_all, int pass_index, "
+         "qg::RunArgs A, int store_lam_last, int64_t num_tiles) {\n"
+      << "  qg::bwd_pass_body<" << tb << ", " << rb << ", qg::BwdPassOps>(passes, ops_all, pass_index, A, "
+         "store_lam_last, num_tiles);\n}\n";
+    return s.str();
+}
+
 // ------------------------------------------------- compile and cache --
 
 struct Loaded {
@@ -372,7 +457,8 @@ int compile_source(const std::string& src, std::vector<char>& cubin, std::string
     return QG_OK;
 }
 
-int load_cubin(const std::vector<char>& cubin, int tb, int rb, Loaded& out, std::string& err) {
+int load_cubin(const std::vector<char>& cubin, const char* fname, int smem, int threads, Loaded& out,
+               std::string& err) {
     const Driver& D = driver();
     CUresult r = D.load(&out.mod, cubin.data());
     if (r != CUDA_SUCCESS) {
@@ -380,19 +466,18 @@ int load_cubin(const std::vector<char>& cubin, int tb, int rb, Loaded& out, std:
         return QG_ECUDA;
     }
     CUfunction f = nullptr;
-    r = D.get_function(&f, out.mod, "qg_fwd_pass");
+    r = D.get_function(&f, out.mod, fname);
     if (r != CUDA_SUCCESS) {
         err = "cuModuleGetFunction: " + cu_error(r);
         return QG_ECUDA;
     }
-    const int smem = fwd_smem_bytes(tb);
     r = D.set_attribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, smem);
     if (r != CUDA_SUCCESS) {
         err = "cuFuncSetAttribute: " + cu_error(r);
         return QG_ECUDA;
     }
     int per_sm = 0;
-    r = D.occupancy(&per_sm, f, 1 << (tb - rb), (size_t)smem);
+    r = D.occupancy(&per_sm, f, threads, (size_t)smem);
     if (r != CUDA_SUCCESS) {
         err = "cuOccupancyMaxActiveBlocksPerMultiprocessor: " + cu_error(r);
         return QG_ECUDA;
@@ -405,22 +490,26 @@ int load_cubin(const std::vector<char>& cubin, int tb, int rb, Loaded& out, std:
 // Per-program state: the compiled kernel of every forward pass, per device.
 struct ProgramJit {
     std::mutex mu;
-    std::map<int, std::vector<JitKernel>> fwd;  // device -> kernel per pass
+    std::map<int, std::vector<JitKernel>> fwd, bwd;  // device -> kernel per pass
 };
 
 }  // namespace
 
-bool jit_forward_kernel(const void* prog, int pass, JitKernel* out) {
+static bool jit_kernel(const void* prog, bool backward, int pass, JitKernel* out) {
     ProgramJit* st = (ProgramJit*)program_jit_state(prog);
     if (!st) return false;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
     std::lock_guard<std::mutex> lk(st->mu);
-    auto it = st->fwd.find(dev);
-    if (it == st->fwd.end() || pass < 0 || pass >= (int)it->second.size()) return false;
+    const auto& m = backward ? st->bwd : st->fwd;
+    auto it = m.find(dev);
+    if (it == m.end() || pass < 0 || pass >= (int)it->second.size()) return false;
     *out = it->second[pass];
     return out->fn != nullptr;
 }
+
+bool jit_forward_kernel(const void* prog, int pass, JitKernel* out) { return jit_kernel(prog, false, pass, out); }
+bool jit_backward_kernel(const void* prog, int pass, JitKernel* out) { return jit_kernel(prog, true, pass, out); }
 
 int jit_launch(const JitKernel& k, unsigned grid, unsigned block, size_t smem, void* stream, void** params) {
     CUresult r = driver().launch((CUfunction)k.fn, grid, 1, 1, block, 1, 1, (unsigned)smem, (CUstream)stream,
@@ -442,6 +531,7 @@ int qg_program_compile(qg_program* prog, int flags) {
     using namespace qg;
     if (!prog) return set_error("qg_program_compile: null pointer"), QG_EINVAL;
     const bool load = !(flags & QG_COMPILE_NO_LOAD);
+    const bool with_bwd = (flags & QG_COMPILE_BACKWARD) != 0;
     const Nvrtc& N = nvrtc();
     if (!N.why.empty()) return set_error("qg_program_compile: " + N.why), QG_ECUDA;
     int dev = -1;
@@ -455,20 +545,31 @@ int qg_program_compile(qg_program* prog, int flags) {
     if (R.reg_bits != 4 && R.reg_bits != 5)
         return set_error("qg_program_compile: reg_bits must be 4 or 5"), QG_EINVAL;
 
-    std::vector<std::string> srcs(R.nfpass);
-    for (int p = 0; p < R.nfpass; ++p) srcs[p] = pass_source(R, p);
+    // one task per pass: forward passes, then (optionally) backward passes
+    struct Task {
+        bool bwd;
+        int pass;
+        std::string src;
+    };
+    std::vector<Task> tasks;
+    for (int p = 0; p < R.nfpass; ++p) tasks.push_back({false, p, pass_source(R, p)});
+    if (with_bwd)
+        for (int p = 0; p < R.nbpass; ++p) tasks.push_back({true, p, bwd_pass_source(R, p)});
+    auto name = [](const Task& t) {
+        return std::string(t.bwd ? "backward pass " : "pass ") + std::to_string(t.pass);
+    };
 
-    // passes not yet in the process-wide cache compile in parallel
-    std::vector<JitKernel> kernels(R.nfpass);
-    std::vector<int> todo;
+    // tasks not yet in the process-wide cache compile in parallel
+    std::vector<JitKernel> kernels(tasks.size());
+    std::vector<size_t> todo;
     {
         std::lock_guard<std::mutex> lk(g_cache_mu);
-        for (int p = 0; p < R.nfpass; ++p) {
-            auto it = g_cache.find({dev, srcs[p]});
+        for (size_t i = 0; i < tasks.size(); ++i) {
+            auto it = g_cache.find({dev, tasks[i].src});
             if (it != g_cache.end())
-                kernels[p] = it->second.k;
+                kernels[i] = it->second.k;
             else
-                todo.push_back(p);
+                todo.push_back(i);
         }
     }
     std::vector<std::vector<char>> cubins(todo.size());
@@ -489,27 +590,30 @@ int qg_program_compile(qg_program* prog, int flags) {
                         if (next >= todo.size()) return;
                         i = next++;
                     }
-                    rcs[i] = compile_source(srcs[todo[i]], cubins[i], errs[i]);
+                    rcs[i] = compile_source(tasks[todo[i]].src, cubins[i], errs[i]);
                 }
             });
         for (auto& th : pool) th.join();
     }
     for (size_t i = 0; i < todo.size(); ++i)
-        if (rcs[i]) return set_error("qg_program_compile: pass " + std::to_string(todo[i]) + ": " + errs[i]), rcs[i];
+        if (rcs[i]) return set_error("qg_program_compile: " + name(tasks[todo[i]]) + ": " + errs[i]), rcs[i];
     if (!load) return QG_OK;
     {
         std::lock_guard<std::mutex> lk(g_cache_mu);
         for (size_t i = 0; i < todo.size(); ++i) {
-            const int p = todo[i];
-            auto it = g_cache.find({dev, srcs[p]});
+            const Task& t = tasks[todo[i]];
+            auto it = g_cache.find({dev, t.src});
             if (it == g_cache.end()) {
                 Loaded L;
                 std::string err;
-                int rc = load_cubin(cubins[i], R.fpass[p].tile_bits, R.reg_bits, L, err);
-                if (rc) return set_error("qg_program_compile: pass " + std::to_string(p) + ": " + err), rc;
-                it = g_cache.emplace(std::make_pair(dev, srcs[p]), L).first;
+                const int tb = t.bwd ? R.bpass[t.pass].tile_bits : R.fpass[t.pass].tile_bits;
+                const int rb = t.bwd ? kBwdRegBits : R.reg_bits;
+                const int smem = t.bwd ? bwd_smem_bytes(tb, rb) : fwd_smem_bytes(tb);
+                int rc = load_cubin(cubins[i], t.bwd ? "qg_bwd_pass" : "qg_fwd_pass", smem, 1 << (tb - rb), L, err);
+                if (rc) return set_error("qg_program_compile: " + name(t) + ": " + err), rc;
+                it = g_cache.emplace(std::make_pair(dev, t.src), L).first;
             }
-            kernels[p] = it->second.k;
+            kernels[todo[i]] = it->second.k;
         }
     }
     ProgramJit* st;
@@ -522,17 +626,18 @@ int qg_program_compile(qg_program* prog, int flags) {
         }
     }
     std::lock_guard<std::mutex> lk(st->mu);
-    st->fwd[dev] = kernels;
+    st->fwd[dev] = std::vector<JitKernel>(kernels.begin(), kernels.begin() + R.nfpass);
+    if (with_bwd) st->bwd[dev] = std::vector<JitKernel>(kernels.begin() + R.nfpass, kernels.end());
     return QG_OK;
 }
 
-int64_t qg_program_pass_source(const qg_program* prog, int pass, char* host_out, int64_t bytes) {
+int64_t qg_program_pass_source(const qg_program* prog, int backward, int pass, char* host_out, int64_t bytes) {
     using namespace qg;
     if (!prog) return -1;
     ProgramRun R;
     program_run_info(prog, &R);
-    if (pass < 0 || pass >= R.nfpass) return -1;
-    const std::string src = pass_source(R, pass);
+    if (pass < 0 || pass >= (backward ? R.nbpass : R.nfpass)) return -1;
+    const std::string src = backward ? bwd_pass_source(R, pass) : pass_source(R, pass);
     const int64_t need = (int64_t)src.size() + 1;
     if (host_out && bytes >= need) memcpy(host_out, src.c_str(), (size_t)need);
     return need;
@@ -540,7 +645,8 @@ int64_t qg_program_pass_source(const qg_program* prog, int pass, char* host_out,
 
 int qg_program_compiled(const qg_program* prog) {
     qg::JitKernel k;
-    return prog && qg::jit_forward_kernel(prog, 0, &k) ? 1 : 0;
+    if (!prog || !qg::jit_forward_kernel(prog, 0, &k)) return 0;
+    return qg::jit_backward_kernel(prog, 0, &k) ? 3 : 1;
 }
 
 }  // extern "C"

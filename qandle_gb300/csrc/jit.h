@@ -14,6 +14,8 @@ struct JitKernel {
 // The compiled kernel of forward pass `pass` of `prog` on the current device;
 // false when the program has not been compiled for it.
 bool jit_forward_kernel(const void* prog, int pass, JitKernel* out);
+// The same for backward pass `pass` (compiled with QG_COMPILE_BACKWARD).
+bool jit_backward_kernel(const void* prog, int pass, JitKernel* out);
 
 // cuLaunchKernel on `stream`; QG_OK or a status with the error text set.
 int jit_launch(const JitKernel& k, unsigned grid, unsigned block, size_t smem, void* stream, void** params);

@@ -13,7 +13,7 @@
 //   SWAP(a, b): apply the physical SWAP and swap bits a and b of xm;
 //   a matrix on bit p with xm_p set acts as X M X (rows and columns reversed).
 #pragma once
-#include "fwd_kernel.cuh"
+#include "bwd_kernel.cuh"
 
 namespace qg {
 
@@ -117,6 +117,81 @@ __device__ __forceinline__ void jnegate_if(PTile<RB>& pt, bool c) {
         const float2 a = get_amp<RB>(pt, r);
         set_amp<RB>(pt, r, make_float2(a.x * s, a.y * s));
     }
+}
+
+// ---- backward: the same ops on psi and lambda (one pending-X mask) ----
+
+template <int P, int RB>
+__device__ __forceinline__ void jmat2(PTile<RB>& pt, PTile<RB>& lt, uint32_t xm, const RunArgs& A,
+                                      const float4* s_mats, int slot, int flags, int64_t sample) {
+    float2 m[4];
+    load_slot(A, s_mats, slot, flags, sample, m);
+    xmx_if(m, (xm >> P) & 1u);
+    pmat<P, RB>(pt, m);
+    pmat<P, RB>(lt, m);
+}
+
+template <int P, int RB>
+__device__ __forceinline__ void jdiag2(PTile<RB>& pt, PTile<RB>& lt, uint32_t xm, const RunArgs& A,
+                                       const float4* s_mats, int slot, int flags, int64_t sample) {
+    float2 m[4];
+    load_slot(A, s_mats, slot, flags, sample, m);
+    const bool sw = (xm >> P) & 1u;
+    const float2 d0 = sw ? m[3] : m[0], d1 = sw ? m[0] : m[3];
+    pdiag<P, RB>(pt, d0, d1);
+    pdiag<P, RB>(lt, d0, d1);
+}
+
+template <int RB>
+__device__ __forceinline__ void jdiag_thread2(PTile<RB>& pt, PTile<RB>& lt, bool bit, const RunArgs& A,
+                                              const float4* s_mats, int slot, int flags, int64_t sample) {
+    float2 m[4];
+    load_slot(A, s_mats, slot, flags, sample, m);
+    pscale<RB>(pt, bit ? m[3] : m[0]);
+    pscale<RB>(lt, bit ? m[3] : m[0]);
+}
+
+template <int P, int C, int RB>
+__device__ __forceinline__ void jcx2(PTile<RB>& pt, PTile<RB>& lt, uint32_t& xm) {
+    pcx<P, C, RB>(pt);
+    pcx<P, C, RB>(lt);
+    xm ^= ((xm >> C) & 1u) << P;
+}
+
+template <int P0, int P1, int RB>
+__device__ __forceinline__ void jswap2(PTile<RB>& pt, PTile<RB>& lt, uint32_t& xm) {
+    pswapbits<P0, P1, RB>(pt);
+    pswapbits<P0, P1, RB>(lt);
+    const uint32_t d = ((xm >> P0) ^ (xm >> P1)) & 1u;
+    xm ^= d * ((1u << P0) | (1u << P1));
+}
+
+template <int P, int RB>
+__device__ __forceinline__ void jmaterialize2(PTile<RB>& pt, PTile<RB>& lt, uint32_t& xm) {
+    const bool c = (xm >> P) & 1u;
+    pswap_if<P, RB>(pt, c);
+    pswap_if<P, RB>(lt, c);
+    xm &= ~(1u << P);
+}
+
+template <int Mask, int RB>
+__device__ __forceinline__ void jnegate2(PTile<RB>& pt, PTile<RB>& lt) {
+    pnegate<Mask, RB>(pt);
+    pnegate<Mask, RB>(lt);
+}
+
+template <int Mask, int RB>
+__device__ __forceinline__ void jnegate_if2(PTile<RB>& pt, PTile<RB>& lt, bool c) {
+    jnegate_if<Mask, RB>(pt, c);
+    jnegate_if<Mask, RB>(lt, c);
+}
+
+// Gradient partial of the rotation on register bit P (axis of its generator)
+// into grad slot `rel` of the pass.
+template <int P, int RB, int NT>
+__device__ __forceinline__ void jgrad(const PTile<RB>& pt, const PTile<RB>& lt, uint32_t xm, int axis, float* gacc,
+                                      uint8_t* gsmp, int rel, int tid, int sample_off) {
+    grad_record<NT>(gacc, gsmp, rel, tid, pgrad_at<P, RB>(pt, lt, axis, xm), sample_off);
 }
 
 }  // namespace qg

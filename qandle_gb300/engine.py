@@ -138,22 +138,27 @@ class Program:
             except Exception:
                 pass
 
-    def pass_source(self, p: int) -> str:
-        """CUDA source of compiled forward pass p (the pass's ops unrolled)."""
+    def pass_source(self, p: int, backward: bool = False) -> str:
+        """CUDA source of compiled pass p (the pass's ops unrolled)."""
         lib = _lib.load()
-        size = lib.qg_program_pass_source(self.handle, p, None, 0)
+        bw = 1 if backward else 0
+        size = lib.qg_program_pass_source(self.handle, bw, p, None, 0)
         if size < 0:
-            raise IndexError(f"no forward pass {p}")
+            raise IndexError(f"no {'backward' if backward else 'forward'} pass {p}")
         buf = ctypes.create_string_buffer(size)
-        lib.qg_program_pass_source(self.handle, p, buf, size)
+        lib.qg_program_pass_source(self.handle, bw, p, buf, size)
         return buf.value.decode()
 
-    def compile(self, device=None, load: bool = True) -> None:
-        """Compile the forward passes into per-pass kernels (NVRTC) for
-        ``device``; with ``load=False`` only check that they build (no GPU
-        needed).  Raises RuntimeError with the compiler's log on failure."""
+    def compile(self, device=None, load: bool = True, backward: bool = None) -> None:
+        """Compile the passes into per-pass kernels (NVRTC) for ``device``:
+        the forward passes, and the backward passes too when ``backward``
+        (default: when the program keeps its state for a backward).  With
+        ``load=False`` only check that they build (no GPU needed).  Raises
+        RuntimeError with the compiler's log on failure."""
         lib = _lib.load()
-        flags = 0 if load else 1
+        if backward is None:
+            backward = self.keep_state
+        flags = (0 if load else 1) | (2 if backward else 0)
         if load:
             with torch.cuda.device(device):
                 _lib.check(lib.qg_program_compile(self.handle, flags))
@@ -161,8 +166,11 @@ class Program:
             _lib.check(lib.qg_program_compile(self.handle, flags))
 
     def compiled(self, device) -> bool:
+        """True when this program's compiled kernels (forward, and backward
+        for a training program) are active on ``device``."""
         with torch.cuda.device(device):
-            return bool(_lib.load().qg_program_compiled(self.handle))
+            v = _lib.load().qg_program_compiled(self.handle)
+        return v == 3 if self.keep_state else v >= 1
 
     def ensure_compiled(self, device) -> None:
         key = str(device)

@@ -69,6 +69,18 @@ def test_fused_forward_vs_oracle(cuda_device, case, oi, compiled):
     assert err < TOL, (case, OPTS[oi], err)
 
 
+def test_compiled_backward_kernels_run(cuda_device):
+    """A training call compiles the backward passes too and runs them."""
+    desc = workloads.adjoint_brick(n=12, batch=2, layers=3)
+    desc["measure"] = "p0"
+    circ = workloads.build_circuit(desc, engine="fused").to(cuda_device)
+    st = torch.zeros(2, 1 << 12, dtype=torch.complex64, device=cuda_device)
+    st[:, 0] = 1
+    circ(st).sum().backward()
+    prog = circ._executor.program(True)
+    assert prog.keep_state and prog.compiled(cuda_device)
+
+
 def test_compiled_kernels_run(cuda_device):
     """The default forward runs the per-program compiled pass kernels."""
     desc = workloads.sel_reupload(n=14, batch=3, layers=2, reupload_every=2)
@@ -139,7 +151,9 @@ def _grad_case(desc, dev, opts, weights_seed=3):
     ("sel_n9", dict()), ("sel_n14", dict(checkpoint_segments=2)), ("sel_n15", dict(tile_bits=12, low_bits=4)),
     ("brick_n13", dict(reg_bits=4)), ("sel_n8", dict(reg_bits=4, checkpoint_segments=2)),
 ])
-def test_fused_adjoint_vs_oracle(cuda_device, case, opts):
+@pytest.mark.parametrize("compiled", [True, False], ids=["compiled", "interpreted"])
+def test_fused_adjoint_vs_oracle(cuda_device, case, opts, compiled):
+    opts = dict(opts, compiled=compiled)
     kind, nq = case.split("_n")
     n = int(nq)
     if kind == "brick":
