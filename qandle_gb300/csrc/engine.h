@@ -17,10 +17,10 @@ constexpr int kBwdRegBits = 4;
 // beside the psi/lambda double buffer, 5 B per slot and thread)
 __host__ __device__ constexpr int max_grad_per_pass(int reg_bits) { return reg_bits == 4 ? 64 : 96; }
 
-// Tile buffers of the forward kernel: three (two loads in flight while one
-// tile computes), four for 2^11 tiles.  Two 2^12 CTAs with three buffers
-// each still fit one SM's shared memory.
-__host__ __device__ constexpr int fwd_stages(int tb) { return tb >= 12 ? 3 : 4; }
+// Tile buffers of the forward kernel: three (tile t computes while tile t+1
+// loads and the bulk store of tile t-1 reads out).  Two 2^12 CTAs with three
+// buffers each still fit one SM's shared memory.
+__host__ __device__ constexpr int fwd_stages(int) { return 3; }
 
 // Resident CTAs per SM the register budget allows: 32 amplitudes per thread
 // (RB = 5) take up to 255 registers, 16 (RB = 4) up to 128.

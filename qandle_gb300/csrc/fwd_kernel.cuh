@@ -33,6 +33,10 @@ __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.comm
 __device__ __forceinline__ void bulk_wait_read0() {
     asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
 __device__ __forceinline__ void bulk_wait_all0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -135,6 +139,39 @@ __device__ __forceinline__ void thread_tile_load(const PassDesc& d, const TileGe
         for (int k = 0; k < RB - 1; ++k)
             if ((i >> k) & 1) off ^= st[k];
         cp_async16(dst + 2 * (tid + i * NT), base + off);
+    }
+}
+
+// Tiles of at most 2^this contiguous blocks are stored by bulk copies.
+constexpr int kMaxBulkStoreBlocksLog2 = 4;
+
+// Local bits below the returned count map to the same global bits, so the
+// tile image is made of contiguous blocks of 2^count amplitudes (at least
+// the runs).
+__device__ __forceinline__ int contiguous_bits(const PassDesc& d) {
+    int e = d.run_bits;
+    while (e < d.tile_bits && d.gbit[e] == e) ++e;
+    return e;
+}
+
+// Bulk copies of a tile's state image from shared memory (local-index order)
+// to global memory, one per contiguous block; issued by the 32 lanes of one
+// warp, which then commit them as their bulk group.
+__device__ void issue_tile_store(const PassDesc& d, const TileGeo& g, float2* dstg, const float2* src, int n,
+                                 int lane) {
+    if (n < d.tile_bits) {
+        const uint32_t bytes = (uint32_t)((int64_t)g.nsamples << n) * 8u;
+        if (lane == 0) bulk_s2g(dstg + g.base, src, bytes);
+        return;
+    }
+    const int e = contiguous_bits(d);
+    const int blocks = 1 << (d.tile_bits - e);
+    const uint32_t bytes = (1u << e) * 8u;
+    for (int r = lane; r < blocks; r += 32) {
+        int64_t off = 0;
+        for (int k = 0; k < d.tile_bits - e; ++k)
+            if ((r >> k) & 1) off += int64_t(1) << d.gbit[e + k];
+        bulk_s2g(dstg + g.base + off, src + ((int64_t)r << e), bytes);
     }
 }
 
@@ -257,6 +294,15 @@ template <int RB>
 __device__ __forceinline__ void pload_nat(PTile<RB>& t, const float2* buf, int tid) {
 #pragma unroll
     for (int r = 0; r < (1 << RB); ++r) set_amp<RB>(t, r, buf[nat_index<RB>(r, tid)]);
+}
+
+// The tile in natural order into shared memory; physical register r holds
+// logical amplitude r ^ xm.
+template <int RB>
+__device__ __forceinline__ void pstore_nat(const PTile<RB>& t, float2* buf, int tid, uint32_t xm) {
+    const int x = (int)xm << 5;
+#pragma unroll
+    for (int r = 0; r < (1 << RB); ++r) buf[nat_index<RB>(r, tid) ^ x] = get_amp<RB>(t, r);
 }
 
 // Probabilities of the tile in natural order into shared memory; physical
@@ -401,9 +447,12 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
     auto tile_loads = [&](int j) -> bool {
         return jt.job[j].pd->init == INIT_LOAD && !jt.job[j].zero_init;
     };
-    // Every thread commits exactly one copy group per prefetch slot (empty
-    // when there is nothing to load), so "tile t has landed" is
-    // cp.async.wait_group S-2 followed by a CTA barrier.
+    // Buffer ring (S = 3): tile t computes in buffer t % 3 while tile t + 1
+    // loads into the next buffer and the bulk store of tile t - 1 reads out of
+    // the previous one.  Every thread commits exactly one copy group per
+    // prefetch (empty when there is nothing to load), so "tile t has landed"
+    // is cp.async.wait_group 0 followed by a CTA barrier; warp 0 commits one
+    // bulk-store group per tile (empty when the tile stores nothing).
     auto issue_prefetch = [&](int64_t t, float2* dst) {
         if (t < total) {
             const int j = find_job(jt, t);
@@ -417,9 +466,9 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         cp_async_commit();
     };
 
+    static_assert(S == 3, "the store write-behind needs three tile buffers");
     const int64_t t0 = blockIdx.x;
-#pragma unroll
-    for (int i = 0; i < S - 1; ++i) issue_prefetch(t0 + (int64_t)i * gridDim.x, bufs + i * AMPS);
+    issue_prefetch(t0, bufs);
     int cur_job = -1;
     int iter = 0;
     for (int64_t t = t0; t < total; t += gridDim.x, ++iter) {
@@ -457,8 +506,8 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         // per-tile data of Ops (in the op-list area when it is not staged),
         // published by the barrier below
         Ops::template tile_start<TB, RB>(A, g, reinterpret_cast<float4*>(s_ops), tid);
-        cp_async_wait<S - 2>();  // this thread's copies of tile t have landed
-        __syncthreads();         // ... and every other thread's
+        cp_async_wait<0>();  // this thread's copies of tile t have landed
+        __syncthreads();     // ... and every other thread's
         if (load_in) {
             pload_nat<RB>(pt, buf, tid);
             decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
@@ -505,22 +554,47 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 }
             }
         }
-        // Prefetch S-1 tiles ahead into the buffer the previous tile used: the
-        // end of that tile waited for every read of it.  (The first exchange
-        // and the epilogue start with a barrier, so every thread has read
-        // `buf` before it is written again.)
-        issue_prefetch(t + (int64_t)(S - 1) * gridDim.x, bufs + ((iter + S - 1) % S) * AMPS);
+        // Prefetch tile t + 1 into the buffer tile t - 2 used, once the bulk
+        // store of tile t - 2 has read it out (it had all of tile t - 1 to do
+        // so; the store of t - 1 may still be reading its own buffer).
+        if (tid < 32) bulk_wait_read<1>();
+        __syncthreads();
+        issue_prefetch(t + (int64_t)gridDim.x, bufs + ((iter + 1) % S) * AMPS);
         // ---- the gate program of this pass ----
         Ops::template apply<TB, RB>(pt, xm, tm, d, A, ops, s_ops, s_mats, reinterpret_cast<float*>(buf), g.sample,
                                     g.fixed_val, tid);
         // ---- epilogue (the planner left the natural mapping) ----
         __syncthreads();  // all exchange reads of `buf` are done
         const int64_t smp0 = g.sample;
+        // A tile made of a few large contiguous blocks is written back by bulk
+        // copies that read the buffer while the next tile computes; a tile of
+        // many small runs is stored straight from registers (one copy engine
+        // working through many 512-byte runs is slower than the warps).
+        const bool bulk_store = n < TB || d.tile_bits - contiguous_bits(d) <= kMaxBulkStoreBlocksLog2;
         if (d.epi & EPI_STORE) {
-            pstore_global<RB>(pt, xm, d, g, A.state, n, tid);
-            if (d.ckpt >= 0) pstore_global<RB>(pt, xm, d, g, A.ckpt + (int64_t)d.ckpt * (A.batch << n), n, tid);
+            if (bulk_store) {
+                pstore_nat<RB>(pt, buf, tid, xm);
+                fence_proxy_async();
+                __syncthreads();
+                if (tid < 32) {
+                    issue_tile_store(d, g, A.state, buf, n, lane);
+                    if (d.ckpt >= 0)
+                        issue_tile_store(d, g, A.ckpt + (int64_t)d.ckpt * (A.batch << n), buf, n, lane);
+                }
+            } else {
+                pstore_global<RB>(pt, xm, d, g, A.state, n, tid);
+                if (d.ckpt >= 0)
+                    pstore_global<RB>(pt, xm, d, g, A.ckpt + (int64_t)d.ckpt * (A.batch << n), n, tid);
+            }
         }
         if (d.epi & (EPI_PROBS | EPI_P0)) {
+            if ((d.epi & EPI_STORE) && bulk_store) {  // the probabilities reuse the buffer: let the store read it first
+                if (tid < 32) {
+                    bulk_commit();
+                    bulk_wait_read0();
+                }
+                __syncthreads();
+            }
             float* pb = reinterpret_cast<float*>(buf);
             pstore_probs<RB>(pt, pb, tid, xm);
             if (d.epi & EPI_PROBS) {
@@ -597,7 +671,7 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 }
             }
         }
-        // make `buf` free before it receives the prefetch S-1 tiles ahead
+        if (tid < 32) bulk_commit();  // this tile's store group (possibly empty)
         fence_proxy_async();
         __syncthreads();
     }

@@ -155,6 +155,82 @@ std::string cu_error(CUresult r) {
 
 std::string loc_bit(int32_t loc) { return "loc_bit_thread(" + std::to_string(loc) + ", tm.tglob)"; }
 
+// ------------------------------------------------ exchange writer --
+
+// A register/lane/warp mapping in OP_MAP encoding, decoded on the host.
+struct MapBits {
+    int regl[5] = {0, 0, 0, 0, 0};  // register bit k -> local bit
+    int thr[16] = {0};              // thread bit k (lanes, then warps) -> local bit
+    int nthr = 0;
+};
+
+MapBits decode_mapping(int32_t y, int32_t z, int32_t w, int rb) {
+    MapBits m;
+    for (int k = 0; k < rb; ++k) m.regl[k] = (y >> (4 * k)) & 15;
+    const int nw = (w >> 16) & 7;
+    m.nthr = 5 + nw;
+    for (int k = 0; k < m.nthr; ++k) m.thr[k] = k < 5 ? ((z >> (4 * k)) & 15) : ((w >> (4 * (k - 5))) & 15);
+    return m;
+}
+
+// The natural mapping (lanes = local bits 0..4, registers = 5.., warps above).
+void natural_mapping(int tb, int rb, int32_t& y, int32_t& z, int32_t& w) {
+    y = 0;
+    for (int k = 0; k < rb; ++k) y |= (5 + k) << (4 * k);
+    z = 0x43210;
+    w = 0;
+    for (int k = 0; k < tb - 5 - rb; ++k) w |= (5 + rb + k) << (4 * k);
+    w |= (tb - 5 - rb) << 16;
+}
+
+int swz_host(int j) { return j ^ (((j >> 5) ^ (j >> 10)) & 31); }
+
+// "C0, C1, C2, C3, C4": slot offsets of the register bits under a mapping.
+std::string reg_offsets(const MapBits& m, int rb) {
+    std::string out;
+    for (int k = 0; k < 5; ++k) {
+        if (k) out += ", ";
+        out += std::to_string(k < rb ? swz_host(1 << m.regl[k]) : 0);
+    }
+    return out;
+}
+
+// Statements that set the thread-dependent parts of a mapping: the slot base
+// `swb`, the global bits of the thread's qubit bits (tm.tglob) and its sample
+// offset in the tile (tm.sample_off) -- what decode_map computes at run time.
+std::string thread_part(const MapBits& m, const PassDesc& d) {
+    std::string swb = "0", tg = "fixed_val", so = "0";
+    for (int k = 0; k < m.nthr; ++k) {
+        const int lb = m.thr[k];
+        const std::string bit = "tbit(tid, " + std::to_string(k) + ")";
+        swb += " ^ (" + bit + " ? " + std::to_string(swz_host(1 << lb)) + " : 0)";
+        if (lb < d.nq_tile)
+            tg += " | ((uint32_t)" + bit + " << " + std::to_string(d.gbit[lb]) + ")";
+        else
+            so += " | (" + bit + " << " + std::to_string(lb - d.nq_tile) + ")";
+    }
+    return "swb = " + swb + "; tm.tglob = " + tg + "; tm.sample_off = " + so + ";";
+}
+
+// One exchange from mapping `cur` to (y, z, w); `two` = psi and lambda.
+std::string exchange_code(const PassDesc& d, const MapBits& cur, int32_t y, int32_t z, int32_t w, int rb,
+                          bool two) {
+    const MapBits nxt = decode_mapping(y, z, w, rb);
+    const std::string cc = reg_offsets(cur, rb), cn = reg_offsets(nxt, rb);
+    std::ostringstream s;
+    s << "{ __syncthreads(); const int wb_ = swb ^ xm_xor<" << cc << ">(xm); ";
+    if (two)
+        s << "cxwrite<TB, RB, " << cc << ">(pp, pt, wb_); cxwrite<TB, RB, " << cc << ">(lp, lt, wb_); ";
+    else
+        s << "cxwrite<TB, RB, " << cc << ">(plane, pt, wb_); ";
+    s << "xm = 0; __syncthreads(); " << thread_part(nxt, d) << " ";
+    if (two)
+        s << "cxread<TB, RB, " << cn << ">(pp, pt, swb); cxread<TB, RB, " << cn << ">(lp, lt, swb); }\n";
+    else
+        s << "cxread<TB, RB, " << cn << ">(plane, pt, swb); }\n";
+    return s.str();
+}
+
 // One forward pass as CUDA source: the shared kernel body with the pass's
 // gate program unrolled.
 std::string pass_source(const ProgramRun& R, int p) {
@@ -203,7 +279,16 @@ std::string pass_source(const ProgramRun& R, int p) {
          "const PassDesc& d, const RunArgs& A, const int4*, const int4* s_ops, const float4* s_mats, float* plane, "
          "int64_t sample0, uint32_t fixed_val, int tid) {\n"
          "    const float4* staged = reinterpret_cast<const float4*>(s_ops);\n"
-         "    (void)staged;\n";
+         "    (void)staged;\n"
+         "    int swb = tm.sw_base;\n"
+         "    (void)swb;\n";
+    MapBits cur;
+    {
+        int32_t y0, z0, w0;
+        natural_mapping(tb, rb, y0, z0, w0);
+        if (d.init == INIT_EMBED) y0 = d.init_map[0], z0 = d.init_map[1], w0 = d.init_map[2];
+        cur = decode_mapping(y0, z0, w0, rb);
+    }
     for (int o = 0; o < d.op_count; ++o) {
         const int32_t k = ops[4 * o], y = ops[4 * o + 1], z = ops[4 * o + 2], w = ops[4 * o + 3];
         const std::string smp = "sample0 + tm.sample_off";
@@ -212,8 +297,8 @@ std::string pass_source(const ProgramRun& R, int p) {
         s << "    ";
         switch (k) {
             case OP_MAP:
-                s << "exchange<TB, RB>(pt, xm, tm, plane, d, " << y << ", " << z << ", " << w
-                  << ", tid, fixed_val);\n";
+                s << exchange_code(d, cur, y, z, w, rb, false);
+                cur = decode_mapping(y, z, w, rb);
                 break;
             case OP_MAT:
                 if (st)
@@ -291,15 +376,23 @@ std::string bwd_pass_source(const ProgramRun& R, int p) {
          "  __device__ __forceinline__ static void apply(PTile<RB>& pt, PTile<RB>& lt, uint32_t& xm, ThreadMap& tm, "
          "const PassDesc& d, const RunArgs& A, const int4*, const int4*, const float4* s_mats, float* pp, float* lp, "
          "int64_t sample0, uint32_t fixed_val, int tid, float* gacc, uint8_t* gsmp) {\n"
-         "    constexpr int NT = 1 << (TB - RB);\n";
+         "    constexpr int NT = 1 << (TB - RB);\n"
+         "    int swb = tm.sw_base;\n"
+         "    (void)swb;\n";
+    MapBits cur;
+    {
+        int32_t y0, z0, w0;
+        natural_mapping(tb, rb, y0, z0, w0);
+        cur = decode_mapping(y0, z0, w0, rb);
+    }
     for (int o = 0; o < d.op_count; ++o) {
         const int32_t k = ops[4 * o], y = ops[4 * o + 1], z = ops[4 * o + 2], w = ops[4 * o + 3];
         const std::string smp = "sample0 + tm.sample_off";
         s << "    ";
         switch (k) {
             case OP_MAP:
-                s << "exchange2<TB, RB>(pt, lt, xm, tm, pp, lp, d, " << y << ", " << z << ", " << w
-                  << ", tid, fixed_val);\n";
+                s << exchange_code(d, cur, y, z, w, rb, true);
+                cur = decode_mapping(y, z, w, rb);
                 break;
             case OP_GRAD:
                 s << "jgrad<" << y << ", RB, NT>(pt, lt, xm, " << z << ", gacc, gsmp, " << (w - d.grad_base)

@@ -119,6 +119,44 @@ __device__ __forceinline__ void jnegate_if(PTile<RB>& pt, bool c) {
     }
 }
 
+// ---- exchanges with compile-time slot offsets ----
+//
+// The swizzle (fwd_kernel.cuh, swz) is linear over XOR, so the shared-memory
+// slot of a thread's register amplitude K under a mapping is
+// base ^ XOR_{bits k of K} C_k, where base depends on the thread's lane/warp
+// bits only and C_k = swz(1 << local bit of register bit k).  The generated
+// pass knows every mapping, so the C_k are template arguments.
+
+template <int K, int C0, int C1, int C2, int C3, int C4>
+__device__ __forceinline__ constexpr int kxor() {
+    return ((K & 1) ? C0 : 0) ^ ((K & 2) ? C1 : 0) ^ ((K & 4) ? C2 : 0) ^ ((K & 8) ? C3 : 0) ^ ((K & 16) ? C4 : 0);
+}
+
+template <int C0, int C1, int C2, int C3, int C4>
+__device__ __forceinline__ int xm_xor(uint32_t xm) {
+    return ((xm & 1u) ? C0 : 0) ^ ((xm & 2u) ? C1 : 0) ^ ((xm & 4u) ? C2 : 0) ^ ((xm & 8u) ? C3 : 0) ^
+           ((xm & 16u) ? C4 : 0);
+}
+
+template <int TB, int RB, int C0, int C1, int C2, int C3, int C4, int K = 0>
+__device__ __forceinline__ void cxwrite(float* plane, const PTile<RB>& t, int base) {
+    const int s = base ^ kxor<K, C0, C1, C2, C3, C4>();
+    const float2 a = get_amp<RB>(t, K);
+    plane[s] = a.x;
+    plane[s + (1 << TB)] = a.y;
+    if constexpr (K + 1 < (1 << RB)) cxwrite<TB, RB, C0, C1, C2, C3, C4, K + 1>(plane, t, base);
+}
+
+template <int TB, int RB, int C0, int C1, int C2, int C3, int C4, int K = 0>
+__device__ __forceinline__ void cxread(const float* plane, PTile<RB>& t, int base) {
+    const int s = base ^ kxor<K, C0, C1, C2, C3, C4>();
+    set_amp<RB>(t, K, make_float2(plane[s], plane[s + (1 << TB)]));
+    if constexpr (K + 1 < (1 << RB)) cxread<TB, RB, C0, C1, C2, C3, C4, K + 1>(plane, t, base);
+}
+
+// Thread bit k of the thread index as 0/1.
+__device__ __forceinline__ int tbit(int tid, int k) { return (tid >> k) & 1; }
+
 // ---- backward: the same ops on psi and lambda (one pending-X mask) ----
 
 template <int P, int RB>
