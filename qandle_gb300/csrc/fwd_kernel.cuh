@@ -503,11 +503,15 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         PTile<RB> pt;
         uint32_t xm = 0;  // pending thread-controlled X per register bit
         ThreadMap tm;
-        // per-tile data of Ops (in the op-list area when it is not staged),
-        // published by the barrier below
-        Ops::template tile_start<TB, RB>(A, g, reinterpret_cast<float4*>(s_ops), tid);
+        // per-tile data of Ops (in the op-list area when it is not staged;
+        // two halves alternate by tile), published by the barrier below
+        Ops::template tile_start<TB, RB>(A, g, reinterpret_cast<float4*>(s_ops) + (iter & 1) * (kSmemOps / 2),
+                                         tid);
         cp_async_wait<0>();  // this thread's copies of tile t have landed
-        __syncthreads();     // ... and every other thread's
+        // warp 0: the bulk store of tile t - 2 has read its buffer out (it had
+        // all of tile t - 1 to do so), so that buffer can take tile t + 1
+        if (tid < 32) bulk_wait_read<1>();
+        __syncthreads();  // tile t has landed everywhere; buffer (t + 1) % 3 is free
         if (load_in) {
             pload_nat<RB>(pt, buf, tid);
             decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
@@ -554,23 +558,22 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 }
             }
         }
-        // Prefetch tile t + 1 into the buffer tile t - 2 used, once the bulk
-        // store of tile t - 2 has read it out (it had all of tile t - 1 to do
-        // so; the store of t - 1 may still be reading its own buffer).
-        if (tid < 32) bulk_wait_read<1>();
-        __syncthreads();
+        // prefetch tile t + 1 into the buffer tile t - 2 used
         issue_prefetch(t + (int64_t)gridDim.x, bufs + ((iter + 1) % S) * AMPS);
         // ---- the gate program of this pass ----
-        Ops::template apply<TB, RB>(pt, xm, tm, d, A, ops, s_ops, s_mats, reinterpret_cast<float*>(buf), g.sample,
-                                    g.fixed_val, tid);
+        // (the op list when Ops reads it, else this tile's half of the staged data)
+        Ops::template apply<TB, RB>(pt, xm, tm, d, A, ops,
+                                    Ops::kStageOps ? s_ops : s_ops + (iter & 1) * (kSmemOps / 2), s_mats,
+                                    reinterpret_cast<float*>(buf), g.sample, g.fixed_val, tid);
         // ---- epilogue (the planner left the natural mapping) ----
-        __syncthreads();  // all exchange reads of `buf` are done
+        const bool bulk_store = n < TB || d.tile_bits - contiguous_bits(d) <= kMaxBulkStoreBlocksLog2;
+        const bool epi_uses_buf = (d.epi & (EPI_PROBS | EPI_P0)) || ((d.epi & EPI_STORE) && bulk_store);
+        if (epi_uses_buf) __syncthreads();  // all exchange reads of `buf` are done
         const int64_t smp0 = g.sample;
         // A tile made of a few large contiguous blocks is written back by bulk
         // copies that read the buffer while the next tile computes; a tile of
         // many small runs is stored straight from registers (one copy engine
         // working through many 512-byte runs is slower than the warps).
-        const bool bulk_store = n < TB || d.tile_bits - contiguous_bits(d) <= kMaxBulkStoreBlocksLog2;
         if (d.epi & EPI_STORE) {
             if (bulk_store) {
                 pstore_nat<RB>(pt, buf, tid, xm);
@@ -672,8 +675,9 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
             }
         }
         if (tid < 32) bulk_commit();  // this tile's store group (possibly empty)
-        fence_proxy_async();
-        __syncthreads();
+        // No barrier here: the next tile's first barrier orders everything
+        // that touches shared memory (the staged per-sample data alternates
+        // between two halves, and `buf` is refilled only two tiles later).
     }
     if (tid < 32) bulk_wait_all0();
 }

@@ -252,7 +252,7 @@ std::string pass_source(const ProgramRun& R, int p) {
                 staged.push_back(z);
             }
         }
-        const int cap = std::min(nt / 2, kSmemOps * 16 / 32);
+        const int cap = std::min(nt / 2, kSmemOps / 2 * 16 / 32);  // one half of the op-list area
         if ((int)staged.size() > cap) {
             staged.clear();
             staged_index.clear();
