@@ -57,6 +57,20 @@ int qg_apply_rotation(void* state, int64_t batch, int n, int qubit, int axis, co
 int qg_apply_matrix(void* state, int64_t batch, int n, int qubit, const void* row_matrix,
                     int dagger, void* stream);
 
+/* Controlled 2x2: the rotation (or row matrix) on `qubit` acts only where
+ * `control` is 1; the other amplitudes are kept.  Replaces
+ * BuiltControlled.forward, qandle/operators.py:486-503 (the reference applies
+ * the target's full matrix to the control-1 rows). */
+int qg_apply_controlled_rotation(void* state, int64_t batch, int n, int control, int qubit, int axis,
+                                 const float* theta, int64_t theta_stride, int dagger, void* stream);
+int qg_apply_controlled_matrix(void* state, int64_t batch, int n, int control, int qubit,
+                               const void* row_matrix, int dagger, void* stream);
+
+/* Reset of `qubit` to |0> keeping the norm: for every pair of amplitudes that
+ * differ in the qubit, a0 <- a0 * |(a0, a1)| / (|a0| + 1e-7), a1 <- 0.
+ * Replaces BuiltReset.forward, qandle/operators.py:612-623. */
+int qg_reset(void* state, int64_t batch, int n, int qubit, void* stream);
+
 /* CNOT: out[i] = in[i ^ target] where the control bit of i is set.  Exact.
  * Replaces BuiltCNOT.forward, qandle/operators.py:536-566. */
 int qg_apply_cnot(void* state, int64_t batch, int n, int control, int target, void* stream);
@@ -121,6 +135,11 @@ int64_t qg_rotation_grad_scratch_bytes(int64_t batch, int n);
 int qg_rotation_grad(const void* out_state, const void* grad_out, float* dtheta, int64_t batch,
                      int n, int qubit, int axis, int per_sample, void* scratch,
                      int64_t scratch_bytes, void* stream);
+/* The same for a controlled rotation: only amplitudes with the control bit
+ * set contribute (same scratch size). */
+int qg_controlled_rotation_grad(const void* out_state, const void* grad_out, float* dtheta, int64_t batch,
+                                int n, int control, int qubit, int axis, int per_sample, void* scratch,
+                                int64_t scratch_bytes, void* stream);
 
 /* ------------------------------------------------------------------------
  * Fused form: a circuit lowered once to a gate program, planned into passes

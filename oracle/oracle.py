@@ -26,7 +26,8 @@ _SRC = os.path.join(_HERE, "sv_oracle.c")
 _lock = threading.Lock()
 _lib = None
 
-KIND = {"rx": 0, "ry": 1, "rz": 2, "u": 3, "cnot": 4, "cz": 5, "swap": 6, "emb": 7}
+KIND = {"rx": 0, "ry": 1, "rz": 2, "u": 3, "cnot": 4, "cz": 5, "swap": 6, "emb": 7, "crot": 8, "cu": 9,
+        "reset": 10}
 ROT = {"rx": 0, "ry": 1, "rz": 2, "x": 0, "y": 1, "z": 2}
 SEED = {"p0": 0, "z": 0, "probs": 1, "state": 2}
 
@@ -100,6 +101,22 @@ class Lowered:
                 umats.append(np.stack([m.real, m.imag], -1).reshape(-1))
             elif k in ("cnot", "cz", "swap"):
                 recs.append([KIND[k], g[1], g[2], 0, 0, 0])
+            elif k in ("crx", "cry", "crz"):
+                # controlled rotation: (kind, control, target, angle, name)
+                axis = ROT[k[1:]]
+                if g[4] is None:
+                    recs.append([KIND["crot"], g[1], g[2], 0, len(theta), axis])
+                    theta.append(float(np.float32(g[3])))
+                    self.theta_gate.append(gi)
+                else:
+                    col = add_named(g[4])
+                    recs.append([KIND["crot"], g[1], g[2], 1, col, axis])
+            elif k == "cu":
+                m = np.asarray(g[3], dtype=np.complex64).astype(np.complex128).reshape(2, 2)
+                recs.append([KIND[k], g[1], g[2], 0, len(umats), 0])
+                umats.append(np.stack([m.real, m.imag], -1).reshape(-1))
+            elif k == "reset":
+                recs.append([KIND[k], g[1], 0, 0, 0, 0])
             elif k == "emb":
                 qs = list(g[3])
                 first = None

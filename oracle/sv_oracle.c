@@ -51,7 +51,10 @@ enum {
     OR_CNOT = 4,
     OR_CZ = 5,
     OR_SWAP = 6,
-    OR_EMBED = 7
+    OR_EMBED = 7,
+    OR_CROT = 8,  /* controlled rotation: q0 control, q1 target, aux axis, src/idx angle */
+    OR_CU = 9,    /* controlled 2x2: q0 control, q1 target, idx matrix */
+    OR_RESET = 10 /* reset of q0 */
 };
 /* measurement kinds for the cotangent seed */
 enum { OR_SEED_P0 = 0, OR_SEED_PROBS = 1, OR_SEED_STATE = 2 };
@@ -106,6 +109,35 @@ static void apply_row2(cd* s, int n, int p, const cd m[4]) {
         cd a0 = s[i], a1 = s[i | st];
         s[i] = cadd(cmul(a0, m[0]), cmul(a1, m[2]));
         s[i | st] = cadd(cmul(a0, m[1]), cmul(a1, m[3]));
+    }
+}
+
+/* out = in @ m on the pairs of bit p whose bit cmask is set
+ * (BuiltControlled.forward, qandle/operators.py:486-503). */
+static void apply_row2_ctrl(cd* s, int n, int p, int64_t cmask, const cd m[4]) {
+    int64_t dim = (int64_t)1 << n, st = (int64_t)1 << p;
+    for (int64_t i = 0; i < dim; ++i) {
+        if ((i & st) || !(i & cmask)) continue;
+        cd a0 = s[i], a1 = s[i | st];
+        s[i] = cadd(cmul(a0, m[0]), cmul(a1, m[2]));
+        s[i | st] = cadd(cmul(a0, m[1]), cmul(a1, m[3]));
+    }
+}
+
+/* Reset of bit p (BuiltReset.forward, qandle/operators.py:612-623): per pair
+ * the |0> amplitude takes the pair's norm, a0 * |pair| / (|a0| + 1e-7). */
+static void apply_reset(cd* s, int n, int p) {
+    int64_t dim = (int64_t)1 << n, st = (int64_t)1 << p;
+    for (int64_t i = 0; i < dim; ++i) {
+        if (i & st) continue;
+        cd a0 = s[i], a1 = s[i | st];
+        double nrm = sqrt(a0.re * a0.re + a0.im * a0.im + a1.re * a1.re + a1.im * a1.im);
+        double n0 = sqrt(a0.re * a0.re + a0.im * a0.im);
+        double sc = nrm / (n0 + 1e-7);
+        s[i].re = a0.re * sc;
+        s[i].im = a0.im * sc;
+        s[i | st].re = 0.0;
+        s[i | st].im = 0.0;
     }
 }
 
@@ -233,6 +265,16 @@ static void apply_gate(cd* s, int n, const int32_t* g, const double* theta,
             }
     } else if (kind == OR_EMBED) {
         apply_embed(s, n, g, named_row, qlist);
+    } else if (kind == OR_CROT) {
+        cd m[4];
+        rot_row_matrix(g[5], 0.5 * gate_angle(g, theta, named_row), m);
+        apply_row2_ctrl(s, n, n - 1 - g[2], (int64_t)1 << (n - 1 - g[1]), m);
+    } else if (kind == OR_CU) {
+        const double* u = umats + 8 * (int64_t)g[4];
+        cd m[4] = {{u[0], u[1]}, {u[2], u[3]}, {u[4], u[5]}, {u[6], u[7]}};
+        apply_row2_ctrl(s, n, n - 1 - g[2], (int64_t)1 << (n - 1 - g[1]), m);
+    } else if (kind == OR_RESET) {
+        apply_reset(s, n, n - 1 - g[1]);
     }
 }
 
@@ -250,6 +292,14 @@ static void apply_gate_inverse(cd* s, int n, const int32_t* g, const double* the
         /* row form M; inverse row form = M^dagger for unitary M */
         cd m[4] = {{u[0], -u[1]}, {u[4], -u[5]}, {u[2], -u[3]}, {u[6], -u[7]}};
         apply_row2(s, n, n - 1 - g[1], m);
+    } else if (kind == OR_CROT) {
+        cd m[4];
+        rot_row_matrix(g[5], -0.5 * gate_angle(g, theta, named_row), m);
+        apply_row2_ctrl(s, n, n - 1 - g[2], (int64_t)1 << (n - 1 - g[1]), m);
+    } else if (kind == OR_CU) {
+        const double* u = umats + 8 * (int64_t)g[4];
+        cd m[4] = {{u[0], -u[1]}, {u[4], -u[5]}, {u[2], -u[3]}, {u[6], -u[7]}};
+        apply_row2_ctrl(s, n, n - 1 - g[2], (int64_t)1 << (n - 1 - g[1]), m);
     } else {
         /* CNOT, CZ, SWAP are involutions */
         apply_gate(s, n, g, theta, named_row, umats, NULL);
@@ -352,12 +402,17 @@ void or_adjoint(const double* psi0, int64_t B, int n, const int32_t* gates, int 
         for (int k = ngates - 1; k >= 0; --k) {
             const int32_t* g = gates + 6 * k;
             int kind = g[0];
-            if (kind <= OR_RZ) {
-                /* psi is the state after the gate: Im <lam| P |psi> */
+            if (kind <= OR_RZ || kind == OR_CROT) {
+                /* psi is the state after the gate: Im <lam| P |psi>, over the
+                 * control-1 amplitudes for a controlled rotation */
+                const int axis = kind == OR_CROT ? g[5] : kind;
+                const int tq = kind == OR_CROT ? g[2] : g[1];
+                const int64_t cm = kind == OR_CROT ? ((int64_t)1 << (n - 1 - g[1])) : 0;
                 memcpy(tmp, psi, sizeof(cd) * dim);
-                apply_pauli(tmp, n, n - 1 - g[1], kind);
+                apply_pauli(tmp, n, n - 1 - tq, axis);
                 double acc = 0.0;
-                for (int64_t i = 0; i < dim; ++i) acc += cmul(cconj(lam[i]), tmp[i]).im;
+                for (int64_t i = 0; i < dim; ++i)
+                    if ((i & cm) == cm) acc += cmul(cconj(lam[i]), tmp[i]).im;
                 if (g[3] == 0)
                     dth[g[4]] += acc;
                 else if (dnr)

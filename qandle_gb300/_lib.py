@@ -72,6 +72,12 @@ SIGNATURES = {
     "qg_apply_rotation": (c_int, [c_void_p, c_int64, c_int, c_int, c_int, c_void_p, c_int64, c_int, c_void_p]),
     "qg_apply_matrix": (c_int, [c_void_p, c_int64, c_int, c_int, c_void_p, c_int, c_void_p]),
     "qg_apply_cnot": (c_int, [c_void_p, c_int64, c_int, c_int, c_int, c_void_p]),
+    "qg_apply_controlled_rotation": (c_int, [c_void_p, c_int64, c_int, c_int, c_int, c_int, c_void_p, c_int64,
+                                             c_int, c_void_p]),
+    "qg_apply_controlled_matrix": (c_int, [c_void_p, c_int64, c_int, c_int, c_int, c_void_p, c_int, c_void_p]),
+    "qg_reset": (c_int, [c_void_p, c_int64, c_int, c_int, c_void_p]),
+    "qg_controlled_rotation_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_int, c_int, c_int,
+                                            c_int, c_void_p, c_int64, c_void_p]),
     "qg_apply_cz": (c_int, [c_void_p, c_int64, c_int, c_int, c_int, c_void_p]),
     "qg_apply_swap": (c_int, [c_void_p, c_int64, c_int, c_int, c_int, c_void_p]),
     "qg_angle_embedding_scratch_bytes": (c_int64, [c_int64, c_int]),

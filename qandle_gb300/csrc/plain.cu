@@ -79,6 +79,43 @@ __global__ void k_1q_n1(float4* __restrict__ s4, int64_t batch, MatSrc ms) {
     s4[b] = make_float4(a0.x, a0.y, a1.x, a1.y);
 }
 
+// Controlled 2x2: the gate on bit p acts on the pairs whose control bit c is
+// 1 (a quarter of the amplitudes per pair side); the rest stay.  Mirrors
+// BuiltControlled.forward (qandle/operators.py:486-503): the target acts on
+// the control=1 subspace, the control=0 rows are kept.
+__global__ void k_c1q(float2* __restrict__ s, int64_t units, int n, int p, int c, MatSrc ms) {
+    const int lo = p < c ? p : c, hi = p < c ? c : p;
+    const uint64_t P = uint64_t(1) << p, C = uint64_t(1) << c;
+    int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    for (; u < units; u += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t i0 = insert_zero(insert_zero((uint64_t)u, lo), hi) | C;
+        float2 m[4];
+        load_matrix(ms, (int64_t)(i0 >> n), m);
+        float2 a0 = s[i0], a1 = s[i0 | P];
+        apply_row2(a0, a1, m);
+        s[i0] = a0;
+        s[i0 | P] = a1;
+    }
+}
+
+// Reset of bit p (qandle/operators.py:612-623): per pair (qubit 0, qubit 1)
+// the |0> amplitude is scaled to carry the pair's norm, the |1> amplitude
+// becomes 0: a0 *= |pair| / (|a0| + 1e-7), a1 = 0 (float32 like the
+// reference).
+__global__ void k_reset(float2* __restrict__ s, int64_t units, int p) {
+    const uint64_t P = uint64_t(1) << p;
+    int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    for (; u < units; u += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t i0 = insert_zero((uint64_t)u, p);
+        const float2 a0 = s[i0], a1 = s[i0 | P];
+        const float nrm = sqrtf(a0.x * a0.x + a0.y * a0.y + a1.x * a1.x + a1.y * a1.y);
+        const float n0 = sqrtf(a0.x * a0.x + a0.y * a0.y);
+        const float sc = nrm / (n0 + 1e-7f);
+        s[i0] = make_float2(a0.x * sc, a0.y * sc);
+        s[i0 | P] = make_float2(0.f, 0.f);
+    }
+}
+
 // Swap amplitude i (bit set_bit = 1, bit other = 0) with i ^ flip.
 //   CNOT(c -> t): set = c, other = t, flip = 1<<t
 //   SWAP(a, b):   set = a, other = b, flip = (1<<a)|(1<<b)
@@ -286,7 +323,7 @@ __global__ void k_p0_final(const float* __restrict__ part, float* __restrict__ o
 // Rotation gradient partials: Im(conj(g_i) (P psi)_i) summed over a chunk of
 // pairs of one sample.  grad = 0.5 * that sum  (torch's g = 2 dL/dpsi*).
 __global__ void k_rotgrad_partial(const float2* __restrict__ psi, const float2* __restrict__ g,
-                                  float* __restrict__ part, int n, int p, int axis, int c) {
+                                  float* __restrict__ part, int n, int p, int axis, int c, uint64_t cmask) {
     __shared__ float sh[32];
     int64_t nch = (int64_t(1) << (n - 1)) >> c;
     int64_t b = blockIdx.x / nch, ch = blockIdx.x % nch;
@@ -295,6 +332,7 @@ __global__ void k_rotgrad_partial(const float2* __restrict__ psi, const float2* 
     for (int k = threadIdx.x; k < (1 << c); k += blockDim.x) {
         uint64_t pair = ((uint64_t)ch << c) + k;  // pair index within the sample
         uint64_t i0 = insert_zero(pair, p);
+        if ((i0 & cmask) != cmask) continue;  // controlled gate: control-0 pairs do not depend on the angle
         uint64_t base = (uint64_t)b << n;
         float2 a0 = psi[base + i0], a1 = psi[base + (i0 | P)];
         float2 g0 = g[base + i0], g1 = g[base + (i0 | P)];
@@ -373,6 +411,19 @@ static int launch_1q(void* state, int64_t batch, int n, int qubit, const MatSrc&
     return QG_OK;
 }
 
+static int launch_c1q(void* state, int64_t batch, int n, int control, int qubit, const MatSrc& ms,
+                      cudaStream_t st) {
+    int rc = check_state(state, batch, n);
+    if (rc) return rc;
+    QG_CHECK_ARG(n >= 2, "a controlled gate needs two qubits");
+    QG_CHECK_ARG(qubit >= 0 && qubit < n && control >= 0 && control < n, "qubit out of range");
+    QG_CHECK_ARG(qubit != control, "control and target must differ");
+    int64_t units = (batch << n) / 4;
+    k_c1q<<<grid_for(units, 256), 256, 0, st>>>((float2*)state, units, n, n - 1 - qubit, n - 1 - control, ms);
+    QG_LAUNCH_CHECK();
+    return QG_OK;
+}
+
 }  // namespace qg
 
 using namespace qg;
@@ -393,6 +444,33 @@ int qg_apply_matrix(void* state, int64_t batch, int n, int qubit, const void* ro
     QG_CHECK_ARG(row_matrix != nullptr, "matrix is null");
     MatSrc ms{3, nullptr, 0, (const float2*)row_matrix, dagger};
     return launch_1q(state, batch, n, qubit, ms, (cudaStream_t)stream);
+}
+
+int qg_apply_controlled_rotation(void* state, int64_t batch, int n, int control, int qubit, int axis,
+                                 const float* theta, int64_t theta_stride, int dagger, void* stream) {
+    QG_CHECK_ARG(axis >= 0 && axis <= 2, "axis must be 0 (x), 1 (y) or 2 (z)");
+    QG_CHECK_ARG(theta != nullptr, "theta is null");
+    QG_CHECK_ARG(theta_stride == 0 || theta_stride == 1, "theta_stride must be 0 or 1");
+    MatSrc ms{axis, theta, theta_stride, nullptr, dagger};
+    return launch_c1q(state, batch, n, control, qubit, ms, (cudaStream_t)stream);
+}
+
+int qg_apply_controlled_matrix(void* state, int64_t batch, int n, int control, int qubit,
+                               const void* row_matrix, int dagger, void* stream) {
+    QG_CHECK_ARG(row_matrix != nullptr, "matrix is null");
+    MatSrc ms{3, nullptr, 0, (const float2*)row_matrix, dagger};
+    return launch_c1q(state, batch, n, control, qubit, ms, (cudaStream_t)stream);
+}
+
+int qg_reset(void* state, int64_t batch, int n, int qubit, void* stream) {
+    int rc = check_state(state, batch, n);
+    if (rc) return rc;
+    QG_CHECK_ARG(qubit >= 0 && qubit < n, "qubit out of range");
+    int64_t units = (batch << n) / 2;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_reset<<<grid_for(units, 256), 256, 0, st>>>((float2*)state, units, n - 1 - qubit);
+    QG_LAUNCH_CHECK();
+    return QG_OK;
 }
 
 static int launch_pair_swap(void* state, int64_t batch, int n, int qa, int qb, int is_swap,
@@ -557,9 +635,28 @@ int64_t qg_rotation_grad_scratch_bytes(int64_t batch, int n) {
     return batch * nch * (int64_t)sizeof(float);
 }
 
+static int rotation_grad(const void* out_state, const void* grad_out, float* dtheta, int64_t batch, int n,
+                         int qubit, int axis, int per_sample, uint64_t cmask, void* scratch,
+                         int64_t scratch_bytes, void* stream);
+
 int qg_rotation_grad(const void* out_state, const void* grad_out, float* dtheta, int64_t batch,
                      int n, int qubit, int axis, int per_sample, void* scratch,
                      int64_t scratch_bytes, void* stream) {
+    return rotation_grad(out_state, grad_out, dtheta, batch, n, qubit, axis, per_sample, 0, scratch,
+                         scratch_bytes, stream);
+}
+
+int qg_controlled_rotation_grad(const void* out_state, const void* grad_out, float* dtheta, int64_t batch,
+                                int n, int control, int qubit, int axis, int per_sample, void* scratch,
+                                int64_t scratch_bytes, void* stream) {
+    QG_CHECK_ARG(control >= 0 && control < n && control != qubit, "bad control qubit");
+    return rotation_grad(out_state, grad_out, dtheta, batch, n, qubit, axis, per_sample,
+                         uint64_t(1) << (n - 1 - control), scratch, scratch_bytes, stream);
+}
+
+static int rotation_grad(const void* out_state, const void* grad_out, float* dtheta, int64_t batch, int n,
+                         int qubit, int axis, int per_sample, uint64_t cmask, void* scratch,
+                         int64_t scratch_bytes, void* stream) {
     int rc = check_state(out_state, batch, n);
     if (rc) return rc;
     QG_CHECK_ARG(grad_out != nullptr && dtheta != nullptr, "null pointer");
@@ -575,7 +672,7 @@ int qg_rotation_grad(const void* out_state, const void* grad_out, float* dtheta,
     QG_CHECK_ARG(batch * nch < (int64_t(1) << 31), "batch * chunks must be < 2^31");
     unsigned grid = (unsigned)(nch * batch);
     k_rotgrad_partial<<<grid, kRedThreads, 0, st>>>((const float2*)out_state, (const float2*)grad_out,
-                                                   (float*)scratch, n, n - 1 - qubit, axis, c);
+                                                   (float*)scratch, n, n - 1 - qubit, axis, c, cmask);
     QG_LAUNCH_CHECK();
     k_rotgrad_final<<<grid_for(per_sample ? batch : 1, 128), 128, 0, st>>>(
         (const float*)scratch, dtheta, batch, nch, per_sample);

@@ -15,6 +15,7 @@ from __future__ import annotations
 import ctypes
 import os
 import threading
+import warnings
 
 import numpy as np
 import torch
@@ -34,6 +35,15 @@ def _rot_axis(rotation: str) -> int:
     return _ROT[r]
 
 
+class NotFusible(ValueError):
+    """A layer the fused engine knows but does not fuse (Reset, controlled
+    arbitrary 2x2, multi-qubit controlled targets): the circuit runs on the
+    per-gate kernels instead."""
+
+
+_H = torch.tensor([[1.0, 1.0], [1.0, -1.0]], dtype=torch.complex64) / (2.0 ** 0.5)
+
+
 class Lowered:
     """Gate records plus where each runtime value comes from."""
 
@@ -42,26 +52,77 @@ class Lowered:
         self.gates: list[tuple] = []
         self.qlist: list[int] = []
         self.param_mods: list = []        # modules whose remapped theta feeds params[i]
+        self.param_scale: list = []       # params[i] = param_scale[i] * remapping(theta)
         self.named_cols: list[tuple] = []  # (kwarg name, column or None)
+        self.named_scale: list = []       # named column c is scaled by named_scale[c] (default 1)
         self.umats: list[torch.Tensor] = []
         self.measure = "state"
+
+    def _rotation(self, axis: int, qubit: int, mod, scale: float = 1.0) -> None:
+        if mod.named:
+            self.gates.append((axis, qubit, 0, 1, len(self.named_cols), 0))
+            self.named_cols.append((mod.name, None))
+            self.named_scale.append(scale)
+        else:
+            self.gates.append((axis, qubit, 0, 0, len(self.param_mods), 0))
+            self.param_mods.append(mod)
+            self.param_scale.append(scale)
+
+    def _matrix(self, qubit: int, m: torch.Tensor) -> None:
+        m = torch.as_tensor(m).to(torch.complex64).reshape(2, 2)
+        diag = bool(m[0, 1] == 0 and m[1, 0] == 0)
+        self.gates.append((_lib.GATE["u"], qubit, 0, 0, len(self.umats), 1 if diag else 0))
+        self.umats.append(m)
+
+    def _controlled(self, mod, inverse: bool) -> None:
+        """Controlled rotation by the standard decomposition (column
+        convention, applied left to right): R(t/2) on the target, CNOT,
+        R(-t/2), CNOT gives R(t) where the control is 1 and I elsewhere for
+        RY and RZ (X R(a) X = R(-a)); RX is H CRZ(t) H on the target."""
+        t = mod.t
+        tname = type(t).__name__
+        if tname not in _AXIS:
+            raise NotFusible(f"Controlled of {tname} runs on the per-gate kernels")
+        axis = _AXIS[tname]
+        sgn = -1.0 if inverse else 1.0
+        c, q = mod.c, t.qubit
+        rot_axis = 2 if axis == 0 else axis
+        if axis == 0:
+            self._matrix(q, _H)
+        self._rotation(rot_axis, q, t, 0.5 * sgn)
+        self.gates.append((_lib.GATE["cnot"], c, q, 0, 0, 0))
+        self._rotation(rot_axis, q, t, -0.5 * sgn)
+        self.gates.append((_lib.GATE["cnot"], c, q, 0, 0, 0))
+        if axis == 0:
+            self._matrix(q, _H)
 
     def add_layer(self, mod) -> None:
         name = type(mod).__name__
         if self.measure != "state" or getattr(self, "_measured", False):
             raise ValueError("layers after a measurement are not supported by the fused engine")
         if name in _AXIS:
-            if mod.named:
-                self.gates.append((_AXIS[name], mod.qubit, 0, 1, len(self.named_cols), 0))
-                self.named_cols.append((mod.name, None))
-            else:
-                self.gates.append((_AXIS[name], mod.qubit, 0, 0, len(self.param_mods), 0))
-                self.param_mods.append(mod)
+            self._rotation(_AXIS[name], mod.qubit, mod)
         elif name == "BuiltU":
-            m = torch.as_tensor(mod.original_matrix).to(torch.complex64).reshape(2, 2)
-            diag = bool(m[0, 1] == 0 and m[1, 0] == 0)
-            self.gates.append((_lib.GATE["u"], mod.qubit, 0, 0, len(self.umats), 1 if diag else 0))
-            self.umats.append(m)
+            self._matrix(mod.qubit, mod.original_matrix)
+        elif name == "BuiltInvert":
+            t = mod.target
+            tname = type(t).__name__
+            if tname in _AXIS:
+                self._rotation(_AXIS[tname], t.qubit, t, -1.0)  # R(a)^-1 = R(-a)
+            elif tname == "BuiltU":
+                self._matrix(t.qubit, torch.linalg.inv(torch.as_tensor(t.original_matrix).to(torch.complex64)))
+            elif tname in ("BuiltCNOT", "BuiltCZ", "BuiltSWAP"):
+                self.add_layer(t)
+            elif tname == "BuiltInvert":
+                self.add_layer(t.target)
+            elif tname == "BuiltControlled":
+                self._controlled(t, inverse=True)
+            else:
+                raise NotFusible(f"Invert of {tname} runs on the per-gate kernels")
+        elif name == "BuiltControlled":
+            self._controlled(mod, inverse=False)
+        elif name == "BuiltReset":
+            raise NotFusible("Reset runs on the per-gate kernels")
         elif name == "BuiltCNOT":
             self.gates.append((_lib.GATE["cnot"], mod.c, mod.t, 0, 0, 0))
         elif name == "BuiltCZ":
@@ -255,6 +316,9 @@ class _Inputs:
             v = v.to(device=device, dtype=torch.float32)
             if j is not None:
                 v = v[..., j]
+            c = len(cols)
+            if c < len(lo.named_scale) and lo.named_scale[c] != 1.0:
+                v = v * lo.named_scale[c]
             if v.dim() > 1:
                 raise ValueError(f"named input {name!r} must be a scalar or [batch] per gate")
             if v.dim() == 1:
@@ -270,8 +334,10 @@ class _Inputs:
         else:
             self.named = torch.zeros(1, 1, dtype=torch.float32, device=device)
         if lo.param_mods:
-            self.params = torch.cat([m.remapping(m.theta).reshape(-1)[:1].to(device=device, dtype=torch.float32)
-                                     for m in lo.param_mods]).contiguous()
+            scales = lo.param_scale if len(lo.param_scale) == len(lo.param_mods) else [1.0] * len(lo.param_mods)
+            self.params = torch.cat([
+                (m.remapping(m.theta).reshape(-1)[:1] * sc if sc != 1.0 else m.remapping(m.theta).reshape(-1)[:1])
+                .to(device=device, dtype=torch.float32) for m, sc in zip(lo.param_mods, scales)]).contiguous()
         else:
             self.params = torch.zeros(1, dtype=torch.float32, device=device)
         if lo.umats:
@@ -313,7 +379,15 @@ class FusedExecutor:
             compiled = os.environ.get("QG_COMPILE", "1") != "0"
         self.compiled = bool(compiled)
         self.n = circuit.num_qubits
-        self.lowered = lower(circuit)
+        try:
+            self.lowered = lower(circuit)
+            self.fusible = True
+        except NotFusible as e:
+            # the circuit holds a layer the fused engine does not fuse: it
+            # runs on the per-gate kernels (same library, one launch per gate)
+            self.lowered = None
+            self.fusible = False
+            warnings.warn(f"{e}; this circuit runs one kernel per gate")
         self.options = dict(tile_bits=tile_bits, low_bits=low_bits, max_high=max_high, reg_bits=reg_bits)
         self.checkpoint_segments = checkpoint_segments
         self._programs = {}
@@ -328,7 +402,7 @@ class FusedExecutor:
         return p
 
     def __call__(self, state=None, **kwargs):
-        if self.n < 5:
+        if self.n < 5 or not self.fusible:
             # the fused tile needs five qubits in registers; tiny circuits run the per-gate kernels
             return self.circuit.forward(state, **kwargs)
         dev = state.device if state is not None else self._device(kwargs)

@@ -14,6 +14,7 @@ Row-vector convention as in the reference: ``forward(state)`` equals
 from __future__ import annotations
 
 import abc
+import warnings
 import typing
 
 import torch
@@ -26,6 +27,7 @@ __all__ = [
     "UnbuiltParametrizedOperator", "BuiltParametrizedOperator",
     "CNOT", "CZ", "SWAP", "BuiltCNOT", "BuiltCZ", "BuiltSWAP",
     "U", "BuiltU", "CustomGate", "BUILT_CLASS_RELATION",
+    "Invert", "BuiltInvert", "Controlled", "BuiltControlled", "Reset", "BuiltReset",
 ]
 
 
@@ -346,6 +348,148 @@ class BuiltSWAP(BuiltOperator):
         return _perm_matrix(f, n).T.contiguous()
 
 
+class Invert(UnbuiltOperator):
+    """Inverse of a target operator (operators.py:416-432)."""
+
+    def __init__(self, target: Operator):
+        self.t = target
+
+    def __str__(self) -> str:
+        return f"{self.t}^-1"
+
+    def build(self, num_qubits, **kwargs) -> "BuiltInvert":
+        return BuiltInvert(target=self.t, num_qubits=num_qubits)
+
+
+class BuiltInvert(BuiltOperator):
+    """state @ inv(target matrix) (operators.py:435-459).  Rotations run as
+    the rotation by the negated angle, U as its 2x2 inverse, CNOT / CZ / SWAP
+    as themselves (involutions); no 2^n x 2^n matrix is formed."""
+
+    def __init__(self, target: Operator, num_qubits: int):
+        super().__init__()
+        if hasattr(target, "build"):
+            warnings.warn(
+                "Building target operator in Invert. If the target operator is parameterized, this might lead to "
+                "different parameter initialization. Please build the target operator before inverting it.")
+            target = target.build(num_qubits)
+        self.target = target
+        self.num_qubits = num_qubits
+
+    def forward(self, state: torch.Tensor) -> torch.Tensor:
+        t, n = self.target, self.num_qubits
+        if isinstance(t, BuiltParametrizedOperator):
+            return plain.Rotation.apply(state, -t.angle(), n, t.qubit, t.axis)
+        if isinstance(t, BuiltU):
+            return plain.Matrix.apply(state, torch.linalg.inv(t._m), n, t.qubit)
+        if isinstance(t, (BuiltCNOT, BuiltCZ, BuiltSWAP)):
+            return t(state)
+        if isinstance(t, BuiltInvert):
+            return t.target(state)
+        if isinstance(t, BuiltControlled):
+            return t.forward_inverse(state)
+        raise NotImplementedError(f"Invert of {type(t).__name__} is not supported")
+
+    def __str__(self) -> str:
+        return Invert(self.target).__str__()
+
+    def to_matrix(self, **kwargs) -> torch.Tensor:
+        return torch.linalg.inv(self.target.to_matrix())
+
+
+class Controlled(UnbuiltOperator):
+    """Apply the target operator where the control qubit is 1 (operators.py:462-478)."""
+
+    def __init__(self, control: int, target: Operator):
+        self.c = control
+        self.t = target
+
+    def __str__(self) -> str:
+        return f"Controlled {self.c}|{self.t}"
+
+    def build(self, num_qubits, **kwargs) -> "BuiltControlled":
+        return BuiltControlled(control=self.c, target=self.t, num_qubits=num_qubits)
+
+
+class BuiltControlled(BuiltOperator):
+    """Target on the control-1 subspace, control-0 amplitudes kept
+    (operators.py:481-515).  Rotation and U targets run on the controlled 2x2
+    kernel; other targets use the reference's own construction (the target's
+    full matrix on the control-1 rows) on the device, for up to 12 qubits."""
+
+    def __init__(self, control: int, target: Operator, num_qubits: int):
+        super().__init__()
+        self.c = control
+        if hasattr(target, "build"):
+            target = target.build(num_qubits)
+        self.t = target
+        self.named = target.named
+        self.num_qubits = num_qubits
+
+    def forward(self, state: torch.Tensor, **kwargs) -> torch.Tensor:
+        return self._run(state, False, **kwargs)
+
+    def forward_inverse(self, state: torch.Tensor, **kwargs) -> torch.Tensor:
+        return self._run(state, True, **kwargs)
+
+    def _run(self, state, inverse: bool, **kwargs):
+        t, n = self.t, self.num_qubits
+        if isinstance(t, BuiltParametrizedOperator):
+            a = t.angle(**kwargs)
+            return plain.ControlledRotation.apply(state, -a if inverse else a, n, self.c, t.qubit, t.axis)
+        if isinstance(t, BuiltU):
+            m = torch.linalg.inv(t._m) if inverse else t._m
+            return plain.ControlledMatrix.apply(state, m, n, self.c, t.qubit)
+        if n > 12:
+            raise NotImplementedError("Controlled of a multi-qubit target is limited to 12 qubits")
+        m = t.to_matrix(**kwargs).to(device=state.device, dtype=torch.complex64)
+        if inverse:
+            m = torch.linalg.inv(m)
+        mask = (torch.arange(1 << n, device=state.device) >> (n - 1 - self.c)) & 1 == 1
+        st = state.unsqueeze(0) if state.dim() == 1 else state
+        c1 = torch.where(mask, st, torch.zeros_like(st))
+        out = torch.where(mask, torch.squeeze(c1.unsqueeze(1) @ m, 1), st)
+        return out.squeeze(0) if state.dim() == 1 else out
+
+    def __str__(self) -> str:
+        return Controlled(self.c, self.t).__str__()
+
+    def to_matrix(self, **kwargs) -> torch.Tensor:
+        return self.t.to_matrix()  # what the reference returns (operators.py:514-515)
+
+
+class Reset(UnbuiltOperator):
+    """Reset a qubit to |0> while preserving the norm (operators.py:632-650)."""
+
+    def __init__(self, qubit: int):
+        self.qubit = qubit
+
+    def __str__(self) -> str:
+        return f"Reset {self.qubit}"
+
+    def build(self, num_qubits, **kwargs) -> "BuiltReset":
+        return BUILT_CLASS_RELATION[self.__class__](qubit=self.qubit, num_qubits=num_qubits)
+
+
+class BuiltReset(BuiltOperator):
+    """Per pair of amplitudes differing in the qubit: a0 * |pair| / (|a0| +
+    1e-7) on |0>, 0 on |1> (operators.py:603-629)."""
+
+    def __init__(self, qubit: int, num_qubits: int):
+        super().__init__()
+        self.qubit = qubit
+        self.num_qubits = num_qubits
+
+    def forward(self, state: torch.Tensor) -> torch.Tensor:
+        return plain.Reset.apply(state, self.num_qubits, self.qubit)
+
+    def __str__(self) -> str:
+        return Reset(self.qubit).__str__()
+
+    def to_matrix(self, **kwargs) -> torch.Tensor:
+        raise ValueError("Reset gate does not have a matrix representation.")
+
+
 class rdict(dict):
     """Reversible dict (operators.py:702-706)."""
 
@@ -364,4 +508,5 @@ BUILT_CLASS_RELATION = rdict({
     U: BuiltU,
     SWAP: BuiltSWAP,
     CZ: BuiltCZ,
+    Reset: BuiltReset,
 })

@@ -98,6 +98,111 @@ class Matrix(torch.autograd.Function):
         return gin.reshape(sshape), None, None, None
 
 
+class ControlledRotation(torch.autograd.Function):
+    """Rotation on ``qubit`` where ``control`` is 1 (BuiltControlled with a
+    rotation target, qandle/operators.py:486-503)."""
+
+    @staticmethod
+    def forward(ctx, state, angle, n, control, qubit, axis):
+        st = _as_batched(state, n)
+        B = st.shape[0]
+        a = angle.to(device=st.device, dtype=torch.float32).reshape(-1).contiguous()
+        per_sample = a.numel() > 1
+        if per_sample and B == 1:
+            st = st.expand(a.numel(), -1)
+            B = a.numel()
+        if per_sample and a.numel() != B:
+            raise ValueError(f"named input has {a.numel()} values for a batch of {B}")
+        out = st.clone()
+        _lib.call("qg_apply_controlled_rotation", out.data_ptr(), B, n, control, qubit, axis, a.data_ptr(),
+                  1 if per_sample else 0, 0, _lib.stream())
+        ctx.save_for_backward(out, a)
+        ctx.meta = (n, control, qubit, axis, per_sample, angle.shape, state.shape, B)
+        if state.dim() == 1 and not per_sample:
+            return out.reshape(state.shape)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        out, a = ctx.saved_tensors
+        n, control, qubit, axis, per_sample, ashape, sshape, B = ctx.meta
+        g = g.reshape(B, 1 << n).contiguous()
+        gin = dth = None
+        if ctx.needs_input_grad[0]:
+            gin = g.clone()
+            _lib.call("qg_apply_controlled_rotation", gin.data_ptr(), B, n, control, qubit, axis, a.data_ptr(),
+                      1 if per_sample else 0, 1, _lib.stream())
+            orig_b = 1 if len(sshape) == 1 else sshape[0]
+            if orig_b != B:
+                gin = gin.sum(0, keepdim=True)
+            gin = gin.reshape(sshape)
+        if ctx.needs_input_grad[1]:
+            scr = _scratch(_lib.load().qg_rotation_grad_scratch_bytes(B, n), g.device)
+            dth = torch.empty(B if per_sample else 1, dtype=torch.float32, device=g.device)
+            _lib.call("qg_controlled_rotation_grad", out.data_ptr(), g.data_ptr(), dth.data_ptr(), B, n, control,
+                      qubit, axis, 1 if per_sample else 0, scr.data_ptr(), scr.numel(), _lib.stream())
+            dth = dth.reshape(ashape)
+        return gin, dth, None, None, None, None
+
+
+class ControlledMatrix(torch.autograd.Function):
+    """Fixed 2x2 on ``qubit`` where ``control`` is 1."""
+
+    @staticmethod
+    def forward(ctx, state, row_matrix, n, control, qubit):
+        st = _as_batched(state, n)
+        m = row_matrix.to(device=st.device, dtype=torch.complex64).contiguous()
+        out = st.clone()
+        _lib.call("qg_apply_controlled_matrix", out.data_ptr(), st.shape[0], n, control, qubit, m.data_ptr(), 0,
+                  _lib.stream())
+        ctx.save_for_backward(m)
+        ctx.meta = (n, control, qubit, state.shape)
+        return out.reshape(state.shape)
+
+    @staticmethod
+    def backward(ctx, g):
+        (m,) = ctx.saved_tensors
+        n, control, qubit, sshape = ctx.meta
+        gin = g.reshape(-1, 1 << n).contiguous().clone()
+        _lib.call("qg_apply_controlled_matrix", gin.data_ptr(), gin.shape[0], n, control, qubit, m.data_ptr(), 1,
+                  _lib.stream())
+        return gin.reshape(sshape), None, None, None, None
+
+
+def _reset_torch(x: torch.Tensor, n: int, qubit: int) -> torch.Tensor:
+    """The reset of qandle/operators.py:612-623 as torch ops on [B, 2^n]
+    (used for its backward: the same formula, differentiated by torch)."""
+    v = x.reshape(x.shape[0], 1 << qubit, 2, 1 << (n - 1 - qubit))
+    a0, a1 = v[:, :, 0, :], v[:, :, 1, :]
+    nrm = torch.sqrt(a0.abs() ** 2 + a1.abs() ** 2)
+    scale = nrm / (a0.abs() + 1e-7)
+    return torch.stack([a0 * scale, torch.zeros_like(a1)], 2).reshape(x.shape)
+
+
+class Reset(torch.autograd.Function):
+    """Reset of ``qubit`` keeping the norm (qandle/operators.py:603-651):
+    forward on the CUDA kernel, backward through the same formula."""
+
+    @staticmethod
+    def forward(ctx, state, n, qubit):
+        st = _as_batched(state, n)
+        out = st.clone()
+        _lib.call("qg_reset", out.data_ptr(), st.shape[0], n, qubit, _lib.stream())
+        ctx.save_for_backward(st)
+        ctx.meta = (n, qubit, state.shape)
+        return out.reshape(state.shape)
+
+    @staticmethod
+    def backward(ctx, g):
+        (st,) = ctx.saved_tensors
+        n, qubit, sshape = ctx.meta
+        with torch.enable_grad():
+            x = st.detach().requires_grad_(True)
+            y = _reset_torch(x, n, qubit)
+            (gin,) = torch.autograd.grad(y, x, g.reshape(y.shape))
+        return gin.reshape(sshape), None, None
+
+
 _PERM = {"cnot": "qg_apply_cnot", "cz": "qg_apply_cz", "swap": "qg_apply_swap"}
 
 
@@ -255,6 +360,11 @@ def run_layers_inplace(layers, state: torch.Tensor | None, n: int, kwargs: dict,
         elif name == "BuiltSWAP":
             if mod.a != mod.b:
                 _lib.call("qg_apply_swap", st.data_ptr(), st.shape[0], n, mod.a, mod.b, _lib.stream())
+        elif name in ("BuiltInvert", "BuiltControlled", "BuiltReset"):
+            prev = st.shape[0]
+            st = (mod(st, **kwargs) if getattr(mod, "named", False) else mod(st)).reshape(-1, 1 << n)
+            if st.shape[0] != prev:
+                unbatched = False
         elif hasattr(mod, "mods"):
             st = run_layers_inplace(list(mod.mods), st, n, kwargs, initial)
         else:

@@ -86,6 +86,11 @@ class Circuit(torch.nn.Module):
             if isinstance(layer, (operators.CNOT, operators.CZ)):
                 qubits.add(layer.c)
                 qubits.add(layer.t)
+            elif isinstance(layer, operators.Controlled):
+                qubits.add(layer.c)
+                qubits.update(Circuit._used_qubits([layer.t]))
+            elif isinstance(layer, operators.Invert):
+                qubits.update(Circuit._used_qubits([layer.t]))
             elif isinstance(layer, operators.SWAP):
                 qubits.add(layer.a)
                 qubits.add(layer.b)

@@ -312,9 +312,142 @@ def circuit_cases(qandle):
     return out
 
 
+def special_cases(qandle):
+    """Reset (test/test_operators.py:6-58 inputs), Invert of every gate kind,
+    Controlled rotations and U (fixed and per-sample angles), the angle
+    gradient through controlled rotations, and one circuit mixing them.
+    Each case stores a JSON spec of how to build the op with the front end."""
+    out = {}
+    idx = 0
+
+    def put(spec, inp, res, kw=None):
+        nonlocal idx
+        out[f"s{idx}_in"] = inp.detach().numpy()
+        out[f"s{idx}_out"] = res.detach().numpy()
+        out[f"s{idx}_spec"] = np.array(json.dumps(spec))
+        if kw:
+            for k, v in kw.items():
+                out[f"s{idx}_kw_{k}"] = v.detach().numpy()
+        idx += 1
+
+    # Reset: the reference's own unbatched and batched inputs
+    for batched in (False, True):
+        torch.manual_seed(3)
+        for n in range(1, 5):
+            if batched:
+                inp = torch.rand(7, 2 ** n, dtype=torch.cfloat)
+                inp = inp / torch.linalg.norm(inp, dim=-1, keepdim=True)
+            else:
+                inp = torch.arange(2 ** n).to(torch.cfloat) + 0.5 - 0.1j
+                inp = inp / torch.linalg.norm(inp)
+            for q in range(n):
+                op = qandle.Reset(qubit=q).build(num_qubits=n)
+                put({"n": n, "op": "reset", "qubit": q}, inp, op(inp))
+    gen = torch.Generator().manual_seed(11)
+    # Invert of every gate kind
+    for n in range(1, 5):
+        inp = torch.rand(5, 2 ** n, dtype=torch.cfloat, generator=gen)
+        inp = inp / torch.linalg.norm(inp, dim=-1, keepdim=True)
+        for q in range(n):
+            for k in ("rx", "ry", "rz"):
+                th = float(np.float32(torch.rand(1, generator=gen).item() * 2 * np.pi))
+                cls = {"rx": qandle.RX, "ry": qandle.RY, "rz": qandle.RZ}[k]
+                tgt = cls(qubit=q, theta=th, remapping=None).build(num_qubits=n)
+                op = qandle.Invert(tgt).build(num_qubits=n)
+                put({"n": n, "op": "invert", "target": [k, q, th]}, inp, op(inp))
+            a, b, c = (torch.rand(3, generator=gen) * 2 * np.pi).tolist()
+            m = workloads.u3_row_matrix(a, b, c)
+            tgt = qandle.U(qubit=q, matrix=torch.tensor(m)).build(num_qubits=n)
+            op = qandle.Invert(tgt).build(num_qubits=n)
+            put({"n": n, "op": "invert", "target": ["u", q, [[float(z.real), float(z.imag)] for z in m.reshape(-1)]]},
+                inp, op(inp))
+            for q2 in range(n):
+                if q2 == q:
+                    continue
+                for k in ("cnot", "cz", "swap"):
+                    cls = {"cnot": qandle.CNOT, "cz": qandle.CZ, "swap": qandle.SWAP}[k]
+                    tgt = (cls(q, q2) if k != "swap" else cls(a=q, b=q2)).build(num_qubits=n)
+                    op = qandle.Invert(tgt).build(num_qubits=n)
+                    put({"n": n, "op": "invert", "target": [k, q, q2]}, inp, op(inp))
+    # Controlled rotations and U
+    for n in range(2, 5):
+        inp = torch.rand(5, 2 ** n, dtype=torch.cfloat, generator=gen)
+        inp = inp / torch.linalg.norm(inp, dim=-1, keepdim=True)
+        for c in range(n):
+            for t in range(n):
+                if c == t:
+                    continue
+                for k in ("rx", "ry", "rz"):
+                    th = float(np.float32(torch.rand(1, generator=gen).item() * 2 * np.pi))
+                    cls = {"rx": qandle.RX, "ry": qandle.RY, "rz": qandle.RZ}[k]
+                    op = qandle.Controlled(c, cls(qubit=t, theta=th, remapping=None)).build(num_qubits=n)
+                    put({"n": n, "op": "controlled", "control": c, "target": [k, t, th]}, inp, op(inp))
+                a, b, cc = (torch.rand(3, generator=gen) * 2 * np.pi).tolist()
+                m = workloads.u3_row_matrix(a, b, cc)
+                op = qandle.Controlled(c, qandle.U(qubit=t, matrix=torch.tensor(m))).build(num_qubits=n)
+                put({"n": n, "op": "controlled", "control": c,
+                     "target": ["u", t, [[float(z.real), float(z.imag)] for z in m.reshape(-1)]]}, inp, op(inp))
+    # per-sample (named) controlled rotation
+    n = 3
+    inp = torch.rand(6, 2 ** n, dtype=torch.cfloat, generator=gen)
+    inp = inp / torch.linalg.norm(inp, dim=-1, keepdim=True)
+    x = torch.rand(6, generator=gen) * np.pi
+    for k in ("rx", "ry", "rz"):
+        cls = {"rx": qandle.RX, "ry": qandle.RY, "rz": qandle.RZ}[k]
+        op = qandle.Controlled(2, cls(qubit=0, name="x", remapping=None)).build(num_qubits=n)
+        put({"n": n, "op": "controlled", "control": 2, "target": [k, 0, None, "x"]}, inp, op(inp, x=x),
+            kw={"x": x})
+    # angle gradients through controlled rotations (autograd of the reference)
+    n = 4
+    inp = torch.rand(3, 2 ** n, dtype=torch.cfloat, generator=gen)
+    inp = inp / torch.linalg.norm(inp, dim=-1, keepdim=True)
+    ths = [torch.tensor(float(v), requires_grad=True) for v in (torch.rand(4, generator=gen) * 6).tolist()]
+    layers = [qandle.RY(qubit=0, theta=ths[0], remapping=None), qandle.CNOT(0, 1),
+              qandle.Controlled(1, qandle.RX(qubit=2, theta=ths[1], remapping=None)),
+              qandle.Controlled(2, qandle.RY(qubit=3, theta=ths[2], remapping=None)),
+              qandle.Controlled(3, qandle.RZ(qubit=0, theta=ths[3], remapping=None)),
+              qandle.MeasureProbability()]
+    circ = qandle.Circuit(layers, num_qubits=n)
+    built_ths = [m.t.theta if hasattr(m, "t") and hasattr(m.t, "theta") else m.theta
+                 for m in circ.circuit.layers if hasattr(m, "theta") or (hasattr(m, "t") and hasattr(m.t, "theta"))]
+    p0 = circ(inp)
+    loss = (p0 * torch.arange(1, p0.shape[-1] + 1)).sum()
+    grads = torch.autograd.grad(loss, built_ths)
+    out["grad_in"] = inp.numpy()
+    out["grad_p0"] = p0.detach().numpy()
+    out["grad_thetas"] = np.array([float(t.detach()) for t in built_ths], dtype=np.float32)
+    out["grad_out"] = np.array([float(g) for g in grads], dtype=np.float64)
+    # one circuit mixing the new gates with the usual ones, |psi|^2 out
+    n = 6
+    inp = torch.rand(4, 2 ** n, dtype=torch.cfloat, generator=gen)
+    inp = inp / torch.linalg.norm(inp, dim=-1, keepdim=True)
+    spec_layers, layers = [], []
+    for d in range(2):
+        for q in range(n):
+            th = float(np.float32(torch.rand(1, generator=gen).item() * 6))
+            layers.append(qandle.RY(qubit=q, theta=th, remapping=None))
+            spec_layers.append(["ry", q, th])
+        for q in range(n - 1):
+            th = float(np.float32(torch.rand(1, generator=gen).item() * 6))
+            layers.append(qandle.Controlled(q, qandle.RZ(qubit=q + 1, theta=th, remapping=None)))
+            spec_layers.append(["controlled", q, ["rz", q + 1, th]])
+        th = float(np.float32(torch.rand(1, generator=gen).item() * 6))
+        tgt = qandle.RX(qubit=d, theta=th, remapping=None).build(num_qubits=n)
+        layers.append(qandle.Invert(tgt))
+        spec_layers.append(["invert", ["rx", d, th]])
+        layers.append(qandle.CNOT(n - 1, 0))
+        spec_layers.append(["cnot", n - 1, 0])
+    layers.append(qandle.MeasureJointProbability())
+    circ = qandle.Circuit(layers, num_qubits=n)
+    put({"n": n, "op": "circuit", "layers": spec_layers, "measure": "probs"}, inp, circ(inp))
+    out["count"] = np.array(idx)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("QANDLE_REFERENCE_SRC", ""))
+    ap.add_argument("--only", default="", help="comma-separated groups to regenerate")
     args = ap.parse_args()
     if not args.reference:
         sys.exit("pass --reference <path to the qandle src directory>")
@@ -327,8 +460,12 @@ def main():
         "sel": sel_cases,
         "reupload": reupload_cases,
         "circuits": circuit_cases,
+        "special": special_cases,
     }
+    only = [g for g in args.only.split(",") if g]
     for name, fn in groups.items():
+        if only and name not in only:
+            continue
         arrays = fn(qandle)
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **arrays)

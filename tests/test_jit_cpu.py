@@ -27,7 +27,10 @@ def test_source_unrolls_every_op():
         src = prog.pass_source(p)
         body = src[src.index("static void apply"):src.index("\n};")]
         skip = ("const float4* staged", "(void)staged;")
-        calls = [ln for ln in body.splitlines()[1:] if ln.strip().endswith(";") and not ln.strip().startswith(skip)]
+        skip = skip + ("int swb", "(void)swb;")
+        calls = [ln for ln in body.splitlines()[1:]
+                 if (ln.strip().endswith(";") or ln.strip().startswith("{ __syncthreads();"))
+                 and not ln.strip().startswith(skip)]
         assert len(calls) == len(pd["ops"]), p
         assert "switch" not in src and "qg_fwd_pass" in src
     with pytest.raises(IndexError):

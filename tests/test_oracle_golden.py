@@ -166,3 +166,35 @@ def test_adjoint_vs_finite_differences_and_shift():
         # chain rule through the MSE with the unshifted residual
         ps = float((2.0 * (z0 - t) / z0.size * dz).sum())
         assert abs(ps - dth[k]) < 1e-7, (k, ps, dth[k])  # shifted angles round to float32
+
+
+def test_oracle_special_gates_vs_reference():
+    """Reset, Invert of every gate kind and Controlled rotations / U (fixed
+    and per-sample angles) against the reference's outputs."""
+    z = golden_io.load("special")
+    for i in range(int(z["count"])):
+        spec = json.loads(str(z[f"s{i}_spec"]))
+        inp = z[f"s{i}_in"]
+        ref = z[f"s{i}_out"]
+        batch = inp.shape[0] if inp.ndim == 2 else 1
+        inputs = {k[len(f"s{i}_kw_"):]: z[k] for k in z.files if k.startswith(f"s{i}_kw_")}
+        desc = {"n": spec["n"], "batch": batch, "gates": golden_io.special_gates(spec), "inputs": inputs,
+                "measure": "state"}
+        st = oracle.run(desc, state=inp.reshape(batch, -1))
+        got = st
+        if spec.get("measure") == "probs":
+            got = np.abs(st) ** 2
+        assert np.abs(got.reshape(ref.shape) - ref).max() < 2e-5, (i, spec)
+
+
+def test_oracle_controlled_gradients_vs_reference_autograd():
+    z = golden_io.load("special")
+    th = [float(v) for v in z["grad_thetas"]]
+    desc = {"n": 4, "batch": 3, "inputs": {}, "measure": "p0",
+            "gates": [("ry", 0, th[0], None), ("cnot", 0, 1), ("crx", 1, 2, th[1], None),
+                      ("cry", 2, 3, th[2], None), ("crz", 3, 0, th[3], None)]}
+    p0 = oracle.forward(desc, state=z["grad_in"])
+    assert np.abs(p0 - z["grad_p0"]).max() < 1e-5
+    w = np.broadcast_to(np.arange(1, 5, dtype=np.float64), (3, 4)).copy()
+    dth, _, _ = oracle.adjoint(desc, w, "p0", state=z["grad_in"])
+    assert np.abs(dth - z["grad_out"]).max() < 1e-4

@@ -12,12 +12,16 @@ from tests import program_emulator as emu
 
 
 def _runtime(lo, desc, B):
-    params = np.array([float(m.remapping(m.theta).reshape(-1)[0].detach()) for m in lo.param_mods])
+    scales = lo.param_scale if len(lo.param_scale) == len(lo.param_mods) else [1.0] * len(lo.param_mods)
+    params = np.array([sc * float(m.remapping(m.theta).reshape(-1)[0].detach())
+                       for m, sc in zip(lo.param_mods, scales)])
     inputs = desc.get("inputs", {})
     cols = []
-    for name, j in lo.named_cols:
+    for c, (name, j) in enumerate(lo.named_cols):
         v = np.asarray(inputs[name], dtype=np.float32).astype(np.float64)
         v = v[..., j] if j is not None else v
+        if c < len(lo.named_scale):
+            v = v * lo.named_scale[c]
         cols.append(np.broadcast_to(v, (B,)))
     named = np.stack(cols, 1) if cols else np.zeros((B, 1))
     umats = [np.asarray(u.numpy(), dtype=complex) for u in lo.umats]
@@ -153,3 +157,26 @@ def test_serving_lowering_matches_front_end():
     d2 = dict(d)
     d2["measure"] = "z"
     assert np.abs(z[:, 1:] - oracle.forward(d2)).max() < 1e-9
+
+
+def test_controlled_and_inverted_gates_plan_matches_oracle():
+    """Controlled rotations (decomposed into rotations and CNOTs), named
+    controlled rotations and inverted gates: planned, emulated, and equal to
+    the oracle's controlled / inverse kinds (forward and adjoint)."""
+    from tests import test_special_gpu as sp
+
+    layers, desc, inputs = sp._mixed(n=9, batch=2, seed=8)
+    n, B = desc["n"], desc["batch"]
+    import qandle_gb300 as q
+
+    circ = q.Circuit(layers, num_qubits=n)
+    lo = engine.lower(circ.circuit)
+    prog = engine.Program(lo, "p0", keep_state=True, segments=2, tile_bits=13, low_bits=5)
+    params, named, umats, embed = _runtime(lo, desc, B)
+    st0 = np.zeros((B, 1 << n), complex)
+    st0[:, 0] = 1
+    st, ck = emu.run_forward(prog, n, B, params, named, umats, embed=embed, state=st0)
+    ref = oracle.run(desc, state=st0)
+    # controlled RX goes through H on the target, a complex64 matrix
+    # (1/sqrt(2) to float precision): agreement is at 1e-8, not 1e-10
+    assert np.abs(st - ref).max() < 1e-6
