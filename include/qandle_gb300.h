@@ -92,6 +92,15 @@ int qg_angle_embedding(void* out, const float* x, int64_t x_row_stride, int64_t 
                        const int* qubits, int nq, int axis, void* scratch, int64_t scratch_bytes,
                        void* stream);
 
+/* AmplitudeEmbedding: out[b] = (x[b][0..len), pad_value, ..., pad_value) as
+ * real amplitudes of 2^n entries, divided by max(||.||_2, 1e-12) when
+ * normalize != 0 (the norm summed in fp64 in a fixed order).  Row b of x
+ * starts at x + b * x_row_stride.  Replaces AmplitudeEmbeddingBuilt.forward,
+ * qandle/embeddings.py:50-62 (pad then torch.nn.functional.normalize). */
+int64_t qg_amplitude_embedding_scratch_bytes(int64_t batch, int64_t len);
+int qg_amplitude_embedding(void* out, const float* x, int64_t x_row_stride, int64_t batch, int n, int64_t len,
+                           float pad_value, int normalize, void* scratch, int64_t scratch_bytes, void* stream);
+
 /* |psi|^2 of `count` amplitudes into float out[count].
  * Replaces MeasureAllAbsolute.forward, qandle/measurements.py:73-82. */
 int qg_probs(const void* state, float* out, int64_t count, void* stream);

@@ -1,8 +1,9 @@
 """qandle_gb300: a GB300 (sm_103a) state-vector engine behind qandle's front end.
 
 The public names mirror qandle's (qandle/__init__.py:3-14): gate layers
-(RX, RY, RZ, U, CNOT, CZ, SWAP), AngleEmbedding, measurements and
-StronglyEntanglingLayer build into torch modules, and ``Circuit`` runs them
+(RX, RY, RZ, U, CNOT, CZ, SWAP, Invert, Controlled, Reset), AngleEmbedding,
+AmplitudeEmbedding, measurements, StronglyEntanglingLayer and QConv build
+into torch modules, and ``Circuit`` runs them
 on hand-written CUDA kernels through the C ABI of libqandle_gb300.so.
 There is no CPU execution path: tensors must live on a CUDA device.
 """
@@ -14,6 +15,7 @@ from .embeddings import *
 from .measurements import *
 from .ansaetze import *
 from .qcircuit import *
+from .convolution import QConv
 from .errors import UnbuiltGateError
 
 __version__ = "1.0.0"

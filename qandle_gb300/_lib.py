@@ -76,6 +76,9 @@ SIGNATURES = {
                                              c_int, c_void_p]),
     "qg_apply_controlled_matrix": (c_int, [c_void_p, c_int64, c_int, c_int, c_int, c_void_p, c_int, c_void_p]),
     "qg_reset": (c_int, [c_void_p, c_int64, c_int, c_int, c_void_p]),
+    "qg_amplitude_embedding_scratch_bytes": (c_int64, [c_int64, c_int64]),
+    "qg_amplitude_embedding": (c_int, [c_void_p, c_void_p, c_int64, c_int64, c_int, c_int64, ctypes.c_float, c_int,
+                                       c_void_p, c_int64, c_void_p]),
     "qg_controlled_rotation_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_int, c_int, c_int,
                                             c_int, c_void_p, c_int64, c_void_p]),
     "qg_apply_cz": (c_int, [c_void_p, c_int64, c_int, c_int, c_int, c_void_p]),

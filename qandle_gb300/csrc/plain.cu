@@ -272,6 +272,51 @@ __device__ __forceinline__ float block_sum(float v, float* sh) {
     return r;  // valid in thread 0
 }
 
+// AmplitudeEmbedding (qandle/embeddings.py:29-66): the state is the real
+// feature vector, padded with pad_value to 2^n entries and optionally
+// divided by max(||.||_2, 1e-12) (torch.nn.functional.normalize).
+constexpr int kAmpChunkBits = 13;
+
+// partial sums of x^2 over chunks of one sample's features
+__global__ void k_amp_partial(const float* __restrict__ x, int64_t stride, int64_t len, int64_t nch,
+                              float* __restrict__ part) {
+    __shared__ float sh[32];
+    const int64_t b = blockIdx.x / nch, ch = blockIdx.x % nch;
+    const int64_t lo = ch << kAmpChunkBits;
+    int64_t hi = lo + (int64_t(1) << kAmpChunkBits);
+    if (hi > len) hi = len;
+    float acc = 0.f;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const float v = x[b * stride + i];
+        acc += v * v;
+    }
+    const float r = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+
+// 1 / max(norm, 1e-12) per sample, partials added in fp64 in chunk order
+__global__ void k_amp_norm(const float* __restrict__ part, int64_t batch, int64_t nch, double pad_sq,
+                           float* __restrict__ inv) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= batch) return;
+    double acc = pad_sq;
+    for (int64_t c = 0; c < nch; ++c) acc += part[b * nch + c];
+    const double nrm = sqrt(acc);
+    inv[b] = (float)(1.0 / (nrm > 1e-12 ? nrm : 1e-12));
+}
+
+__global__ void k_amp_write(float2* __restrict__ out, const float* __restrict__ x, int64_t stride, int64_t len,
+                            int n, int64_t total, float pad, const float* __restrict__ inv) {
+    int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    for (; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = u >> n, i = u & ((int64_t(1) << n) - 1);
+        float v = i < len ? x[b * stride + i] : pad;
+        if (inv) v *= inv[b];
+        out[u] = make_float2(v, 0.f);
+    }
+}
+
+
 // P0 partials: block (chunk, sample) writes, for each bit j < c, the sum of
 // |a|^2 over its amplitudes with bit j clear, and the chunk total at slot c.
 __global__ void k_p0_partial(const float2* __restrict__ s, float* __restrict__ part, int n, int c) {
@@ -460,6 +505,42 @@ int qg_apply_controlled_matrix(void* state, int64_t batch, int n, int control, i
     QG_CHECK_ARG(row_matrix != nullptr, "matrix is null");
     MatSrc ms{3, nullptr, 0, (const float2*)row_matrix, dagger};
     return launch_c1q(state, batch, n, control, qubit, ms, (cudaStream_t)stream);
+}
+
+int64_t qg_amplitude_embedding_scratch_bytes(int64_t batch, int64_t len) {
+    const int64_t nch = (len + (int64_t(1) << kAmpChunkBits) - 1) >> kAmpChunkBits;
+    return (batch * (nch > 0 ? nch : 1) + batch) * (int64_t)sizeof(float);
+}
+
+int qg_amplitude_embedding(void* out, const float* x, int64_t x_row_stride, int64_t batch, int n, int64_t len,
+                           float pad_value, int normalize, void* scratch, int64_t scratch_bytes, void* stream) {
+    int rc = check_state(out, batch, n);
+    if (rc) return rc;
+    QG_CHECK_ARG(x != nullptr, "x is null");
+    QG_CHECK_ARG(len >= 0 && len <= (int64_t(1) << n), "feature count must be in [0, 2^n]");
+    QG_CHECK_ARG(x_row_stride >= len, "x_row_stride must be >= the feature count");
+    cudaStream_t st = (cudaStream_t)stream;
+    const float* inv = nullptr;
+    if (normalize) {
+        QG_CHECK_ARG(scratch != nullptr && scratch_bytes >= qg_amplitude_embedding_scratch_bytes(batch, len),
+                     "scratch too small");
+        const int64_t nch = (len + (int64_t(1) << kAmpChunkBits) - 1) >> kAmpChunkBits;
+        float* part = (float*)scratch;
+        float* invb = part + batch * (nch > 0 ? nch : 1);
+        if (nch > 0) {
+            QG_CHECK_ARG(batch * nch < (int64_t(1) << 31), "batch * chunks must be < 2^31");
+            k_amp_partial<<<(unsigned)(batch * nch), kRedThreads, 0, st>>>(x, x_row_stride, len, nch, part);
+            QG_LAUNCH_CHECK();
+        }
+        const double pad_sq = (double)pad_value * pad_value * (double)((int64_t(1) << n) - len);
+        k_amp_norm<<<grid_for(batch, 128), 128, 0, st>>>(part, batch, nch, pad_sq, invb);
+        QG_LAUNCH_CHECK();
+        inv = invb;
+    }
+    const int64_t total = batch << n;
+    k_amp_write<<<grid_for(total, 256), 256, 0, st>>>((float2*)out, x, x_row_stride, len, n, total, pad_value, inv);
+    QG_LAUNCH_CHECK();
+    return QG_OK;
 }
 
 int qg_reset(void* state, int64_t batch, int n, int qubit, void* stream) {

@@ -14,7 +14,8 @@ import torch
 from . import operators as op
 from . import plain
 
-__all__ = ["AngleEmbedding", "AngleEmbeddingBuilt", "InputOperator", "InputOperatorBuilt"]
+__all__ = ["AngleEmbedding", "AngleEmbeddingBuilt", "AmplitudeEmbedding", "AmplitudeEmbeddingBuilt",
+           "InputOperator", "InputOperatorBuilt"]
 
 _ROT = {"x": 0, "y": 1, "z": 2}
 
@@ -82,3 +83,44 @@ class AngleEmbedding(InputOperator):
 
     def __str__(self) -> str:
         return f"AngleEmbedding_{self.rotation}"
+
+
+class AmplitudeEmbeddingBuilt(InputOperatorBuilt):
+    """Ignores the incoming state and sets the features as the state
+    (embeddings.py:29-66): padded with ``pad_with`` to 2^n entries,
+    optionally normalised, imaginary part 0."""
+
+    def __init__(self, name: str, num_qubits: int, normalize: bool, pad_with: typing.Union[float, None]):
+        super().__init__()
+        self.num_qubits = num_qubits
+        self.normalize = bool(normalize)
+        self.pad_with = pad_with
+        self.named = True
+        self.name = name
+
+    def forward(self, _=None, **kwargs):
+        x = torch.as_tensor(kwargs[self.name])
+        return plain.AmpEmbed.apply(x, self.num_qubits, self.pad_with, self.normalize)
+
+    def __str__(self) -> str:
+        return "AmplitudeEmbedding"
+
+
+class AmplitudeEmbedding(InputOperator):
+    """Amplitude embedding of a named input (embeddings.py:69-111)."""
+
+    def __init__(self, name: str, qubits: list, normalize: bool = False,
+                 pad_with: typing.Union[float, None] = None):
+        self.name = name
+        self.named = True
+        self.qubits = qubits
+        self.pad_with = pad_with
+        self.normalize = normalize
+
+    def build(self, num_qubits: int, **kwargs) -> AmplitudeEmbeddingBuilt:
+        assert num_qubits == len(self.qubits), "Current Implementation requires all qubits to be used."
+        return AmplitudeEmbeddingBuilt(num_qubits=num_qubits, normalize=self.normalize, pad_with=self.pad_with,
+                                       name=self.name)
+
+    def __str__(self) -> str:
+        return "AmplitudeEmbedding"

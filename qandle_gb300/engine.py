@@ -57,6 +57,7 @@ class Lowered:
         self.named_scale: list = []       # named column c is scaled by named_scale[c] (default 1)
         self.umats: list[torch.Tensor] = []
         self.measure = "state"
+        self.amp_embed = None  # AmplitudeEmbeddingBuilt that sets the initial state, if any
 
     def _rotation(self, axis: int, qubit: int, mod, scale: float = 1.0) -> None:
         if mod.named:
@@ -123,6 +124,12 @@ class Lowered:
             self._controlled(mod, inverse=False)
         elif name == "BuiltReset":
             raise NotFusible("Reset runs on the per-gate kernels")
+        elif name == "AmplitudeEmbeddingBuilt":
+            # overwrites the state: earlier layers are dead; the executor
+            # writes the embedded state and runs the program on it
+            self.gates, self.qlist, self.umats = [], [], []
+            self.param_mods, self.param_scale, self.named_cols, self.named_scale = [], [], [], []
+            self.amp_embed = mod
         elif name == "BuiltCNOT":
             self.gates.append((_lib.GATE["cnot"], mod.c, mod.t, 0, 0, 0))
         elif name == "BuiltCZ":
@@ -130,6 +137,7 @@ class Lowered:
         elif name == "BuiltSWAP":
             self.gates.append((_lib.GATE["swap"], mod.a, mod.b, 0, 0, 0))
         elif name == "AngleEmbeddingBuilt":
+            self.amp_embed = None  # a later embedding overwrites it
             qs = list(mod.qubits)
             self.gates.append((_lib.GATE["emb"], _rot_axis(mod.rotation), len(qs), 1,
                                len(self.named_cols), len(self.qlist)))
@@ -405,6 +413,8 @@ class FusedExecutor:
         if self.n < 5 or not self.fusible:
             # the fused tile needs five qubits in registers; tiny circuits run the per-gate kernels
             return self.circuit.forward(state, **kwargs)
+        if self.lowered.amp_embed is not None:
+            state = self.lowered.amp_embed(**kwargs)  # the embedded features are the input state
         dev = state.device if state is not None else self._device(kwargs)
         if dev.type != "cuda":
             raise RuntimeError("qandle_gb300 runs on CUDA tensors only; move the circuit and its inputs "

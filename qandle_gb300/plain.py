@@ -203,6 +203,54 @@ class Reset(torch.autograd.Function):
         return gin.reshape(sshape), None, None
 
 
+def _amp_embed_torch(x: torch.Tensor, n: int, pad_with, normalize: bool) -> torch.Tensor:
+    """AmplitudeEmbeddingBuilt.forward (qandle/embeddings.py:50-62) as torch
+    ops, for the backward of AmpEmbed."""
+    pad_len = (1 << n) - x.shape[-1]
+    if pad_len:
+        x = torch.nn.functional.pad(x, (0, pad_len), mode="constant", value=pad_with)
+    if normalize:
+        x = torch.nn.functional.normalize(x, p=2, dim=-1)
+    return torch.complex(x, torch.zeros_like(x))
+
+
+class AmpEmbed(torch.autograd.Function):
+    """AmplitudeEmbedding: real features padded to 2^n and optionally
+    normalised, as a complex64 state (CUDA kernel); the backward
+    differentiates the same formula."""
+
+    @staticmethod
+    def forward(ctx, x, n, pad_with, normalize):
+        xf = x.to(dtype=torch.float32)
+        lead = xf.shape[:-1]
+        x2 = xf.reshape(-1, xf.shape[-1]).contiguous()
+        if not x2.is_cuda:
+            raise RuntimeError("qandle_gb300 runs on CUDA tensors only; move the features with .to('cuda')")
+        B, L = x2.shape
+        if L > (1 << n):
+            raise ValueError(f"{L} features do not fit {n} qubits")
+        if L != (1 << n) and pad_with is None:
+            raise ValueError(f"{L} features for {n} qubits need pad_with")
+        out = torch.empty(B, 1 << n, dtype=torch.complex64, device=x2.device)
+        lib = _lib.load()
+        scr = _scratch(lib.qg_amplitude_embedding_scratch_bytes(B, L) if normalize else 16, x2.device)
+        _lib.call("qg_amplitude_embedding", out.data_ptr(), x2.data_ptr(), L, B, n, L,
+                  float(pad_with or 0.0), 1 if normalize else 0, scr.data_ptr(), scr.numel(), _lib.stream())
+        ctx.save_for_backward(x2)
+        ctx.meta = (n, pad_with, normalize, x.shape, x.dtype)
+        return out.reshape(*lead, 1 << n)
+
+    @staticmethod
+    def backward(ctx, g):
+        (x2,) = ctx.saved_tensors
+        n, pad_with, normalize, xshape, xdtype = ctx.meta
+        with torch.enable_grad():
+            xx = x2.detach().requires_grad_(True)
+            y = _amp_embed_torch(xx, n, pad_with, normalize)
+            (gx,) = torch.autograd.grad(y, xx, g.reshape(y.shape))
+        return gx.reshape(xshape).to(xdtype), None, None, None
+
+
 _PERM = {"cnot": "qg_apply_cnot", "cz": "qg_apply_cz", "swap": "qg_apply_swap"}
 
 
@@ -337,7 +385,7 @@ def run_layers_inplace(layers, state: torch.Tensor | None, n: int, kwargs: dict,
     unbatched = src.dim() == 1
     for mod in layers:
         name = type(mod).__name__
-        if name == "AngleEmbeddingBuilt":
+        if name in ("AngleEmbeddingBuilt", "AmplitudeEmbeddingBuilt"):
             st = mod(None, **kwargs)
             unbatched = st.dim() == 1
             st = st.reshape(-1, 1 << n)

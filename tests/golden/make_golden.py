@@ -444,6 +444,63 @@ def special_cases(qandle):
     return out
 
 
+def amplitude_cases(qandle):
+    """AmplitudeEmbedding (embeddings.py:29-111) with and without padding and
+    normalisation, its input gradient through a circuit, and QConv
+    (convolution.py:9-61) with the SEL angles recorded (their remapping set
+    to the identity: qandle's default remapping is qw_map.tanh, unpinned)."""
+    out = {}
+    gen = torch.Generator().manual_seed(21)
+    idx = 0
+    for n in range(1, 6):
+        for length in sorted({2 ** n, max(1, 2 ** n - 3), 1}):
+            for normalize in (False, True):
+                pad = None if length == 2 ** n else 0.25
+                x = torch.rand(4, length, generator=gen) + 0.1
+                op = qandle.AmplitudeEmbedding(name="x", qubits=list(range(n)), normalize=normalize,
+                                               pad_with=pad).build(num_qubits=n)
+                res = op(x=x)
+                out[f"a{idx}_x"] = x.numpy()
+                out[f"a{idx}_out"] = res.detach().numpy()
+                out[f"a{idx}_spec"] = np.array(json.dumps({"n": n, "normalize": normalize, "pad": pad}))
+                idx += 1
+    out["count"] = np.array(idx)
+    # input gradient through an amplitude-embedded circuit
+    n = 3
+    x = (torch.rand(3, 6, generator=gen) + 0.1).requires_grad_(True)
+    th = (torch.rand(n, generator=gen) * 6).tolist()
+    layers = [qandle.AmplitudeEmbedding(name="x", qubits=list(range(n)), normalize=True, pad_with=0.0)]
+    layers += [qandle.RY(qubit=q, theta=th[q], remapping=None) for q in range(n)]
+    layers += [qandle.CNOT(0, 1), qandle.CNOT(1, 2), qandle.MeasureProbability()]
+    circ = qandle.Circuit(layers, num_qubits=n)
+    p0 = circ(x=x)
+    (p0 * torch.arange(1, n + 1)).sum().backward()
+    out["grad_x"] = x.detach().numpy()
+    out["grad_th"] = np.array(th, dtype=np.float32)
+    out["grad_p0"] = p0.detach().numpy()
+    out["grad_dx"] = x.grad.numpy()
+    # QConv: SEL angles recorded, remapping set to the identity
+    for ci, (c_in, c_out, h, w, pad) in enumerate(((1, 3, 5, 6, 1), (2, 5, 4, 4, 0))):
+        torch.manual_seed(100 + ci)
+        conv = qandle.QConv(in_channels=c_in, out_channels=c_out, padding=pad)
+        thetas = []
+        for m in conv.qcircuit.circuit.layers[1].mods:
+            if hasattr(m, "theta"):
+                m.remapping = _qw_none
+                thetas.append(float(m.theta.detach()))
+        x = torch.rand(2, c_in, h, w, generator=gen)
+        y = conv(x)
+        out[f"qconv{ci}_x"] = x.numpy()
+        out[f"qconv{ci}_thetas"] = np.array(thetas, dtype=np.float32)
+        out[f"qconv{ci}_out"] = y.detach().numpy()
+        out[f"qconv{ci}_cfg"] = np.array(json.dumps({"c_in": c_in, "c_out": c_out, "padding": pad}))
+    return out
+
+
+def _qw_none(x):
+    return x
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("QANDLE_REFERENCE_SRC", ""))
@@ -461,6 +518,7 @@ def main():
         "reupload": reupload_cases,
         "circuits": circuit_cases,
         "special": special_cases,
+        "amplitude": amplitude_cases,
     }
     only = [g for g in args.only.split(",") if g]
     for name, fn in groups.items():

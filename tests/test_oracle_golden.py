@@ -198,3 +198,17 @@ def test_oracle_controlled_gradients_vs_reference_autograd():
     w = np.broadcast_to(np.arange(1, 5, dtype=np.float64), (3, 4)).copy()
     dth, _, _ = oracle.adjoint(desc, w, "p0", state=z["grad_in"])
     assert np.abs(dth - z["grad_out"]).max() < 1e-4
+
+
+def test_amplitude_formula_vs_reference():
+    """The torch restatement used by the amplitude embedding's backward
+    equals the reference's forward on every golden case (host-side logic)."""
+    import torch
+
+    from qandle_gb300 import plain
+
+    z = golden_io.load("amplitude")
+    for i in range(int(z["count"])):
+        spec = json.loads(str(z[f"a{i}_spec"]))
+        y = plain._amp_embed_torch(torch.tensor(z[f"a{i}_x"]), spec["n"], spec["pad"], spec["normalize"])
+        assert np.abs(y.numpy() - z[f"a{i}_out"]).max() < 1e-6, spec
