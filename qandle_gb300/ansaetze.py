@@ -90,6 +90,9 @@ class StronglyEntanglingLayerBuilt(op.BuiltOperator):
     def decompose(self):
         return [copy.deepcopy(m) for m in self.mods]
 
+    def to_qasm(self):
+        return [g.to_qasm() for g in self.decompose()]
+
     def to_matrix(self, **kwargs):
         m = None
         for mod in self.mods:

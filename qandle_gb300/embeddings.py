@@ -7,6 +7,7 @@ directly (8 bytes per amplitude, no matmuls).
 """
 from __future__ import annotations
 
+import random
 import typing
 
 import torch
@@ -64,6 +65,12 @@ class AngleEmbeddingBuilt(InputOperatorBuilt):
 
     def __str__(self) -> str:
         return f"AngleEmbedding_{self.rotation}"
+
+    def to_qasm(self):
+        """One named rotation per embedded qubit (embeddings.py:166-171)."""
+        rot = {0: op.RX, 1: op.RY, 2: op.RZ}[self.axis]
+        r = hash(random.random())
+        return [rot(qubit=w, name=f"angle_{r}_{w}").to_qasm() for w in self.qubits]
 
 
 class AngleEmbedding(InputOperator):

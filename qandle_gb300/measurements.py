@@ -9,6 +9,8 @@ counterpart in the reference: <Z_q> = P0_q - P1_q, which equals
 """
 from __future__ import annotations
 
+import random
+
 import torch
 
 from . import operators as op
@@ -22,6 +24,14 @@ __all__ = ["BuiltMeasurement", "UnbuiltMeasurement", "MeasureAllAbsolute", "Meas
 class BuiltMeasurement(op.BuiltOperator):
     def __str__(self) -> str:
         return "M"
+
+    def to_qasm(self):
+        """measure q[w] -> c[w] for every qubit (measurements.py:16-22)."""
+        from . import qasm
+
+        i = hash(random.random())
+        return [qasm.QasmRepresentation(gate_str=f"measure q[{w}] -> c[{w}]", qasm3_outputs=f"measured_{i}_{w}")
+                for w in range(self.num_qubits)]
 
     def to_matrix(self):
         return torch.eye(2 ** self.num_qubits)

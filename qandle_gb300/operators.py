@@ -19,7 +19,7 @@ import typing
 
 import torch
 
-from . import config, errors, plain, remap
+from . import config, errors, plain, qasm, remap
 
 __all__ = [
     "Operator", "UnbuiltOperator", "BuiltOperator",
@@ -35,6 +35,10 @@ class Operator(abc.ABC):
     """Everything that can be applied to a state (operators.py:35-49)."""
 
     named = False
+
+    def to_qasm(self):
+        """OpenQASM representation (qandle_gb300.qasm)."""
+        raise NotImplementedError(f"{type(self).__name__} has no OpenQASM representation")
 
     @abc.abstractmethod
     def __str__(self) -> str: ...
@@ -94,6 +98,9 @@ class U(UnbuiltOperator):
         return BuiltU(qubit=self.qubit, matrix=self.matrix, num_qubits=num_qubits)
 
 
+    def to_qasm(self):
+        return qasm.QasmRepresentation(gate_str="U", qubit=self.qubit)
+
 class BuiltU(BuiltOperator):
     """Built fixed gate (operators.py:87-129).  Keeps the 2x2 only."""
 
@@ -118,6 +125,13 @@ class BuiltU(BuiltOperator):
 
     def to_matrix(self, **kwargs) -> torch.Tensor:
         return self.matrix
+
+    def to_qasm(self):
+        m = torch.as_tensor(self.original_matrix)
+        u = f"{m[0, 0]:.2f}, {m[0, 1]:.2f}, {m[1, 0]:.2f}, {m[1, 1]:.2f}"
+        definition = "gate " + self.description + "_" + str(self.qubit) + " q[" + str(self.qubit) + "] {{ " + \
+            "U(" + u + ") }}"
+        return qasm.QasmRepresentation(gate_str=definition, qubit=self.qubit)
 
 
 CustomGate = BuiltU
@@ -153,6 +167,13 @@ class UnbuiltParametrizedOperator(UnbuiltOperator):
             qubit=self.qubit, initialtheta=self.theta, name=self.name,
             remapping=self.remapping, num_qubits=num_qubits)
 
+
+    def to_qasm(self):
+        if self.named:
+            return qasm.QasmRepresentation(gate_str=self.__class__.__name__.lower(), qubit=self.qubit,
+                                           qasm3_inputs=self.name)
+        return qasm.QasmRepresentation(gate_str=self.__class__.__name__.lower(), qubit=self.qubit,
+                                       gate_value=self.remapping(self.theta).item())
 
 class BuiltParametrizedOperator(BuiltOperator, abc.ABC):
     """Built rotation (operators.py:215-305): theta is a Parameter, the angle
@@ -201,6 +222,13 @@ class BuiltParametrizedOperator(BuiltOperator, abc.ABC):
         return _kron_embed(m2.reshape(2, 2), self.qubit, self.num_qubits)
 
 
+    def to_qasm(self):
+        if self.named:
+            return qasm.QasmRepresentation(gate_str=self.unbuilt_class.__name__.lower(), qubit=self.qubit,
+                                           qasm3_inputs=self.name)
+        return qasm.QasmRepresentation(gate_str=self.unbuilt_class.__name__.lower(), qubit=self.qubit,
+                                       gate_value=self.remapping(self.theta).item())
+
 class RX(UnbuiltParametrizedOperator):
     """Parametrised RX gate (operators.py:308-325)."""
 
@@ -240,6 +268,9 @@ class CNOT(UnbuiltOperator):
         return BuiltCNOT(control=self.c, target=self.t, num_qubits=num_qubits)
 
 
+    def to_qasm(self):
+        return qasm.QasmRepresentation(gate_str=f"cx q[{self.c}], q[{self.t}]")
+
 class CZ(UnbuiltOperator):
     """CZ gate (operators.py:518-533)."""
 
@@ -255,6 +286,9 @@ class CZ(UnbuiltOperator):
         return BuiltCZ(control=self.c, target=self.t, num_qubits=num_qubits)
 
 
+    def to_qasm(self):
+        return qasm.QasmRepresentation(gate_str=f"cz q[{self.c}], q[{self.t}]")
+
 class SWAP(UnbuiltOperator):
     """SWAP gate (operators.py:686-699)."""
 
@@ -268,6 +302,9 @@ class SWAP(UnbuiltOperator):
     def build(self, num_qubits, **kwargs) -> "BuiltSWAP":
         return BuiltSWAP(a=self.a, b=self.b, num_qubits=num_qubits)
 
+
+    def to_qasm(self):
+        return qasm.QasmRepresentation(gate_str=f"swap q[{self.a}], q[{self.b}]")
 
 def _perm_matrix(fn, num_qubits):
     dim = 2 ** num_qubits
@@ -299,6 +336,9 @@ class BuiltCNOT(BuiltOperator):
         return _perm_matrix(lambda i: ((i ^ (1 << t2)) if i & (1 << c2) else i, 1.0), n).T.contiguous()
 
 
+    def to_qasm(self):
+        return CNOT(self.c, self.t).to_qasm()
+
 class BuiltCZ(BuiltOperator):
     """Negate amplitudes with both bits set (operators.py:570-601)."""
 
@@ -320,6 +360,9 @@ class BuiltCZ(BuiltOperator):
         d = torch.tensor([-1.0 if (i & m) == m else 1.0 for i in range(2 ** n)], dtype=torch.complex64)
         return torch.diag(d)
 
+
+    def to_qasm(self):
+        return CZ(self.c, self.t).to_qasm()
 
 class BuiltSWAP(BuiltOperator):
     """Exchange two qubits (operators.py:653-684)."""
@@ -348,6 +391,9 @@ class BuiltSWAP(BuiltOperator):
         return _perm_matrix(f, n).T.contiguous()
 
 
+    def to_qasm(self):
+        return SWAP(self.a, self.b).to_qasm()
+
 class Invert(UnbuiltOperator):
     """Inverse of a target operator (operators.py:416-432)."""
 
@@ -360,6 +406,9 @@ class Invert(UnbuiltOperator):
     def build(self, num_qubits, **kwargs) -> "BuiltInvert":
         return BuiltInvert(target=self.t, num_qubits=num_qubits)
 
+
+    def to_qasm(self):
+        return qasm.QasmRepresentation(gate_str=f"{self.t}^-1")
 
 class BuiltInvert(BuiltOperator):
     """state @ inv(target matrix) (operators.py:435-459).  Rotations run as
@@ -397,6 +446,9 @@ class BuiltInvert(BuiltOperator):
         return torch.linalg.inv(self.target.to_matrix())
 
 
+    def to_qasm(self):
+        return Invert(self.target).to_qasm()
+
 class Controlled(UnbuiltOperator):
     """Apply the target operator where the control qubit is 1 (operators.py:462-478)."""
 
@@ -410,6 +462,9 @@ class Controlled(UnbuiltOperator):
     def build(self, num_qubits, **kwargs) -> "BuiltControlled":
         return BuiltControlled(control=self.c, target=self.t, num_qubits=num_qubits)
 
+
+    def to_qasm(self):
+        return qasm.QasmRepresentation(gate_str=f"controlled q[{self.c}], {self.t}")
 
 class BuiltControlled(BuiltOperator):
     """Target on the control-1 subspace, control-0 amplitudes kept
@@ -458,6 +513,9 @@ class BuiltControlled(BuiltOperator):
         return self.t.to_matrix()  # what the reference returns (operators.py:514-515)
 
 
+    def to_qasm(self):
+        return Controlled(self.c, self.t).to_qasm()
+
 class Reset(UnbuiltOperator):
     """Reset a qubit to |0> while preserving the norm (operators.py:632-650)."""
 
@@ -470,6 +528,9 @@ class Reset(UnbuiltOperator):
     def build(self, num_qubits, **kwargs) -> "BuiltReset":
         return BUILT_CLASS_RELATION[self.__class__](qubit=self.qubit, num_qubits=num_qubits)
 
+
+    def to_qasm(self):
+        return qasm.QasmRepresentation(gate_str="reset", qubit=self.qubit)
 
 class BuiltReset(BuiltOperator):
     """Per pair of amplitudes differing in the qubit: a0 * |pair| / (|a0| +
@@ -489,6 +550,9 @@ class BuiltReset(BuiltOperator):
     def to_matrix(self, **kwargs) -> torch.Tensor:
         raise ValueError("Reset gate does not have a matrix representation.")
 
+
+    def to_qasm(self):
+        return Reset(self.qubit).to_qasm()
 
 class rdict(dict):
     """Reversible dict (operators.py:702-706)."""

@@ -75,6 +75,28 @@ class Circuit(torch.nn.Module):
     def to_matrix(self, **kwargs):
         return self.circuit.to_matrix(**kwargs)
 
+    def to_qasm(self):
+        return self.circuit.to_qasm()
+
+    def to_openqasm2(self) -> str:
+        from . import qasm
+
+        return qasm.convert_to_qasm(self, qasm_version=2, include_header=True)
+
+    def to_openqasm3(self) -> str:
+        from . import qasm
+
+        return qasm.convert_to_qasm(self, qasm_version=3, include_header=True)
+
+    @classmethod
+    def from_qasm(cls, text: str, **options) -> "Circuit":
+        """A circuit from OpenQASM 2/3 text in the supported subset
+        (qandle_gb300.qasm.parse); named angles become named inputs."""
+        from . import qasm
+
+        layers, n = qasm.parse(text)
+        return cls(layers, num_qubits=n, **options)
+
     def __matmul__(self, x):
         return self.forward(x)
 
@@ -164,6 +186,13 @@ class UnsplittedCircuit(torch.nn.Module):
             else:
                 new_layers.append(layer)
         return UnsplittedCircuit(self.num_qubits, new_layers)
+
+    def to_qasm(self):
+        reps = []
+        for layer in self.layers:
+            if hasattr(layer, "to_qasm"):
+                reps.extend(layer.to_qasm())
+        return reps
 
     def to_matrix(self, **kwargs):
         m = None

@@ -73,6 +73,35 @@ def lower_description(desc: dict, pad_to: int = 5):
     return lo, np.asarray(params + [np.float32(0)], np.float32), named, shift
 
 
+def description_from_qasm(text: str, inputs: dict, batch: int, measure: str = "z") -> dict:
+    """A serving request from OpenQASM 2/3 text (the wire format): rx/ry/rz
+    with values or named inputs (``inputs[name]`` = [batch] angles), cx, cz,
+    swap.  The measurement is <Z> unless ``measure`` says otherwise."""
+    from . import operators, qasm
+
+    layers, n = qasm.parse(text)
+    gates = []
+    for lay in layers:
+        if isinstance(lay, operators.UnbuiltParametrizedOperator):
+            k = type(lay).__name__.lower()
+            if lay.named:
+                gates.append((k, lay.qubit, None, lay.name))
+            else:
+                gates.append((k, lay.qubit, float(lay.remapping(lay.theta).detach()), None))
+        elif isinstance(lay, operators.CNOT):
+            gates.append(("cnot", lay.c, lay.t))
+        elif isinstance(lay, operators.CZ):
+            gates.append(("cz", lay.c, lay.t))
+        elif isinstance(lay, operators.SWAP):
+            gates.append(("swap", lay.a, lay.b))
+        elif type(lay).__name__.startswith("Measure"):
+            continue
+        else:
+            raise ValueError(f"the serving loop does not take {type(lay).__name__}")
+    return {"name": "qasm", "n": n, "batch": batch, "gates": gates,
+            "inputs": {k: np.asarray(v, dtype=np.float32) for k, v in inputs.items()}, "measure": measure}
+
+
 def structure_key(lo: Lowered):
     return (lo.n, lo.measure, tuple(lo.gates), tuple(lo.qlist))
 

@@ -497,6 +497,30 @@ def amplitude_cases(qandle):
     return out
 
 
+def qasm_circuits(qandle_mod):
+    """Circuits whose OpenQASM export is compared as text (the random hash in
+    embedding and measurement names is normalised)."""
+    Q = qandle_mod
+    return {
+        "rot_fixed": ([Q.RX(0, theta=0.25, remapping=None), Q.RY(1, theta=-1.5, remapping=None),
+                       Q.RZ(2, theta=3.0, remapping=None), Q.CNOT(0, 2), Q.CZ(1, 2),
+                       Q.MeasureProbability()], 3),
+        "named": ([Q.AngleEmbedding(name="x", qubits=[0, 1, 2], rotation="ry"), Q.RZ(1, name="up", remapping=None),
+                   Q.CNOT(2, 0), Q.MeasureProbability()], 3),
+        "special": ([Q.Reset(qubit=1), Q.Controlled(0, Q.RY(1, theta=0.5, remapping=None)),
+                     Q.Invert(Q.RX(2, theta=0.75, remapping=None).build(num_qubits=3))], 3),
+    }
+
+
+def qasm_cases(qandle):
+    out = {}
+    for name, (layers, n) in qasm_circuits(qandle).items():
+        circ = qandle.Circuit(layers, num_qubits=n)
+        out[f"{name}_qasm2"] = np.array(circ.to_openqasm2())
+        out[f"{name}_qasm3"] = np.array(circ.to_openqasm3())
+    return out
+
+
 def _qw_none(x):
     return x
 
@@ -519,6 +543,7 @@ def main():
         "circuits": circuit_cases,
         "special": special_cases,
         "amplitude": amplitude_cases,
+        "qasm": qasm_cases,
     }
     only = [g for g in args.only.split(",") if g]
     for name, fn in groups.items():
