@@ -17,16 +17,33 @@ constexpr int kBwdRegBits = 4;
 // beside the psi/lambda double buffer, 5 B per slot and thread)
 __host__ __device__ constexpr int max_grad_per_pass(int reg_bits) { return reg_bits == 4 ? 64 : 96; }
 
-// Tile buffers of the forward kernel: three (tile t computes while tile t+1
-// loads and the bulk store of tile t-1 reads out).  Two 2^12 CTAs with three
-// buffers each still fit one SM's shared memory.
+// Tile buffers of the forward kernel: three (the compute warps work on tile
+// t while the producer warp stores tile t-2 out of the third buffer and then
+// loads tile t+1 into it).  Two 2^12 CTAs with three buffers each still fit
+// one SM's shared memory.
 __host__ __device__ constexpr int fwd_stages(int) { return 3; }
 
-// Resident CTAs per SM the register budget allows: 32 amplitudes per thread
-// (RB = 5) take up to 255 registers, 16 (RB = 4) up to 128.
-__host__ __device__ constexpr int fwd_min_blocks(int tb, int rb) {
-    return 65536 / ((1 << (tb - rb)) * (rb == 5 ? 256 : 128));
+// Producer warps of a forward CTA: they move the tiles between global and
+// shared memory, each warp a fixed share of every tile's rows.
+__host__ __device__ constexpr int fwd_producer_warps(int tb) { return tb >= 13 ? 4 : 2; }
+
+// Threads of a forward CTA: 2^(TB-RB) compute threads (2^RB amplitudes each)
+// and the producer warps.
+__host__ __device__ constexpr int fwd_threads(int tb, int rb) {
+    return (1 << (tb - rb)) + 32 * fwd_producer_warps(tb);
 }
+
+// Resident CTAs per SM the launch bounds ask for.  The compiler caps a thread
+// at 65536 / (threads x CTAs) registers: 168 for the compute threads of
+// RB = 5 (32 amplitudes), about 100 for RB = 4.
+__host__ __device__ constexpr int fwd_min_blocks(int tb, int rb) {
+    return tb >= 13 ? 1 : tb == 12 ? 2 : 3;
+}
+
+// Producer row-offset tables: a tile's 2^(TB-1) 16-byte chunks are copied as
+// lane + 32 * row, one table of 2^(TB-6) row offsets for the load and one
+// for the store side.
+__host__ __device__ constexpr int fwd_chunk_rows(int tb) { return 1 << (tb - 6); }
 
 // Device op codes (int4 per op: x = opcode, y/z/w operands).
 enum Opcode : int32_t {
@@ -116,10 +133,12 @@ struct RunArgs {
 constexpr int kSmemOps = 512;
 constexpr int kSmemMats = 256;
 
-// Dynamic shared memory of the forward kernel: the tile ring, the op list and
-// the shared matrix table.
+// Dynamic shared memory of the forward kernel: the tile ring, the op list,
+// the shared matrix table, the full/empty mbarrier of each tile buffer and the
+// producer's row-offset tables.
 __host__ __device__ constexpr int fwd_smem_bytes(int tb) {
-    return fwd_stages(tb) * (1 << tb) * 8 + kSmemOps * 16 + kSmemMats * 32;
+    return fwd_stages(tb) * (1 << tb) * 8 + kSmemOps * 16 + kSmemMats * 32 + 2 * fwd_stages(tb) * 8 +
+           2 * fwd_chunk_rows(tb) * 4;
 }
 
 // Dynamic shared memory of the backward kernel: psi and lambda double

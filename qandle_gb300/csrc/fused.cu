@@ -218,7 +218,7 @@ struct InterpOps {
 };
 
 template <int TB, int RB, int MAXJ>
-__global__ void __launch_bounds__(1 << (TB - RB), fwd_min_blocks(TB, RB))
+__global__ void __launch_bounds__(fwd_threads(TB, RB), fwd_min_blocks(TB, RB))
     k_fwd_pass(const __grid_constant__ JobTable<MAXJ> jt) {
     fwd_pass_body<TB, RB, MAXJ, InterpOps>(jt);
 }
@@ -501,7 +501,7 @@ static BwdLayout bwd_layout(const ProgramRun& R, int64_t B) {
 
 template <int TB, int RB, int MAXJ>
 static int launch_fwd_jobs(const JobTable<MAXJ>& jt, cudaStream_t st) {
-    constexpr int NT = 1 << (TB - RB);
+    constexpr int NT = fwd_threads(TB, RB);
     size_t smem = fwd_smem_bytes(TB);
     static bool attr_set = false;
     if (!attr_set) {
@@ -572,7 +572,7 @@ static int launch_fwd_compiled(const JitKernel& k, const PassDesc* dpass, const 
     int64_t slots = (int64_t)sm_count() * k.per_sm;
     int64_t grid = tiles < slots ? tiles : slots;
     void* params[] = {&jt};
-    return jit_launch(k, (unsigned)grid, 1u << (tb - rb), (size_t)fwd_smem_bytes(tb), st, params);
+    return jit_launch(k, (unsigned)grid, (unsigned)fwd_threads(tb, rb), (size_t)fwd_smem_bytes(tb), st, params);
 }
 
 template <int TB, int RB>

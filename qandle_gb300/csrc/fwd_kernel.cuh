@@ -3,13 +3,15 @@
 // program (jit.cpp).  Everything here is device code that needs no host
 // header, so the same text is handed to NVRTC.
 //
-// A pass walks tiles of 2^TB amplitudes: each tile is loaded by per-thread
-// async copies (cp.async) into one of a ring of shared-memory buffers, so
-// later tiles stream in while the current one is computed, and stored
-// straight from registers.  A thread holds 2^RB amplitudes in registers (planar.cuh); the
-// gate program of the pass runs on them (`Ops`), exchanging through the
-// tile's buffer when the register qubits change; the epilogue stores the
-// tile, its probabilities or P0 partials.
+// A pass walks tiles of 2^TB amplitudes through a ring of three shared-memory
+// buffers.  Producer warps move the tiles: they load tile t+1 with async
+// copies (cp.async) and store tile t-2 while the compute warps work on tile t,
+// and the two sides hand buffers over through a full and an empty mbarrier per
+// buffer.  A compute thread holds 2^RB amplitudes in registers
+// (planar.cuh); the gate program of the pass runs on them (`Ops`), exchanging
+// through the tile's buffer when the register qubits change; the epilogue
+// writes the tile back into its buffer and computes its probabilities or P0
+// partials.
 #pragma once
 #include "devmath.cuh"
 #include "engine.h"
@@ -33,13 +35,69 @@ __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.comm
 __device__ __forceinline__ void bulk_wait_read0() {
     asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
-template <int N>
-__device__ __forceinline__ void bulk_wait_read() {
-    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
-}
 __device__ __forceinline__ void bulk_wait_all0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// ---------------------------------------------- producer / compute sync --
+
+// Compute-warp barrier (named barrier 1): the producer warps of a forward CTA
+// never join it.  In a backward CTA, N is the whole block.
+template <int N>
+__device__ __forceinline__ void cta_sync() {
+    asm volatile("bar.sync 1, %0;" ::"n"(N) : "memory");
+}
+// cta_sync that also ANDs a flag over the N threads.
+template <int N>
+__device__ __forceinline__ bool cta_sync_and(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{ .reg .pred p, q; setp.ne.u32 p, %1, 0; bar.red.and.pred q, 1, %2, p; selp.u32 %0, 1, 0, q; }"
+        : "=r"(r)
+        : "r"((uint32_t)v), "n"(N)
+        : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+    asm volatile("{ .reg .b64 st; mbarrier.arrive.shared::cta.b64 st, [%0]; }" ::"r"(smem_u32(b)) : "memory");
+}
+// Arrive on b once every earlier cp.async of this thread has landed.
+__device__ __forceinline__ void mbar_arrive_cp_async(uint64_t* b) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+// Test for the completion of the phase of parity `parity`; a waiting thread
+// is suspended (up to about a millisecond) instead of polling shared memory.
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.b32 %0, 1, 0, p; }"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity), "r"(1000000u)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait for the phase of parity `parity` of b.  False when it did not
+// complete within about two seconds (or 2^16 tries): the caller reports
+// kStatusTimeout and winds the CTA down instead of waiting on.
+constexpr uint64_t kWaitNs = 2000000000ull;
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+    if (mbar_try_wait(b, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t i = 1; i < (1u << 16); ++i) {
+        if (mbar_try_wait(b, parity)) return true;
+        if (global_ns() - t0 > kWaitNs) return false;
+    }
+    return false;
 }
 
 // ------------------------------------------------------- tile geometry --
@@ -57,15 +115,59 @@ struct TileGeo {
     int tile_in_sample;   // n >= TB: tile index within the sample
 };
 
+// The low bits of v deposited into the set bits of mask, lowest first.
+__device__ __forceinline__ uint32_t deposit_bits(uint32_t v, uint32_t mask) {
+    uint32_t r = 0;
+    while (mask) {
+        const uint32_t low = mask & (0u - mask);
+        if (v & 1u) r |= low;
+        v >>= 1;
+        mask ^= low;
+    }
+    return r;
+}
+
+// Global bits of the qubits outside the tile, as a mask.
+__device__ __forceinline__ uint32_t fixed_mask_of(const PassDesc& d) {
+    uint32_t m = 0;
+    for (int k = 0; k < d.nfixed; ++k) m |= 1u << d.fixed_gbit[k];
+    return m;
+}
+
+// Geometry of tile t of a pass with tiles of 2^tile_bits amplitudes whose
+// outside qubits are the global bits in fixed_mask (register arithmetic only).
+__device__ __forceinline__ TileGeo tile_geo_m(int tile_bits, uint32_t fixed_mask, int64_t t, int n,
+                                              int64_t batch) {
+    TileGeo g;
+    if (n >= tile_bits) {
+        const int sh = n - tile_bits;  // tiles per sample = 2^sh
+        g.sample = t >> sh;
+        const uint32_t ti = (uint32_t)(t & ((int64_t(1) << sh) - 1));
+        g.tile_in_sample = (int)ti;
+        g.fixed_val = deposit_bits(ti, fixed_mask);
+        g.base = (g.sample << n) + g.fixed_val;
+        g.nsamples = 1;
+    } else {
+        int spt = 1 << (tile_bits - n);
+        g.sample = t * spt;
+        int64_t rem = batch - g.sample;
+        g.nsamples = rem < spt ? (int)rem : spt;
+        g.fixed_val = 0;
+        g.base = g.sample << n;
+        g.tile_in_sample = 0;
+    }
+    return g;
+}
+
 __device__ __forceinline__ TileGeo tile_geo(const PassDesc& d, int64_t t, int n, int64_t batch) {
     TileGeo g;
     if (n >= d.tile_bits) {
-        int64_t tps = int64_t(1) << (n - d.tile_bits);
-        g.sample = t / tps;
-        int64_t ti = t - g.sample * tps;
+        const int sh = n - d.tile_bits;  // tiles per sample = 2^sh
+        g.sample = t >> sh;
+        const uint32_t ti = (uint32_t)(t & ((int64_t(1) << sh) - 1));
         g.tile_in_sample = (int)ti;
         uint32_t fv = 0;
-        for (int k = 0; k < d.nfixed; ++k) fv |= (uint32_t)((ti >> k) & 1) << d.fixed_gbit[k];
+        for (int k = 0; k < d.nfixed; ++k) fv |= ((ti >> k) & 1u) << d.fixed_gbit[k];
         g.fixed_val = fv;
         g.base = (g.sample << n) + fv;
         g.nsamples = 1;
@@ -139,39 +241,6 @@ __device__ __forceinline__ void thread_tile_load(const PassDesc& d, const TileGe
         for (int k = 0; k < RB - 1; ++k)
             if ((i >> k) & 1) off ^= st[k];
         cp_async16(dst + 2 * (tid + i * NT), base + off);
-    }
-}
-
-// Tiles of at most 2^this contiguous blocks are stored by bulk copies.
-constexpr int kMaxBulkStoreBlocksLog2 = 4;
-
-// Local bits below the returned count map to the same global bits, so the
-// tile image is made of contiguous blocks of 2^count amplitudes (at least
-// the runs).
-__device__ __forceinline__ int contiguous_bits(const PassDesc& d) {
-    int e = d.run_bits;
-    while (e < d.tile_bits && d.gbit[e] == e) ++e;
-    return e;
-}
-
-// Bulk copies of a tile's state image from shared memory (local-index order)
-// to global memory, one per contiguous block; issued by the 32 lanes of one
-// warp, which then commit them as their bulk group.
-__device__ void issue_tile_store(const PassDesc& d, const TileGeo& g, float2* dstg, const float2* src, int n,
-                                 int lane) {
-    if (n < d.tile_bits) {
-        const uint32_t bytes = (uint32_t)((int64_t)g.nsamples << n) * 8u;
-        if (lane == 0) bulk_s2g(dstg + g.base, src, bytes);
-        return;
-    }
-    const int e = contiguous_bits(d);
-    const int blocks = 1 << (d.tile_bits - e);
-    const uint32_t bytes = (1u << e) * 8u;
-    for (int r = lane; r < blocks; r += 32) {
-        int64_t off = 0;
-        for (int k = 0; k < d.tile_bits - e; ++k)
-            if ((r >> k) & 1) off += int64_t(1) << d.gbit[e + k];
-        bulk_s2g(dstg + g.base + off, src + ((int64_t)r << e), bytes);
     }
 }
 
@@ -415,68 +484,215 @@ template <int TB, int RB>
 __device__ __forceinline__ void exchange(PTile<RB>& pt, uint32_t& xm, ThreadMap& tm, float* plane,
                                          const PassDesc& d, int32_t y, int32_t z, int32_t w, int tid,
                                          uint32_t fixed_val) {
-    __syncthreads();
+    cta_sync<(1 << (TB - RB))>();
     pxwrite_k<RB>(plane, pt, tm, tm.sw_base ^ xm_slot_offset<RB>(tm, xm), 1 << TB);
     xm = 0;
-    __syncthreads();
+    cta_sync<(1 << (TB - RB))>();
     decode_map<RB>(d, y, z, w, tid, fixed_val, tm);
     pxread_k<RB>(plane, pt, tm, 1 << TB);
+}
+
+// ---------------------------------------------------- producer warps --
+
+// The producer warps copy a tile as 2^(TB-1) chunks of 16 bytes (two
+// amplitudes: local bit 0 is global bit 0), chunk lane + 32 * row; warp w of
+// P takes rows [w R / P, (w + 1) R / P).  The lane part and the row part of a
+// chunk's global offset use distinct global bits and combine by XOR; the row
+// parts of the pass come from a table each warp fills for its rows whenever
+// the job of a side (load / store) changes.
+struct ChunkSide {
+    int job = -1;        // job whose pass the side holds
+    uint32_t lane_off;   // offset (amplitudes) of this lane's chunk in row 0
+    uint32_t fixed_mask; // global bits of the qubits outside the tile
+    int epi, ckpt;       // the pass's epilogue flags and checkpoint
+    bool loads;          // the pass reads its tiles from the state
+};
+
+// Point side `cs` at job j (reads the pass descriptor from global memory
+// once per job, not per tile).
+template <int TB, int MAXJ>
+__device__ __forceinline__ void chunk_side(ChunkSide& cs, uint32_t* tab, const JobTable<MAXJ>& jt, int j,
+                                           int r0, int r1, int lane) {
+    if (cs.job == j) return;
+    const PassDesc& pd = *jt.job[j].pd;
+    __syncwarp();  // every lane is done with the old table
+    for (int r = r0 + lane; r < r1; r += 32) {
+        uint32_t o = 0;
+        for (int k = 0; k < TB - 6; ++k)
+            if ((r >> k) & 1) o ^= 1u << pd.gbit[6 + k];
+        tab[r] = o;
+    }
+    uint32_t lo = 0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+        if ((lane >> k) & 1) lo ^= 1u << pd.gbit[1 + k];
+    cs.lane_off = lo;
+    cs.fixed_mask = fixed_mask_of(pd);
+    cs.epi = pd.epi;
+    cs.ckpt = pd.ckpt;
+    cs.loads = pd.init == INIT_LOAD && !jt.job[j].zero_init;
+    cs.job = j;
+    __syncwarp();
+}
+
+// Async copies of one tile's state image (global, from `src` = amplitude 0
+// of the tile) into `dst` in local-index order.
+template <int RPW>
+__device__ __forceinline__ void producer_load(float2* dst, const float2* src, const ChunkSide& cs,
+                                              const uint32_t* tab, bool whole, int64_t lim_chunks, int r0,
+                                              int lane) {
+    if (whole) {  // n < TB: whole samples, the tile image is contiguous
+        for (int r = r0; r < r0 + RPW; ++r) {
+            const int c = lane + 32 * r;
+            if (c < lim_chunks) cp_async16(dst + 2 * c, src + 2 * c);
+        }
+        return;
+    }
+#pragma unroll 8
+    for (int r = r0; r < r0 + RPW; ++r) cp_async16(dst + 2 * (lane + 32 * r), src + (cs.lane_off ^ tab[r]));
+}
+
+// One tile's state image from shared memory (local-index order) to global
+// memory, eight 16-byte chunks in flight per lane.
+template <int RPW>
+__device__ __forceinline__ void producer_store(const float2* src, float2* dst, const ChunkSide& cs,
+                                               const uint32_t* tab, bool whole, int64_t lim_chunks, int r0,
+                                               int lane) {
+    constexpr int K = RPW < 8 ? RPW : 8;  // chunks in flight per lane
+    for (int rb = r0; rb < r0 + RPW; rb += K) {
+        float4 v[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            v[k] = *reinterpret_cast<const float4*>(src + 2 * (lane + 32 * (rb + k)));
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int c = lane + 32 * (rb + k);
+            if (whole) {
+                if (c < lim_chunks) *reinterpret_cast<float4*>(dst + 2 * c) = v[k];
+            } else {
+                *reinterpret_cast<float4*>(dst + (cs.lane_off ^ tab[rb + k])) = v[k];
+            }
+        }
+    }
+}
+
+// A producer warp: for the CTA's i-th tile (buffer i % S) it first stores its
+// rows of tile i - S out of that buffer once the compute warps released it
+// (empty barrier), then loads its rows of tile i into it and arrives on the
+// full barrier when the copies land.  Tiles whose pass does not load (|0..0> start, embedding)
+// get a plain arrive: the compute warps still need the buffer.
+template <int TB, int MAXJ>
+__device__ __forceinline__ void fwd_producer(const JobTable<MAXJ>& jt, float2* bufs, uint64_t* bar_full,
+                                             uint64_t* bar_empty, uint32_t* tabs, int ptid) {
+    constexpr int AMPS = 1 << TB;
+    constexpr int S = fwd_stages(TB);
+    constexpr int ROWS = 1 << (TB - 6);
+    constexpr int RPW = ROWS / fwd_producer_warps(TB);  // rows per producer warp
+    const int lane = ptid & 31;
+    const int r0 = (ptid >> 5) * RPW;
+    const int64_t total = jt.begin[jt.njobs];
+    const int64_t G = gridDim.x;
+    const int64_t t0 = blockIdx.x;
+    const int64_t mine = (total - t0 + G - 1) / G;  // tiles of this CTA
+    ChunkSide ld, st;
+    uint32_t* tab_ld = tabs;
+    uint32_t* tab_st = tabs + ROWS;
+    int failed_job = -1;
+    for (int64_t i = 0; i < mine + S; ++i) {
+        const int s = (int)(i % S);
+        float2* buf = bufs + s * AMPS;
+        if (i >= S) {
+            const int64_t t = t0 + (i - S) * G;
+            const int j = find_job(jt, t);
+            if (!mbar_wait(bar_empty + s, (uint32_t)((i / S - 1) & 1))) {
+                failed_job = j;
+                break;
+            }
+            chunk_side<TB>(st, tab_st, jt, j, r0, r0 + RPW, lane);
+            if (st.epi & EPI_STORE) {
+                const RunArgs& A = jt.job[j].A;
+                const bool whole = A.n < TB;
+                const TileGeo g = tile_geo_m(TB, st.fixed_mask, t - jt.begin[j], A.n, A.batch);
+                const int64_t lim = ((int64_t)g.nsamples << A.n) >> 1;
+                producer_store<RPW>(buf, A.state + g.base, st, tab_st, whole, lim, r0, lane);
+                if (st.ckpt >= 0)
+                    producer_store<RPW>(buf, A.ckpt + (int64_t)st.ckpt * (A.batch << A.n) + g.base, st, tab_st,
+                                        whole, lim, r0, lane);
+            }
+            __syncwarp();  // the warp has read its rows out before it refills them
+        }
+        if (i < mine) {
+            const int64_t t = t0 + i * G;
+            const int j = find_job(jt, t);
+            chunk_side<TB>(ld, tab_ld, jt, j, r0, r0 + RPW, lane);
+            if (ld.loads) {
+                const RunArgs& A = jt.job[j].A;
+                const bool whole = A.n < TB;
+                const TileGeo g = tile_geo_m(TB, ld.fixed_mask, t - jt.begin[j], A.n, A.batch);
+                const int64_t lim = ((int64_t)g.nsamples << A.n) >> 1;
+                producer_load<RPW>(buf, A.state + g.base, ld, tab_ld, whole, lim, r0, lane);
+                mbar_arrive_cp_async(bar_full + s);
+            } else {
+                mbar_arrive(bar_full + s);
+            }
+        }
+    }
+    cp_async_wait<0>();  // the warp's copies have landed before it leaves
+    if (failed_job >= 0 && lane == 0) atomicExch(jt.job[failed_job].A.status, kStatusTimeout);
 }
 
 // Body of the forward pass kernel.  One persistent CTA per SM walks the tiles
 // of every job of the launch (the passes of independent programs / states,
 // e.g. several serving requests of different widths); a single-program
-// forward is a one-job launch.  Ops::apply runs the pass's gate program on
-// the thread's tile.
+// forward is a one-job launch.  The CTA's last warps are producers
+// (fwd_producer): they move tiles between global memory and a ring of three
+// shared-memory buffers, so the compute warps only read a tile out of its
+// buffer into registers, run the pass's gate program on it (Ops::apply,
+// exchanging through the same buffer), and write the result back.
 template <int TB, int RB, int MAXJ, class Ops>
 __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
     constexpr int NT = 1 << (TB - RB);
     constexpr int AMPS = 1 << TB;
-    constexpr int S = fwd_stages(TB);  // tile buffers: loads run S-1 tiles ahead
+    constexpr int S = fwd_stages(TB);
+    static_assert(S == 3, "the producer ring is three tile buffers");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* bufs = reinterpret_cast<float2*>(smem_raw);
     int4* s_ops = reinterpret_cast<int4*>(bufs + S * AMPS);         // [kSmemOps]
     float4* s_mats = reinterpret_cast<float4*>(s_ops + kSmemOps);   // [kSmemMats][2]
+    uint64_t* bar_full = reinterpret_cast<uint64_t*>(s_mats + 2 * kSmemMats);  // [S]
+    uint64_t* bar_empty = bar_full + S;                                        // [S]
+    uint32_t* s_tabs = reinterpret_cast<uint32_t*>(bar_empty + S);             // [2][chunk rows]
     __shared__ PassDesc sd;
     __shared__ RunArgs sa;
 
     const int tid = threadIdx.x;
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(bar_full + s, 32 * fwd_producer_warps(TB));  // every producer thread
+            mbar_init(bar_empty + s, NT / 32);  // lane 0 of every compute warp
+        }
+    }
+    __syncthreads();  // the only barrier the producer joins
+    if (tid >= NT) {
+        fwd_producer<TB, MAXJ>(jt, bufs, bar_full, bar_empty, s_tabs, tid - NT);
+        return;
+    }
+
     const int lane = tid & 31;
     const int64_t total = jt.begin[jt.njobs];
-
-    auto tile_loads = [&](int j) -> bool {
-        return jt.job[j].pd->init == INIT_LOAD && !jt.job[j].zero_init;
-    };
-    // Buffer ring (S = 3): tile t computes in buffer t % 3 while tile t + 1
-    // loads into the next buffer and the bulk store of tile t - 1 reads out of
-    // the previous one.  Every thread commits exactly one copy group per
-    // prefetch (empty when there is nothing to load), so "tile t has landed"
-    // is cp.async.wait_group 0 followed by a CTA barrier; warp 0 commits one
-    // bulk-store group per tile (empty when the tile stores nothing).
-    auto issue_prefetch = [&](int64_t t, float2* dst) {
-        if (t < total) {
-            const int j = find_job(jt, t);
-            if (tile_loads(j)) {
-                const PassDesc& pd = *jt.job[j].pd;
-                const RunArgs& ra = jt.job[j].A;
-                TileGeo gn = tile_geo(pd, t - jt.begin[j], ra.n, ra.batch);
-                thread_tile_load<TB, RB>(pd, gn, ra.state, dst, ra.n, tid);
-            }
-        }
-        cp_async_commit();
-    };
-
-    static_assert(S == 3, "the store write-behind needs three tile buffers");
+    const int64_t G = gridDim.x;
     const int64_t t0 = blockIdx.x;
-    issue_prefetch(t0, bufs);
     int cur_job = -1;
     int iter = 0;
-    for (int64_t t = t0; t < total; t += gridDim.x, ++iter) {
+    int staged_iter = -1;  // iteration whose per-tile data of Ops is already on its way
+    uint32_t fmask = 0;    // global bits of the qubits outside the tile (current job)
+    bool ok = true;
+    for (int64_t t = t0; t < total; t += G, ++iter) {
         const int slot = iter % S;
         float2* buf = bufs + slot * AMPS;
         const int j = find_job(jt, t);
         if (j != cur_job) {
-            __syncthreads();  // nobody reads the previous job's descriptors any more
+            cta_sync<NT>();  // nobody reads the previous job's descriptors any more
             if (tid == 0) {
                 sd = *jt.job[j].pd;
                 sa = jt.job[j].A;
@@ -491,27 +707,29 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
             const int nm = jt.job[j].A.nslots_shared < kSmemMats ? jt.job[j].A.nslots_shared : kSmemMats;
             const float4* gm = reinterpret_cast<const float4*>(jt.job[j].A.mats);
             for (int i = tid; i < 2 * nm; i += NT) s_mats[i] = __ldg(gm + i);
-            __syncthreads();
+            cta_sync<NT>();
+            fmask = fixed_mask_of(sd);
             cur_job = j;
         }
         const PassDesc& d = sd;
         const RunArgs& A = sa;
         const int4* ops = jt.job[j].ops;
         const int n = A.n;
-        const bool load_in = tile_loads(j);
-        TileGeo g = tile_geo(d, t - jt.begin[j], n, A.batch);
+        const bool load_in = jt.job[j].pd->init == INIT_LOAD && !jt.job[j].zero_init;
+        const TileGeo g = tile_geo_m(TB, fmask, t - jt.begin[j], n, A.batch);
+        float4* const half = reinterpret_cast<float4*>(s_ops) + (iter & 1) * (kSmemOps / 2);
+        // per-tile data of Ops (in the op-list area when it is not staged;
+        // two halves alternate by tile), usually issued one tile ahead
+        if (staged_iter != iter) Ops::template tile_start<TB, RB>(A, g, half, tid);
+        const bool landed = mbar_wait(bar_full + slot, (uint32_t)((iter / S) & 1));
+        cp_async_wait<0>();  // this thread's copies of the per-tile data
+        if (!cta_sync_and<NT>(landed)) {
+            ok = false;
+            break;
+        }
         PTile<RB> pt;
         uint32_t xm = 0;  // pending thread-controlled X per register bit
         ThreadMap tm;
-        // per-tile data of Ops (in the op-list area when it is not staged;
-        // two halves alternate by tile), published by the barrier below
-        Ops::template tile_start<TB, RB>(A, g, reinterpret_cast<float4*>(s_ops) + (iter & 1) * (kSmemOps / 2),
-                                         tid);
-        cp_async_wait<0>();  // this thread's copies of tile t have landed
-        // warp 0: the bulk store of tile t - 2 has read its buffer out (it had
-        // all of tile t - 1 to do so), so that buffer can take tile t + 1
-        if (tid < 32) bulk_wait_read<1>();
-        __syncthreads();  // tile t has landed everywhere; buffer (t + 1) % 3 is free
         if (load_in) {
             pload_nat<RB>(pt, buf, tid);
             decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
@@ -558,58 +776,35 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 }
             }
         }
-        // prefetch tile t + 1 into the buffer tile t - 2 used
-        issue_prefetch(t + (int64_t)gridDim.x, bufs + ((iter + 1) % S) * AMPS);
+        // the next tile's per-tile data of Ops, into the other half (its
+        // last reader, tile t - 1, is done: the barrier above)
+        if (t + G < total && find_job(jt, t + G) == j) {
+            const TileGeo gn = tile_geo_m(TB, fmask, t + G - jt.begin[j], n, A.batch);
+            Ops::template tile_start<TB, RB>(A, gn, reinterpret_cast<float4*>(s_ops) + ((iter + 1) & 1) * (kSmemOps / 2),
+                                             tid);
+            staged_iter = iter + 1;
+        }
         // ---- the gate program of this pass ----
         // (the op list when Ops reads it, else this tile's half of the staged data)
         Ops::template apply<TB, RB>(pt, xm, tm, d, A, ops,
-                                    Ops::kStageOps ? s_ops : s_ops + (iter & 1) * (kSmemOps / 2), s_mats,
+                                    Ops::kStageOps ? s_ops : reinterpret_cast<const int4*>(half), s_mats,
                                     reinterpret_cast<float*>(buf), g.sample, g.fixed_val, tid);
         // ---- epilogue (the planner left the natural mapping) ----
-        const bool bulk_store = n < TB || d.tile_bits - contiguous_bits(d) <= kMaxBulkStoreBlocksLog2;
-        const bool epi_uses_buf = (d.epi & (EPI_PROBS | EPI_P0)) || ((d.epi & EPI_STORE) && bulk_store);
-        if (epi_uses_buf) __syncthreads();  // all exchange reads of `buf` are done
         const int64_t smp0 = g.sample;
-        // A tile made of a few large contiguous blocks is written back by bulk
-        // copies that read the buffer while the next tile computes; a tile of
-        // many small runs is stored straight from registers (one copy engine
-        // working through many 512-byte runs is slower than the warps).
-        if (d.epi & EPI_STORE) {
-            if (bulk_store) {
-                pstore_nat<RB>(pt, buf, tid, xm);
-                fence_proxy_async();
-                __syncthreads();
-                if (tid < 32) {
-                    issue_tile_store(d, g, A.state, buf, n, lane);
-                    if (d.ckpt >= 0)
-                        issue_tile_store(d, g, A.ckpt + (int64_t)d.ckpt * (A.batch << n), buf, n, lane);
-                }
-            } else {
-                pstore_global<RB>(pt, xm, d, g, A.state, n, tid);
-                if (d.ckpt >= 0)
-                    pstore_global<RB>(pt, xm, d, g, A.ckpt + (int64_t)d.ckpt * (A.batch << n), n, tid);
-            }
-        }
         if (d.epi & (EPI_PROBS | EPI_P0)) {
-            if ((d.epi & EPI_STORE) && bulk_store) {  // the probabilities reuse the buffer: let the store read it first
-                if (tid < 32) {
-                    bulk_commit();
-                    bulk_wait_read0();
-                }
-                __syncthreads();
-            }
+            cta_sync<NT>();  // all exchange reads of `buf` are done
             float* pb = reinterpret_cast<float*>(buf);
             pstore_probs<RB>(pt, pb, tid, xm);
             if (d.epi & EPI_PROBS) {
                 fence_proxy_async();
-                __syncthreads();
+                cta_sync<NT>();
                 if (tid < 32) {
                     issue_tile_store_f32(d, g, A.out, pb, n, lane);
                     bulk_commit();
                     bulk_wait_read0();
                 }
             }
-            __syncthreads();
+            cta_sync<NT>();
             if (d.epi & EPI_P0) {
                 // phase A: thread t owns the 2^RB consecutive probabilities of chunk t
                 constexpr int CH = 1 << RB;
@@ -630,7 +825,7 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 ptot[tid] = tot;
 #pragma unroll
                 for (int jj = 0; jj < RB; ++jj) psub[jj * NT + tid] = sj[jj];
-                __syncthreads();
+                cta_sync<NT>();
                 // phase B: (sample, local bit) items
                 const int nq = d.nq_tile;
                 const int cps = 1 << (nq - RB);           // chunks (threads) per sample
@@ -674,12 +869,18 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 }
             }
         }
-        if (tid < 32) bulk_commit();  // this tile's store group (possibly empty)
-        // No barrier here: the next tile's first barrier orders everything
-        // that touches shared memory (the staged per-sample data alternates
-        // between two halves, and `buf` is refilled only two tiles later).
+        if (d.epi & EPI_STORE) {
+            cta_sync<NT>();  // all reads of `buf` (exchanges, probabilities) are done
+            pstore_nat<RB>(pt, buf, tid, xm);
+        }
+        // the warp is done with the buffer (and its part of the state image
+        // is in it when the pass stores): the producer writes it out and
+        // refills the buffer
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar_empty + slot);
     }
-    if (tid < 32) bulk_wait_all0();
+    if (!ok && tid == 0) atomicExch(sa.status, kStatusTimeout);
+    if (tid < 32) bulk_wait_all0();  // probability stores have completed
 }
 
 

@@ -218,12 +218,12 @@ std::string exchange_code(const PassDesc& d, const MapBits& cur, int32_t y, int3
     const MapBits nxt = decode_mapping(y, z, w, rb);
     const std::string cc = reg_offsets(cur, rb), cn = reg_offsets(nxt, rb);
     std::ostringstream s;
-    s << "{ __syncthreads(); const int wb_ = swb ^ xm_xor<" << cc << ">(xm); ";
+    s << "{ cta_sync<(1 << (TB - RB))>(); const int wb_ = swb ^ xm_xor<" << cc << ">(xm); ";
     if (two)
         s << "cxwrite<TB, RB, " << cc << ">(pp, pt, wb_); cxwrite<TB, RB, " << cc << ">(lp, lt, wb_); ";
     else
         s << "cxwrite<TB, RB, " << cc << ">(plane, pt, wb_); ";
-    s << "xm = 0; __syncthreads(); " << thread_part(nxt, d) << " ";
+    s << "xm = 0; cta_sync<(1 << (TB - RB))>(); " << thread_part(nxt, d) << " ";
     if (two)
         s << "cxread<TB, RB, " << cn << ">(pp, pt, swb); cxread<TB, RB, " << cn << ">(lp, lt, swb); }\n";
     else
@@ -239,9 +239,10 @@ std::string pass_source(const ProgramRun& R, int p) {
     const int nt = 1 << (tb - rb);
     const int32_t* ops = R.fops + 4 * (size_t)d.op_begin;
     // With n >= TB a tile lies in one sample, so the pass's per-sample
-    // matrices are the same for the whole CTA: they are copied into shared
-    // memory (the op-list area, unused here) at each tile's start instead of
-    // being read from global memory by every thread at every op.
+    // matrices are the same for the whole CTA: async copies put them into
+    // shared memory (the op-list area, unused here; two halves alternate by
+    // tile) while the tile before computes, instead of every thread reading
+    // them from global memory at every op.
     std::vector<int32_t> staged;  // per-sample slot of each staged matrix
     std::map<int32_t, int> staged_index;
     if (R.n >= tb) {
@@ -270,8 +271,9 @@ std::string pass_source(const ProgramRun& R, int p) {
         s << "    if (tid < " << 2 * staged.size() << ") {\n      const int k = tid >> 1;\n      const int slot = ";
         for (size_t i = 0; i + 1 < staged.size(); ++i) s << "k == " << i << " ? " << staged[i] << " : ";
         s << staged.back() << ";\n"
-          << "      sm[tid] = __ldg(reinterpret_cast<const float4*>(A.mats_ps + (g.sample * A.nslots_ps + slot) * 4)"
-             " + (tid & 1));\n    }\n";
+          << "      cp_async16(sm + tid, reinterpret_cast<const float4*>(A.mats_ps + (g.sample * A.nslots_ps + slot) * 4)"
+             " + (tid & 1));\n    }\n"
+          << "    cp_async_commit();\n";
     }
     s << "  }\n"
          "  template <int TB, int RB>\n"
@@ -354,7 +356,8 @@ std::string pass_source(const ProgramRun& R, int p) {
         }
     }
     s << "  }\n};\n}  // namespace qg\n"
-      << "extern \"C\" __global__ void __launch_bounds__(" << nt << ", " << fwd_min_blocks(tb, rb) << ")\n"
+      << "extern \"C\" __global__ void __launch_bounds__(" << fwd_threads(tb, rb) << ", " << fwd_min_blocks(tb, rb)
+      << ")\n"
       << "qg_fwd_pass(const __grid_constant__ qg::JobTable<1> jt) {\n"
       << "  qg::fwd_pass_body<" << tb << ", " << rb << ", 1, qg::PassOps>(jt);\n}\n";
     return s.str();
@@ -702,7 +705,8 @@ int qg_program_compile(qg_program* prog, int flags) {
                 const int tb = t.bwd ? R.bpass[t.pass].tile_bits : R.fpass[t.pass].tile_bits;
                 const int rb = t.bwd ? kBwdRegBits : R.reg_bits;
                 const int smem = t.bwd ? bwd_smem_bytes(tb, rb) : fwd_smem_bytes(tb);
-                int rc = load_cubin(cubins[i], t.bwd ? "qg_bwd_pass" : "qg_fwd_pass", smem, 1 << (tb - rb), L, err);
+                const int threads = t.bwd ? 1 << (tb - rb) : fwd_threads(tb, rb);
+                int rc = load_cubin(cubins[i], t.bwd ? "qg_bwd_pass" : "qg_fwd_pass", smem, threads, L, err);
                 if (rc) return set_error("qg_program_compile: " + name(t) + ": " + err), rc;
                 it = g_cache.emplace(std::make_pair(dev, t.src), L).first;
             }

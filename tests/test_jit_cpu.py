@@ -29,7 +29,7 @@ def test_source_unrolls_every_op():
         skip = ("const float4* staged", "(void)staged;")
         skip = skip + ("int swb", "(void)swb;")
         calls = [ln for ln in body.splitlines()[1:]
-                 if (ln.strip().endswith(";") or ln.strip().startswith("{ __syncthreads();"))
+                 if (ln.strip().endswith(";") or ln.strip().startswith("{ cta_sync<"))
                  and not ln.strip().startswith(skip)]
         assert len(calls) == len(pd["ops"]), p
         assert "switch" not in src and "qg_fwd_pass" in src
