@@ -494,109 +494,93 @@ __device__ __forceinline__ void exchange(PTile<RB>& pt, uint32_t& xm, ThreadMap&
 
 // ---------------------------------------------------- producer warps --
 
-// The producer warps copy a tile as 2^(TB-1) chunks of 16 bytes (two
-// amplitudes: local bit 0 is global bit 0), chunk lane + 32 * row; warp w of
-// P takes rows [w R / P, (w + 1) R / P).  The lane part and the row part of a
-// chunk's global offset use distinct global bits and combine by XOR; the row
-// parts of the pass come from a table each warp fills for its rows whenever
-// the job of a side (load / store) changes.
-struct ChunkSide {
-    int job = -1;        // job whose pass the side holds
-    uint32_t lane_off;   // offset (amplitudes) of this lane's chunk in row 0
-    uint32_t fixed_mask; // global bits of the qubits outside the tile
-    int epi, ckpt;       // the pass's epilogue flags and checkpoint
-    bool loads;          // the pass reads its tiles from the state
+// The producer warps copy a tile as blocks of 2^cb amplitudes, cb being the
+// number of low local bits that map to the same global bits: each block is
+// contiguous in global memory and in the tile image, and moves with one bulk
+// (TMA) copy.  Producer thread p takes blocks p, p + 32 P, ...; a block's
+// global offset deposits its index into the tile's higher global bits.
+struct BlockSide {
+    int job = -1;         // job whose pass the side holds
+    int cb;               // log2 amplitudes per block
+    int nblk;             // blocks per tile (n >= TB)
+    uint32_t fixed_mask;  // global bits of the qubits outside the tile
+    int epi, ckpt;        // the pass's epilogue flags and checkpoint
+    bool loads;           // the pass reads its tiles from the state
 };
 
-// Point side `cs` at job j (reads the pass descriptor from global memory
-// once per job, not per tile).
 template <int TB, int MAXJ>
-__device__ __forceinline__ void chunk_side(ChunkSide& cs, uint32_t* tab, const JobTable<MAXJ>& jt, int j,
-                                           int r0, int r1, int lane) {
+__device__ __forceinline__ void block_side(BlockSide& cs, const JobTable<MAXJ>& jt, int j) {
     if (cs.job == j) return;
     const PassDesc& pd = *jt.job[j].pd;
-    __syncwarp();  // every lane is done with the old table
-    for (int r = r0 + lane; r < r1; r += 32) {
-        uint32_t o = 0;
-        for (int k = 0; k < TB - 6; ++k)
-            if ((r >> k) & 1) o ^= 1u << pd.gbit[6 + k];
-        tab[r] = o;
-    }
-    uint32_t lo = 0;
-#pragma unroll
-    for (int k = 0; k < 5; ++k)
-        if ((lane >> k) & 1) lo ^= 1u << pd.gbit[1 + k];
-    cs.lane_off = lo;
+    int e = pd.run_bits;
+    while (e < TB && pd.gbit[e] == e) ++e;
+    cs.cb = e;
+    cs.nblk = 1 << (TB - e);
     cs.fixed_mask = fixed_mask_of(pd);
     cs.epi = pd.epi;
     cs.ckpt = pd.ckpt;
     cs.loads = pd.init == INIT_LOAD && !jt.job[j].zero_init;
     cs.job = j;
-    __syncwarp();
 }
 
-// Async copies of one tile's state image (global, from `src` = amplitude 0
-// of the tile) into `dst` in local-index order.
-template <int RPW>
-__device__ __forceinline__ void producer_load(float2* dst, const float2* src, const ChunkSide& cs,
-                                              const uint32_t* tab, bool whole, int64_t lim_chunks, int r0,
-                                              int lane) {
-    if (whole) {  // n < TB: whole samples, the tile image is contiguous
-        for (int r = r0; r < r0 + RPW; ++r) {
-            const int c = lane + 32 * r;
-            if (c < lim_chunks) cp_async16(dst + 2 * c, src + 2 * c);
-        }
-        return;
-    }
-#pragma unroll 8
-    for (int r = r0; r < r0 + RPW; ++r) cp_async16(dst + 2 * (lane + 32 * r), src + (cs.lane_off ^ tab[r]));
+// Global offset (amplitudes, within the tile) of block b.
+template <int TB, int MAXJ>
+__device__ __forceinline__ uint32_t block_offset(const JobTable<MAXJ>& jt, const BlockSide& cs, int b) {
+    const PassDesc& pd = *jt.job[cs.job].pd;
+    uint32_t o = 0;
+    for (int k = 0; k < TB - cs.cb; ++k)
+        if ((b >> k) & 1) o |= 1u << pd.gbit[cs.cb + k];
+    return o;
 }
 
-// One tile's state image from shared memory (local-index order) to global
-// memory, eight 16-byte chunks in flight per lane.
-template <int RPW>
-__device__ __forceinline__ void producer_store(const float2* src, float2* dst, const ChunkSide& cs,
-                                               const uint32_t* tab, bool whole, int64_t lim_chunks, int r0,
-                                               int lane) {
-    constexpr int K = RPW < 8 ? RPW : 8;  // chunks in flight per lane
-    for (int rb = r0; rb < r0 + RPW; rb += K) {
-        float4 v[K];
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            v[k] = *reinterpret_cast<const float4*>(src + 2 * (lane + 32 * (rb + k)));
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const int c = lane + 32 * (rb + k);
-            if (whole) {
-                if (c < lim_chunks) *reinterpret_cast<float4*>(dst + 2 * c) = v[k];
-            } else {
-                *reinterpret_cast<float4*>(dst + (cs.lane_off ^ tab[rb + k])) = v[k];
-            }
-        }
-    }
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes)
+                 : "memory");
+}
+template <int N>
+__device__ __forceinline__ void producer_sync() {
+    asm volatile("bar.sync 2, %0;" ::"n"(N) : "memory");
+}
+template <int N>
+__device__ __forceinline__ bool producer_sync_and(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{ .reg .pred p, q; setp.ne.u32 p, %1, 0; bar.red.and.pred q, 2, %2, p; selp.u32 %0, 1, 0, q; }"
+        : "=r"(r)
+        : "r"((uint32_t)v), "n"(N)
+        : "memory");
+    return r != 0;
 }
 
-// A producer warp: for the CTA's i-th tile (buffer i % S) it first stores its
-// rows of tile i - S out of that buffer once the compute warps released it
-// (empty barrier), then loads its rows of tile i into it and arrives on the
-// full barrier when the copies land.  Tiles whose pass does not load (|0..0> start, embedding)
-// get a plain arrive: the compute warps still need the buffer.
+// The producer warps: for the CTA's i-th tile (buffer i % S) they first store
+// tile i - S out of that buffer once the compute warps released it (empty
+// barrier) and wait until the bulk copies have read it, then load tile i into
+// it; the full barrier completes when every byte has landed.  Tiles whose
+// pass does not load (|0..0> start, embedding) get plain arrives: the compute
+// warps still need the buffer.
 template <int TB, int MAXJ>
 __device__ __forceinline__ void fwd_producer(const JobTable<MAXJ>& jt, float2* bufs, uint64_t* bar_full,
-                                             uint64_t* bar_empty, uint32_t* tabs, int ptid) {
+                                             uint64_t* bar_empty, uint32_t*, int ptid) {
     constexpr int AMPS = 1 << TB;
     constexpr int S = fwd_stages(TB);
-    constexpr int ROWS = 1 << (TB - 6);
-    constexpr int RPW = ROWS / fwd_producer_warps(TB);  // rows per producer warp
+    constexpr int PT = 32 * fwd_producer_warps(TB);
     const int lane = ptid & 31;
-    const int r0 = (ptid >> 5) * RPW;
     const int64_t total = jt.begin[jt.njobs];
     const int64_t G = gridDim.x;
     const int64_t t0 = blockIdx.x;
     const int64_t mine = (total - t0 + G - 1) / G;  // tiles of this CTA
-    ChunkSide ld, st;
-    uint32_t* tab_ld = tabs;
-    uint32_t* tab_st = tabs + ROWS;
+    BlockSide ld, st;
+    // offsets of this thread's blocks ptid + PT k of each side (tiles of at
+    // most KB PT blocks; more, smaller blocks are located on the fly)
+    constexpr int KB = ((1 << (TB - 6)) + PT - 1) / PT;
+    uint32_t st_off[KB], ld_off[KB];
     int failed_job = -1;
     for (int64_t i = 0; i < mine + S; ++i) {
         const int s = (int)(i % S);
@@ -604,40 +588,76 @@ __device__ __forceinline__ void fwd_producer(const JobTable<MAXJ>& jt, float2* b
         if (i >= S) {
             const int64_t t = t0 + (i - S) * G;
             const int j = find_job(jt, t);
-            if (!mbar_wait(bar_empty + s, (uint32_t)((i / S - 1) & 1))) {
+            const bool released = mbar_wait(bar_empty + s, (uint32_t)((i / S - 1) & 1));
+            if (!producer_sync_and<PT>(released)) {
                 failed_job = j;
                 break;
             }
-            chunk_side<TB>(st, tab_st, jt, j, r0, r0 + RPW, lane);
+            if (st.job != j) {
+                block_side<TB>(st, jt, j);
+#pragma unroll
+                for (int k = 0; k < KB; ++k)
+                    st_off[k] = ptid + PT * k < st.nblk ? block_offset<TB>(jt, st, ptid + PT * k) : 0;
+            }
             if (st.epi & EPI_STORE) {
                 const RunArgs& A = jt.job[j].A;
-                const bool whole = A.n < TB;
                 const TileGeo g = tile_geo_m(TB, st.fixed_mask, t - jt.begin[j], A.n, A.batch);
-                const int64_t lim = ((int64_t)g.nsamples << A.n) >> 1;
-                producer_store<RPW>(buf, A.state + g.base, st, tab_st, whole, lim, r0, lane);
-                if (st.ckpt >= 0)
-                    producer_store<RPW>(buf, A.ckpt + (int64_t)st.ckpt * (A.batch << A.n) + g.base, st, tab_st,
-                                        whole, lim, r0, lane);
+                float2* ck = st.ckpt >= 0 ? A.ckpt + (int64_t)st.ckpt * (A.batch << A.n) : nullptr;
+                if (A.n < TB) {  // whole samples: one contiguous image
+                    if (ptid == 0) {
+                        const uint32_t bytes = (uint32_t)(((int64_t)g.nsamples << A.n) * 8);
+                        bulk_s2g(A.state + g.base, buf, bytes);
+                        if (ck) bulk_s2g(ck + g.base, buf, bytes);
+                    }
+                } else {
+                    const uint32_t bytes = 8u << st.cb;
+                    for (int b = ptid, k = 0; b < st.nblk; b += PT, ++k) {
+                        const uint32_t off = k < KB ? st_off[k < KB ? k : 0] : block_offset<TB>(jt, st, b);
+                        bulk_s2g(A.state + g.base + off, buf + ((int64_t)b << st.cb), bytes);
+                        if (ck) bulk_s2g(ck + g.base + off, buf + ((int64_t)b << st.cb), bytes);
+                    }
+                }
+                bulk_commit();
+                bulk_wait_read0();  // this thread's copies have read the buffer
             }
-            __syncwarp();  // the warp has read its rows out before it refills them
+            producer_sync<PT>();  // every copy out of the buffer has read it
         }
         if (i < mine) {
             const int64_t t = t0 + i * G;
             const int j = find_job(jt, t);
-            chunk_side<TB>(ld, tab_ld, jt, j, r0, r0 + RPW, lane);
+            if (ld.job != j) {
+                block_side<TB>(ld, jt, j);
+#pragma unroll
+                for (int k = 0; k < KB; ++k)
+                    ld_off[k] = ptid + PT * k < ld.nblk ? block_offset<TB>(jt, ld, ptid + PT * k) : 0;
+            }
             if (ld.loads) {
                 const RunArgs& A = jt.job[j].A;
-                const bool whole = A.n < TB;
                 const TileGeo g = tile_geo_m(TB, ld.fixed_mask, t - jt.begin[j], A.n, A.batch);
-                const int64_t lim = ((int64_t)g.nsamples << A.n) >> 1;
-                producer_load<RPW>(buf, A.state + g.base, ld, tab_ld, whole, lim, r0, lane);
-                mbar_arrive_cp_async(bar_full + s);
-            } else {
+                uint32_t mine_bytes = 0;
+                if (A.n < TB) {
+                    if (ptid == 0) mine_bytes = (uint32_t)(((int64_t)g.nsamples << A.n) * 8);
+                } else {
+                    for (int b = ptid; b < ld.nblk; b += PT) mine_bytes += 8u << ld.cb;
+                }
+                const uint32_t warp_bytes = __reduce_add_sync(0xffffffffu, mine_bytes);
+                if (lane == 0) mbar_arrive_expect_tx(bar_full + s, warp_bytes);
+                __syncwarp();
+                if (A.n < TB) {
+                    if (ptid == 0) bulk_g2s(buf, A.state + g.base, mine_bytes, bar_full + s);
+                } else {
+                    const uint32_t bytes = 8u << ld.cb;
+                    for (int b = ptid, k = 0; b < ld.nblk; b += PT, ++k) {
+                        const uint32_t off = k < KB ? ld_off[k < KB ? k : 0] : block_offset<TB>(jt, ld, b);
+                        bulk_g2s(buf + ((int64_t)b << ld.cb), A.state + g.base + off, bytes, bar_full + s);
+                    }
+                }
+            } else if (lane == 0) {
                 mbar_arrive(bar_full + s);
             }
         }
     }
-    cp_async_wait<0>();  // the warp's copies have landed before it leaves
+    bulk_wait_all0();  // this thread's stores have completed before it leaves
     if (failed_job >= 0 && lane == 0) atomicExch(jt.job[failed_job].A.status, kStatusTimeout);
 }
 
@@ -668,7 +688,7 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
     const int tid = threadIdx.x;
     if (tid == 0) {
         for (int s = 0; s < S; ++s) {
-            mbar_init(bar_full + s, 32 * fwd_producer_warps(TB));  // every producer thread
+            mbar_init(bar_full + s, fwd_producer_warps(TB));  // lane 0 of every producer warp
             mbar_init(bar_empty + s, NT / 32);  // lane 0 of every compute warp
         }
     }
@@ -715,7 +735,7 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         const RunArgs& A = sa;
         const int4* ops = jt.job[j].ops;
         const int n = A.n;
-        const bool load_in = jt.job[j].pd->init == INIT_LOAD && !jt.job[j].zero_init;
+        const bool load_in = d.init == INIT_LOAD && !jt.job[j].zero_init;
         const TileGeo g = tile_geo_m(TB, fmask, t - jt.begin[j], n, A.batch);
         float4* const half = reinterpret_cast<float4*>(s_ops) + (iter & 1) * (kSmemOps / 2);
         // per-tile data of Ops (in the op-list area when it is not staged;
@@ -872,6 +892,7 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         if (d.epi & EPI_STORE) {
             cta_sync<NT>();  // all reads of `buf` (exchanges, probabilities) are done
             pstore_nat<RB>(pt, buf, tid, xm);
+            fence_proxy_async();  // the bulk copies that store the buffer see these writes
         }
         // the warp is done with the buffer (and its part of the state image
         // is in it when the pass stores): the producer writes it out and
