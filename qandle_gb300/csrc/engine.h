@@ -40,11 +40,6 @@ __host__ __device__ constexpr int fwd_min_blocks(int tb, int rb) {
     return tb >= 13 ? 1 : tb == 12 ? 2 : 3;
 }
 
-// Producer row-offset tables: a tile's 2^(TB-1) 16-byte chunks are copied as
-// lane + 32 * row, one table of 2^(TB-6) row offsets for the load and one
-// for the store side.
-__host__ __device__ constexpr int fwd_chunk_rows(int tb) { return 1 << (tb - 6); }
-
 // Device op codes (int4 per op: x = opcode, y/z/w operands).
 enum Opcode : int32_t {
     OP_MAP = 1,   // exchange through shared memory to a new register/lane/warp mapping
@@ -132,13 +127,15 @@ struct RunArgs {
 // and of the shared matrix table (longer lists / tables stay in global memory).
 constexpr int kSmemOps = 512;
 constexpr int kSmemMats = 256;
+// Compiled forward passes keep no op list; the op-list area holds the
+// per-sample matrices of the tile in each of the three buffers instead, up to
+// this many 2x2 matrices (32 bytes) per buffer.
+constexpr int kStagedPerSlot = kSmemOps * 16 / 3 / 32;
 
 // Dynamic shared memory of the forward kernel: the tile ring, the op list,
-// the shared matrix table, the full/empty mbarrier of each tile buffer and the
-// producer's row-offset tables.
+// the shared matrix table and the full/empty mbarrier of each tile buffer.
 __host__ __device__ constexpr int fwd_smem_bytes(int tb) {
-    return fwd_stages(tb) * (1 << tb) * 8 + kSmemOps * 16 + kSmemMats * 32 + 2 * fwd_stages(tb) * 8 +
-           2 * fwd_chunk_rows(tb) * 4;
+    return fwd_stages(tb) * (1 << tb) * 8 + kSmemOps * 16 + kSmemMats * 32 + 2 * fwd_stages(tb) * 8;
 }
 
 // Dynamic shared memory of the backward kernel: psi and lambda double

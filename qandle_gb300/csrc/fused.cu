@@ -198,8 +198,8 @@ __device__ __forceinline__ float pgrad_op(const PTile<RB>& ps, const PTile<RB>& 
 // (the prebuilt kernels; the compiled pass kernels of jit.cpp unroll it).
 struct InterpOps {
     static constexpr bool kStageOps = true;
-    template <int TB, int RB>
-    __device__ __forceinline__ static void tile_start(const RunArgs&, const TileGeo&, float4*, int) {}
+    static constexpr uint32_t kStagedBytes = 0;
+    __device__ __forceinline__ static void stage(const RunArgs&, const TileGeo&, float4*, uint64_t*, int) {}
     template <int TB, int RB>
     __device__ __forceinline__ static void apply(PTile<RB>& pt, uint32_t& xm, ThreadMap& tm, const PassDesc& d,
                                                  const RunArgs& A, const int4* ops, const int4* s_ops,

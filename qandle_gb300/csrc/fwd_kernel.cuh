@@ -561,13 +561,14 @@ __device__ __forceinline__ bool producer_sync_and(bool v) {
 
 // The producer warps: for the CTA's i-th tile (buffer i % S) they first store
 // tile i - S out of that buffer once the compute warps released it (empty
-// barrier) and wait until the bulk copies have read it, then load tile i into
-// it; the full barrier completes when every byte has landed.  Tiles whose
-// pass does not load (|0..0> start, embedding) get plain arrives: the compute
-// warps still need the buffer.
-template <int TB, int MAXJ>
+// barrier) and wait until the bulk copies have read it, then publish tile i's
+// geometry, copy its per-sample matrices (Ops::stage) and load it into the
+// buffer; the full barrier completes when every byte has landed.  Tiles whose
+// pass does not load (|0..0> start, embedding) still get their geometry and
+// matrices: the compute warps need them and the buffer.
+template <int TB, int MAXJ, class Ops>
 __device__ __forceinline__ void fwd_producer(const JobTable<MAXJ>& jt, float2* bufs, uint64_t* bar_full,
-                                             uint64_t* bar_empty, uint32_t*, int ptid) {
+                                             uint64_t* bar_empty, TileGeo* s_geo, float4* staged, int ptid) {
     constexpr int AMPS = 1 << TB;
     constexpr int S = fwd_stages(TB);
     constexpr int PT = 32 * fwd_producer_warps(TB);
@@ -631,18 +632,23 @@ __device__ __forceinline__ void fwd_producer(const JobTable<MAXJ>& jt, float2* b
                 for (int k = 0; k < KB; ++k)
                     ld_off[k] = ptid + PT * k < ld.nblk ? block_offset<TB>(jt, ld, ptid + PT * k) : 0;
             }
+            const RunArgs& A = jt.job[j].A;
+            const TileGeo g = tile_geo_m(TB, ld.fixed_mask, t - jt.begin[j], A.n, A.batch);
+            if (ptid == 0) s_geo[s] = g;  // published by this thread's arrive below
+            uint32_t mine_bytes = 0;
             if (ld.loads) {
-                const RunArgs& A = jt.job[j].A;
-                const TileGeo g = tile_geo_m(TB, ld.fixed_mask, t - jt.begin[j], A.n, A.batch);
-                uint32_t mine_bytes = 0;
                 if (A.n < TB) {
                     if (ptid == 0) mine_bytes = (uint32_t)(((int64_t)g.nsamples << A.n) * 8);
                 } else {
                     for (int b = ptid; b < ld.nblk; b += PT) mine_bytes += 8u << ld.cb;
                 }
-                const uint32_t warp_bytes = __reduce_add_sync(0xffffffffu, mine_bytes);
-                if (lane == 0) mbar_arrive_expect_tx(bar_full + s, warp_bytes);
-                __syncwarp();
+            }
+            uint32_t warp_bytes = __reduce_add_sync(0xffffffffu, mine_bytes);
+            if (ptid < 32) warp_bytes += Ops::kStagedBytes;
+            if (lane == 0) mbar_arrive_expect_tx(bar_full + s, warp_bytes);
+            __syncwarp();
+            if (ptid < 32) Ops::stage(A, g, staged + s * (2 * kStagedPerSlot), bar_full + s, lane);
+            if (ld.loads) {
                 if (A.n < TB) {
                     if (ptid == 0) bulk_g2s(buf, A.state + g.base, mine_bytes, bar_full + s);
                 } else {
@@ -652,8 +658,6 @@ __device__ __forceinline__ void fwd_producer(const JobTable<MAXJ>& jt, float2* b
                         bulk_g2s(buf + ((int64_t)b << ld.cb), A.state + g.base + off, bytes, bar_full + s);
                     }
                 }
-            } else if (lane == 0) {
-                mbar_arrive(bar_full + s);
             }
         }
     }
@@ -681,9 +685,9 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
     float4* s_mats = reinterpret_cast<float4*>(s_ops + kSmemOps);   // [kSmemMats][2]
     uint64_t* bar_full = reinterpret_cast<uint64_t*>(s_mats + 2 * kSmemMats);  // [S]
     uint64_t* bar_empty = bar_full + S;                                        // [S]
-    uint32_t* s_tabs = reinterpret_cast<uint32_t*>(bar_empty + S);             // [2][chunk rows]
     __shared__ PassDesc sd;
     __shared__ RunArgs sa;
+    __shared__ TileGeo s_geo[S];  // geometry of the tile in each buffer (written by the producer)
 
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -694,7 +698,8 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
     }
     __syncthreads();  // the only barrier the producer joins
     if (tid >= NT) {
-        fwd_producer<TB, MAXJ>(jt, bufs, bar_full, bar_empty, s_tabs, tid - NT);
+        fwd_producer<TB, MAXJ, Ops>(jt, bufs, bar_full, bar_empty, s_geo, reinterpret_cast<float4*>(s_ops),
+                                    tid - NT);
         return;
     }
 
@@ -704,8 +709,6 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
     const int64_t t0 = blockIdx.x;
     int cur_job = -1;
     int iter = 0;
-    int staged_iter = -1;  // iteration whose per-tile data of Ops is already on its way
-    uint32_t fmask = 0;    // global bits of the qubits outside the tile (current job)
     bool ok = true;
     for (int64_t t = t0; t < total; t += G, ++iter) {
         const int slot = iter % S;
@@ -728,7 +731,6 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
             const float4* gm = reinterpret_cast<const float4*>(jt.job[j].A.mats);
             for (int i = tid; i < 2 * nm; i += NT) s_mats[i] = __ldg(gm + i);
             cta_sync<NT>();
-            fmask = fixed_mask_of(sd);
             cur_job = j;
         }
         const PassDesc& d = sd;
@@ -736,17 +738,15 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         const int4* ops = jt.job[j].ops;
         const int n = A.n;
         const bool load_in = d.init == INIT_LOAD && !jt.job[j].zero_init;
-        const TileGeo g = tile_geo_m(TB, fmask, t - jt.begin[j], n, A.batch);
-        float4* const half = reinterpret_cast<float4*>(s_ops) + (iter & 1) * (kSmemOps / 2);
-        // per-tile data of Ops (in the op-list area when it is not staged;
-        // two halves alternate by tile), usually issued one tile ahead
-        if (staged_iter != iter) Ops::template tile_start<TB, RB>(A, g, half, tid);
+        // the tile's per-sample matrices (compiled passes) in the buffer's
+        // share of the op-list area
+        const float4* const staged = reinterpret_cast<const float4*>(s_ops) + slot * (2 * kStagedPerSlot);
         const bool landed = mbar_wait(bar_full + slot, (uint32_t)((iter / S) & 1));
-        cp_async_wait<0>();  // this thread's copies of the per-tile data
         if (!cta_sync_and<NT>(landed)) {
             ok = false;
             break;
         }
+        const TileGeo g = s_geo[slot];
         PTile<RB> pt;
         uint32_t xm = 0;  // pending thread-controlled X per register bit
         ThreadMap tm;
@@ -796,18 +796,10 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 }
             }
         }
-        // the next tile's per-tile data of Ops, into the other half (its
-        // last reader, tile t - 1, is done: the barrier above)
-        if (t + G < total && find_job(jt, t + G) == j) {
-            const TileGeo gn = tile_geo_m(TB, fmask, t + G - jt.begin[j], n, A.batch);
-            Ops::template tile_start<TB, RB>(A, gn, reinterpret_cast<float4*>(s_ops) + ((iter + 1) & 1) * (kSmemOps / 2),
-                                             tid);
-            staged_iter = iter + 1;
-        }
         // ---- the gate program of this pass ----
-        // (the op list when Ops reads it, else this tile's half of the staged data)
+        // (the op list when Ops reads it, else the tile's staged matrices)
         Ops::template apply<TB, RB>(pt, xm, tm, d, A, ops,
-                                    Ops::kStageOps ? s_ops : reinterpret_cast<const int4*>(half), s_mats,
+                                    Ops::kStageOps ? s_ops : reinterpret_cast<const int4*>(staged), s_mats,
                                     reinterpret_cast<float*>(buf), g.sample, g.fixed_val, tid);
         // ---- epilogue (the planner left the natural mapping) ----
         const int64_t smp0 = g.sample;

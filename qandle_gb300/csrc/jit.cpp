@@ -239,10 +239,10 @@ std::string pass_source(const ProgramRun& R, int p) {
     const int nt = 1 << (tb - rb);
     const int32_t* ops = R.fops + 4 * (size_t)d.op_begin;
     // With n >= TB a tile lies in one sample, so the pass's per-sample
-    // matrices are the same for the whole CTA: async copies put them into
-    // shared memory (the op-list area, unused here; two halves alternate by
-    // tile) while the tile before computes, instead of every thread reading
-    // them from global memory at every op.
+    // matrices are the same for the whole CTA: the producer warps copy them
+    // into shared memory with the tile (the op-list area, unused here, has a
+    // share per tile buffer) instead of every thread reading them from global
+    // memory at every op.
     std::vector<int32_t> staged;  // per-sample slot of each staged matrix
     std::map<int32_t, int> staged_index;
     if (R.n >= tb) {
@@ -253,7 +253,7 @@ std::string pass_source(const ProgramRun& R, int p) {
                 staged.push_back(z);
             }
         }
-        const int cap = std::min(nt / 2, kSmemOps / 2 * 16 / 32);  // one half of the op-list area
+        const int cap = kStagedPerSlot;  // the op-list area's share of one tile buffer
         if ((int)staged.size() > cap) {
             staged.clear();
             staged_index.clear();
@@ -264,16 +264,17 @@ std::string pass_source(const ProgramRun& R, int p) {
          "namespace qg {\n"
          "struct PassOps {\n"
          "  static constexpr bool kStageOps = false;\n"
-         "  template <int TB, int RB>\n"
-         "  __device__ __forceinline__ static void tile_start(const RunArgs& A, const TileGeo& g, float4* sm, "
-         "int tid) {\n";
+      << "  static constexpr uint32_t kStagedBytes = " << 32 * staged.size() << ";\n"
+         "  __device__ __forceinline__ static void stage(const RunArgs& A, const TileGeo& g, float4* sm, "
+         "uint64_t* bar, int lane) {\n";
+    // (called by the 32 lanes of the first producer warp, after its lane 0
+    // added kStagedBytes to the buffer's full barrier)
     if (!staged.empty()) {
-        s << "    if (tid < " << 2 * staged.size() << ") {\n      const int k = tid >> 1;\n      const int slot = ";
+        s << "    for (int k = lane; k < " << staged.size() << "; k += 32) {\n"
+          << "      const int slot = ";
         for (size_t i = 0; i + 1 < staged.size(); ++i) s << "k == " << i << " ? " << staged[i] << " : ";
         s << staged.back() << ";\n"
-          << "      cp_async16(sm + tid, reinterpret_cast<const float4*>(A.mats_ps + (g.sample * A.nslots_ps + slot) * 4)"
-             " + (tid & 1));\n    }\n"
-          << "    cp_async_commit();\n";
+          << "      bulk_g2s(sm + 2 * k, A.mats_ps + (g.sample * A.nslots_ps + slot) * 4, 32u, bar);\n    }\n";
     }
     s << "  }\n"
          "  template <int TB, int RB>\n"
