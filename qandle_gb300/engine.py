@@ -309,6 +309,84 @@ class Program:
         return torch.empty(max(int(nb), 256), dtype=torch.uint8, device=device)
 
 
+def _gather_params(lo: Lowered, device) -> torch.Tensor:
+    """params[i] = param_scale[i] * remapping_i(theta_i) for every unnamed
+    rotation, as one float32 vector on `device`.  The thetas are stacked by
+    one op and each remapping (an elementwise function) runs once on the
+    angles that use it, so a call costs a handful of ops, not a few per gate;
+    gradients reach every theta through the stack."""
+    mods = lo.param_mods
+    thetas = [m.theta for m in mods]
+    if any(t.numel() != 1 for t in thetas):
+        raise ValueError("a rotation angle must hold one value")
+    shape0 = thetas[0].shape
+    if any(t.shape != shape0 for t in thetas):
+        thetas = [t.reshape(()) for t in thetas]
+    vals = torch.stack(thetas).reshape(-1)
+    groups: dict = {}
+    for i, m in enumerate(mods):
+        groups.setdefault(m.remapping, []).append(i)
+    if len(groups) == 1:
+        vals = next(iter(groups))(vals)
+    else:
+        parts = torch.empty_like(vals)
+        for fn, idx in groups.items():
+            ix = torch.tensor(idx, device=vals.device)
+            parts = parts.index_put((ix,), fn(vals[ix]))
+        vals = parts
+    vals = vals.to(device=device, dtype=torch.float32)
+    scales = lo.param_scale if len(lo.param_scale) == len(mods) else None
+    if scales is not None and any(sc != 1.0 for sc in scales):
+        vals = vals * torch.tensor(scales, dtype=torch.float32, device=device)
+    return vals.contiguous()
+
+
+def _named_plan(lo: Lowered):
+    """Named columns grouped by input name, in first-use order: [(name,
+    [j, ...] or None)]; a name used both indexed and whole gets two groups."""
+    plan = getattr(lo, "_named_plan_cache", None)
+    if plan is None:
+        groups: dict = {}
+        for name, j in lo.named_cols:
+            groups.setdefault((name, j is None), []).append(j)
+        plan = [(name, None if whole else js) for (name, whole), js in groups.items()]
+        # a whole (unindexed) input contributes one column per use
+        plan = [(name, js) for name, js in plan for _ in range(len(groups[(name, True)]) if js is None else 1)]
+        lo._named_plan_cache = plan
+    return plan
+
+
+def _named_order(lo: Lowered, device):
+    """Permutation from the grouped column order of _named_plan to the
+    column order of lo.named_cols, and the column scales (None when they are
+    the identity / all one)."""
+    key = ("_named_order_cache", str(device))
+    cache = getattr(lo, "_named_order_cache", None)
+    if cache is not None and cache[0] == key:
+        return cache[1], cache[2]
+    slots: dict = {}
+    pos = 0
+    for name, js in _named_plan(lo):
+        if js is None:
+            slots.setdefault((name, None), []).append(pos)
+            pos += 1
+        else:
+            for j in js:
+                slots.setdefault((name, j), []).append(pos)
+                pos += 1
+    used: dict = {}
+    perm = []
+    for name, j in lo.named_cols:
+        k = used.get((name, j), 0)
+        perm.append(slots[(name, j)][k])
+        used[(name, j)] = k + 1
+    perm_t = None if perm == list(range(len(perm))) else torch.tensor(perm, device=device)
+    sc = list(lo.named_scale) + [1.0] * (len(lo.named_cols) - len(lo.named_scale))
+    scale_t = None if all(x == 1.0 for x in sc) else torch.tensor(sc, dtype=torch.float32, device=device)
+    lo._named_order_cache = (key, perm_t, scale_t)
+    return perm_t, scale_t
+
+
 class _Inputs:
     """Runtime values of one call, gathered on the device."""
 
@@ -316,36 +394,42 @@ class _Inputs:
         sizes = []
         if state is not None and state.dim() == 2:
             sizes.append(state.shape[0])
-        cols = []
-        for name, j in lo.named_cols:
+        # one block per named input: its columns (v[..., j] for an indexed
+        # input, v itself otherwise) gathered by one op
+        blocks = []
+        for name, idx in _named_plan(lo):
             if name not in kwargs:
                 raise KeyError(f"missing named input {name!r}")
-            v = torch.as_tensor(kwargs[name])
-            v = v.to(device=device, dtype=torch.float32)
-            if j is not None:
-                v = v[..., j]
-            c = len(cols)
-            if c < len(lo.named_scale) and lo.named_scale[c] != 1.0:
-                v = v * lo.named_scale[c]
-            if v.dim() > 1:
+            v = torch.as_tensor(kwargs[name]).to(device=device, dtype=torch.float32)
+            if idx is None:
+                blk = v.unsqueeze(-1)
+            else:
+                if v.dim() == 0:
+                    raise ValueError(f"named input {name!r} is indexed per qubit but is a scalar")
+                blk = v.index_select(-1, torch.as_tensor(idx, device=v.device))
+            if blk.dim() > 2:
                 raise ValueError(f"named input {name!r} must be a scalar or [batch] per gate")
-            if v.dim() == 1:
-                sizes.append(v.shape[0])
-            cols.append(v)
+            if blk.dim() == 2:
+                sizes.append(blk.shape[0])
+            blocks.append(blk)
         big = [s for s in sizes if s != 1]
         if big and any(s != big[0] for s in big):
             raise ValueError(f"inconsistent batch sizes {sizes}")
         self.batch = big[0] if big else (1 if not sizes else sizes[0])
         self.unbatched = not sizes
-        if cols:
-            self.named = torch.stack([c.reshape(-1).expand(self.batch) for c in cols], 1).contiguous()
+        if blocks:
+            named = torch.cat([b.expand(self.batch, -1) if b.dim() == 2 else b.unsqueeze(0).expand(self.batch, -1)
+                               for b in blocks], 1)
+            perm, scale = _named_order(lo, device)
+            if perm is not None:
+                named = named.index_select(1, perm)
+            if scale is not None:
+                named = named * scale
+            self.named = named.contiguous()
         else:
             self.named = torch.zeros(1, 1, dtype=torch.float32, device=device)
         if lo.param_mods:
-            scales = lo.param_scale if len(lo.param_scale) == len(lo.param_mods) else [1.0] * len(lo.param_mods)
-            self.params = torch.cat([
-                (m.remapping(m.theta).reshape(-1)[:1] * sc if sc != 1.0 else m.remapping(m.theta).reshape(-1)[:1])
-                .to(device=device, dtype=torch.float32) for m, sc in zip(lo.param_mods, scales)]).contiguous()
+            self.params = _gather_params(lo, device)
         else:
             self.params = torch.zeros(1, dtype=torch.float32, device=device)
         if lo.umats:
