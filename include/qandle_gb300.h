@@ -310,6 +310,18 @@ int qg_program_prepare(const qg_program* prog, const void* dev_table, void* work
 /* One kernel launch running pass jobs[i].pass of every job.  The jobs must be
  * independent (distinct states) and planned with the same tile_bits. */
 int qg_jobs_run_pass(const qg_job* jobs, int njobs, void* stream);
+
+/* Status word of a program workspace after the work queued on `stream`: QG_OK,
+ * or QG_ETIMEOUT when a pass kernel's bounded wait on a producer / compute
+ * hand-off ran out (its results are then invalid).  Synchronises the stream.
+ * (No reference counterpart: the reference runs no asynchronous kernels.) */
+int qg_workspace_status(const void* workspace, void* stream);
+
+/* Self-test of the bounded waits: one CTA waits on an mbarrier that nothing
+ * completes, with a limit of limit_ns (at most 2e9).  Returns QG_ETIMEOUT when
+ * the wait ran out and reported it (the expected outcome); the context stays
+ * usable.  (No reference counterpart.) */
+int qg_selftest_wait_timeout(int64_t limit_ns, void* stream);
 int qg_program_finish(const qg_program* prog, const void* dev_table, void* workspace,
                       int64_t workspace_bytes, int64_t batch, float* out, void* stream);
 

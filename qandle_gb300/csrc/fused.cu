@@ -622,6 +622,16 @@ static int launch_bwd(const PassDesc* dpass, const int4* dops, int p, const RunA
     }
 }
 
+// A wait that runs out on purpose: one CTA waits on an mbarrier nothing
+// arrives on, with a short limit, and reports what the bounded wait saw.
+__global__ void k_selftest_wait(int* status, uint64_t limit_ns) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    const bool done = mbar_wait(&bar, 0, limit_ns);
+    if (threadIdx.x == 0) *status = done ? 0 : kStatusTimeout;
+}
+
 static int64_t num_tiles(int n, int tb, int64_t B) {
     if (n >= tb) return B << (n - tb);
     int64_t spt = int64_t(1) << (tb - n);
@@ -725,6 +735,37 @@ int qg_program_finish(const qg_program* prog, const void* dev_table, void* works
         R.measure == QG_MEASURE_Z);
     QG_LAUNCH_CHECK();
     return QG_OK;
+}
+
+int qg_workspace_status(const void* workspace, void* stream) {
+    QG_CHECK_ARG(workspace, "null pointer");
+    int h = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    QG_CUDA_TRY(cudaMemcpyAsync(&h, workspace, sizeof(int), cudaMemcpyDeviceToHost, st));
+    QG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (h == 0) return QG_OK;
+    qg::set_error(h == QG_ETIMEOUT ? "a kernel wait timed out (a producer / compute hand-off never completed)"
+                                   : "a kernel reported an error status");
+    return h;
+}
+
+int qg_selftest_wait_timeout(int64_t limit_ns, void* stream) {
+    QG_CHECK_ARG(limit_ns > 0 && limit_ns <= 2000000000LL, "limit_ns must be in (0, 2e9]");
+    cudaStream_t st = (cudaStream_t)stream;
+    int* d = nullptr;
+    QG_CUDA_TRY(cudaMalloc(&d, sizeof(int)));
+    int h = -1;
+    cudaError_t e = cudaMemsetAsync(d, 0xff, sizeof(int), st);
+    if (e == cudaSuccess) {
+        qg::k_selftest_wait<<<1, 32, 0, st>>>(d, (uint64_t)limit_ns);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d);
+    if (e != cudaSuccess) return qg::set_error(std::string("selftest: ") + cudaGetErrorString(e)), QG_ECUDA;
+    if (h == QG_ETIMEOUT) return QG_ETIMEOUT;
+    return qg::set_error("selftest: the wait did not report a timeout"), QG_ECUDA;
 }
 
 int qg_jobs_run_pass(const qg_job* jobs, int njobs, void* stream) {

@@ -87,15 +87,16 @@ __device__ __forceinline__ uint64_t global_ns() {
     return t;
 }
 // Bounded wait for the phase of parity `parity` of b.  False when it did not
-// complete within about two seconds (or 2^16 tries): the caller reports
-// kStatusTimeout and winds the CTA down instead of waiting on.
+// complete within limit_ns (about two seconds by default; at most 2^16
+// tries): the caller reports kStatusTimeout and winds the CTA down instead of
+// waiting on.
 constexpr uint64_t kWaitNs = 2000000000ull;
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, uint64_t limit_ns = kWaitNs) {
     if (mbar_try_wait(b, parity)) return true;
     const uint64_t t0 = global_ns();
     for (uint32_t i = 1; i < (1u << 16); ++i) {
         if (mbar_try_wait(b, parity)) return true;
-        if (global_ns() - t0 > kWaitNs) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     }
     return false;
 }

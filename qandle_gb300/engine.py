@@ -309,6 +309,18 @@ class Program:
         return torch.empty(max(int(nb), 256), dtype=torch.uint8, device=device)
 
 
+# QG_CHECK_STATUS=1: read the workspace status word after every fused forward
+# and backward (one stream synchronisation per call) and raise on a timeout.
+_CHECK_STATUS = os.environ.get("QG_CHECK_STATUS", "0") not in ("", "0")
+
+
+def check_status(workspace: torch.Tensor) -> None:
+    """Raise RuntimeError when a pass kernel that used `workspace` reported a
+    timed-out wait (its results are then invalid).  Synchronises the current
+    stream."""
+    _lib.check(_lib.load().qg_workspace_status(workspace.data_ptr(), _lib.stream()))
+
+
 def _gather_params(lo: Lowered, device) -> torch.Tensor:
     """params[i] = param_scale[i] * remapping_i(theta_i) for every unnamed
     rotation, as one float32 vector on `device`.  The thetas are stacked by
@@ -552,6 +564,8 @@ class FusedExecutor:
         _lib.call("qg_program_forward", prog.handle, prog.table(dev).data_ptr(), ws.data_ptr(), ws.numel(),
                   st.data_ptr(), B, zero_init, params.data_ptr(), named.data_ptr(), umats.data_ptr(),
                   _lib.ptr(out), _lib.ptr(ckpt), _lib.stream())
+        if _CHECK_STATUS:
+            check_status(ws)
         ctx.ex = self
         ctx.prog = prog
         ctx.batch = B
@@ -587,6 +601,8 @@ class FusedExecutor:
                   st.data_ptr(), lam.data_ptr(), B, params.data_ptr(), named.data_ptr(), umats.data_ptr(),
                   g.data_ptr(), dparams.data_ptr(), dnamed.data_ptr(), _lib.ptr(dstate),
                   _lib.ptr(ctx.ckpt), _lib.stream())
+        if _CHECK_STATUS:
+            check_status(ws)
         gstate = None
         if need_state:
             shp = ctx.state_shape
