@@ -75,7 +75,8 @@ struct PassDesc {
     int32_t grad_base;        // backward: first grad slot of this pass
     int32_t ngrad;            // backward: grad slots in this pass
     int32_t psi_from_ckpt;    // backward: read psi from checkpoint (>= 0) instead of the state
-    int32_t pad[3];
+    int32_t end_map[3];       // mapping the gate program ends in (OP_MAP encoding); its lanes
+                              // are local bits 0..4, so the tile is written back from it
 };
 
 struct SlotDesc {

@@ -375,6 +375,32 @@ __device__ __forceinline__ void pstore_nat(const PTile<RB>& t, float2* buf, int 
     for (int r = 0; r < (1 << RB); ++r) buf[nat_index<RB>(r, tid) ^ x] = get_amp<RB>(t, r);
 }
 
+// The tile in natural order into shared memory from a mapping `em` (OP_MAP
+// encoding) whose lanes are local bits 0..4; physical register r holds
+// logical amplitude r ^ xm.  Register and warp bits are distinct local bits,
+// so a register index's offset is the XOR of its bits' offsets.
+template <int RB>
+__device__ __forceinline__ void pstore_map(const PTile<RB>& t, float2* buf, const int32_t em[3], int tid,
+                                           uint32_t xm) {
+    int thr = tid & 31;
+    const int nw = (em[2] >> 16) & 7;
+    for (int k = 0; k < nw; ++k) thr |= ((tid >> (5 + k)) & 1) << ((em[2] >> (4 * k)) & 15);
+    int ro[1 << RB];
+    ro[0] = 0;
+#pragma unroll
+    for (int k = 0; k < RB; ++k) {
+        const int bit = 1 << ((em[0] >> (4 * k)) & 15);
+#pragma unroll
+        for (int r = 0; r < (1 << k); ++r) ro[r + (1 << k)] = ro[r] | bit;
+    }
+    int xoff = 0;
+#pragma unroll
+    for (int k = 0; k < RB; ++k)
+        if ((xm >> k) & 1) xoff ^= ro[1 << k];
+#pragma unroll
+    for (int r = 0; r < (1 << RB); ++r) buf[thr | (ro[r] ^ xoff)] = get_amp<RB>(t, r);
+}
+
 // Probabilities of the tile in natural order into shared memory; physical
 // register r holds logical amplitude r ^ xm.
 template <int RB>
@@ -802,7 +828,8 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         Ops::template apply<TB, RB>(pt, xm, tm, d, A, ops,
                                     Ops::kStageOps ? s_ops : reinterpret_cast<const int4*>(staged), s_mats,
                                     reinterpret_cast<float*>(buf), g.sample, g.fixed_val, tid);
-        // ---- epilogue (the planner left the natural mapping) ----
+        // ---- epilogue (the planner left the natural mapping, or for a pass
+        // that only stores, a mapping with natural lanes: d.end_map) ----
         const int64_t smp0 = g.sample;
         if (d.epi & (EPI_PROBS | EPI_P0)) {
             cta_sync<NT>();  // all exchange reads of `buf` are done
@@ -884,7 +911,10 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         }
         if (d.epi & EPI_STORE) {
             cta_sync<NT>();  // all reads of `buf` (exchanges, probabilities) are done
-            pstore_nat<RB>(pt, buf, tid, xm);
+            if (d.end_map[0] == NatMap<TB, RB>::y && d.end_map[2] == NatMap<TB, RB>::w)
+                pstore_nat<RB>(pt, buf, tid, xm);
+            else
+                pstore_map<RB>(pt, buf, d.end_map, tid, xm);
             fence_proxy_async();  // the bulk copies that store the buffer see these writes
         }
         // the warp is done with the buffer (and its part of the state image

@@ -486,13 +486,24 @@ void emit_pass(Program& P, PassPlan& pp, const std::vector<LGate>& G, bool backw
         have_map = true;
         cur = nat;
     }
-    // the epilogue moves the tile through shared memory in natural order
+    // The epilogue moves the tile through shared memory in natural order.  A
+    // forward pass that only stores writes it back from any mapping whose
+    // lanes are local bits 0..4 (each warp access still covers consecutive
+    // amplitudes), which saves the exchange back to the natural mapping.
     bool need_nat = backward || (d.epi & (EPI_STORE | EPI_PROBS | EPI_P0)) != 0;
-    if (need_nat && !(cur == nat)) {
-        int32_t e[3];
-        nat.encode(e);
-        ops.insert(ops.end(), {OP_MAP, e[0], e[1], e[2]});
-        ++nexchanges;
+    bool lanes_nat = true;
+    for (int k = 0; k < 5; ++k) lanes_nat = lanes_nat && cur.lane[k] == k;
+    const bool store_only = !backward && (d.epi & (EPI_PROBS | EPI_P0)) == 0;
+    if (store_only && lanes_nat) {
+        cur.encode(d.end_map);
+    } else {
+        if (need_nat && !(cur == nat)) {
+            int32_t e[3];
+            nat.encode(e);
+            ops.insert(ops.end(), {OP_MAP, e[0], e[1], e[2]});
+            ++nexchanges;
+        }
+        nat.encode(d.end_map);
     }
     d.op_count = (int)ops.size() / 4 - d.op_begin;
     (void)nshared;
