@@ -139,11 +139,17 @@ __host__ __device__ constexpr int fwd_smem_bytes(int tb) {
     return fwd_stages(tb) * (1 << tb) * 8 + kSmemOps * 16 + kSmemMats * 32 + 2 * fwd_stages(tb) * 8;
 }
 
-// Dynamic shared memory of the backward kernel: psi and lambda double
-// buffers, the op list, the shared matrix table, the gradient partials and
-// their sample tags.
+// Threads of a backward CTA: 2^(TB-RB) compute threads and one producer warp
+// (the backward's compute threads need up to ~224 registers, so there is no
+// room for more producer warps).
+__host__ __device__ constexpr int bwd_threads(int tb, int rb) { return (1 << (tb - rb)) + 32; }
+
+// Dynamic shared memory of the backward kernel: psi and lambda in two tile
+// slots, the op list, the shared matrix table, the gradient partials and
+// their sample tags, and the full/empty mbarrier of each slot.
 __host__ __device__ constexpr int bwd_smem_bytes(int tb, int rb) {
-    return 4 * (1 << tb) * 8 + kSmemOps * 16 + kSmemMats * 32 + max_grad_per_pass(rb) * (1 << (tb - rb)) * 5;
+    return 4 * (1 << tb) * 8 + kSmemOps * 16 + kSmemMats * 32 + max_grad_per_pass(rb) * (1 << (tb - rb)) * 5 +
+           4 * 8;
 }
 
 #ifndef __CUDACC_RTC__

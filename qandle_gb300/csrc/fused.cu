@@ -256,7 +256,7 @@ struct BwdInterpOps {
 };
 
 template <int TB, int RB>
-__global__ void __launch_bounds__(1 << (TB - RB), 1)
+__global__ void __launch_bounds__(bwd_threads(TB, RB), 1)
     k_bwd_pass(const PassDesc* __restrict__ passes, const int4* __restrict__ ops_all, int pass_index, RunArgs A,
                int store_lam_last, int64_t num_tiles) {
     bwd_pass_body<TB, RB, BwdInterpOps>(passes, ops_all, pass_index, A, store_lam_last, num_tiles);
@@ -578,7 +578,7 @@ static int launch_fwd_compiled(const JitKernel& k, const PassDesc* dpass, const 
 template <int TB, int RB>
 static int launch_bwd_pass(const PassDesc* dpass, const int4* dops, int p, const RunArgs& A, int store_lam,
                            int64_t tiles, cudaStream_t st) {
-    constexpr int NT = 1 << (TB - RB);
+    constexpr int NT = bwd_threads(TB, RB);
     size_t smem = bwd_smem_bytes(TB, RB);
     static bool attr_set = false;
     if (!attr_set) {
@@ -608,7 +608,7 @@ static int launch_bwd_compiled(const JitKernel& k, const PassDesc* dpass, const 
     int pass = p, sl = store_lam;
     int64_t nt = tiles;
     void* params[] = {(void*)&dpass, (void*)&dops, &pass, &a, &sl, &nt};
-    return jit_launch(k, (unsigned)grid, 1u << (tb - rb), (size_t)bwd_smem_bytes(tb, rb), st, params);
+    return jit_launch(k, (unsigned)grid, (unsigned)bwd_threads(tb, rb), (size_t)bwd_smem_bytes(tb, rb), st, params);
 }
 
 static int launch_bwd(const PassDesc* dpass, const int4* dops, int p, const RunArgs& A, int store_lam,

@@ -449,7 +449,7 @@ std::string bwd_pass_source(const ProgramRun& R, int p) {
         }
     }
     s << "  }\n};\n}  // namespace qg\n"
-      << "extern \"C\" __global__ void __launch_bounds__(" << nt << ", 1)\n"
+      << "extern \"C\" __global__ void __launch_bounds__(" << bwd_threads(tb, rb) << ", 1)\n"
       << "qg_bwd_pass(const qg::PassDesc* __restrict__ passes, const int4* __restrict__ ops_all, int pass_index, "
          "qg::RunArgs A, int store_lam_last, int64_t num_tiles) {\n"
       << "  qg::bwd_pass_body<" << tb << ", " << rb << ", qg::BwdPassOps>(passes, ops_all, pass_index, A, "
@@ -706,7 +706,7 @@ int qg_program_compile(qg_program* prog, int flags) {
                 const int tb = t.bwd ? R.bpass[t.pass].tile_bits : R.fpass[t.pass].tile_bits;
                 const int rb = t.bwd ? kBwdRegBits : R.reg_bits;
                 const int smem = t.bwd ? bwd_smem_bytes(tb, rb) : fwd_smem_bytes(tb);
-                const int threads = t.bwd ? 1 << (tb - rb) : fwd_threads(tb, rb);
+                const int threads = t.bwd ? bwd_threads(tb, rb) : fwd_threads(tb, rb);
                 int rc = load_cubin(cubins[i], t.bwd ? "qg_bwd_pass" : "qg_fwd_pass", smem, threads, L, err);
                 if (rc) return set_error("qg_program_compile: " + name(t) + ": " + err), rc;
                 it = g_cache.emplace(std::make_pair(dev, t.src), L).first;
