@@ -66,10 +66,6 @@ __device__ __forceinline__ void mbar_init(uint64_t* b, int count) {
 __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
     asm volatile("{ .reg .b64 st; mbarrier.arrive.shared::cta.b64 st, [%0]; }" ::"r"(smem_u32(b)) : "memory");
 }
-// Arrive on b once every earlier cp.async of this thread has landed.
-__device__ __forceinline__ void mbar_arrive_cp_async(uint64_t* b) {
-    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(b)) : "memory");
-}
 // Test for the completion of the phase of parity `parity`; a waiting thread
 // is suspended (up to about a millisecond) instead of polling shared memory.
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
@@ -160,30 +156,6 @@ __device__ __forceinline__ TileGeo tile_geo_m(int tile_bits, uint32_t fixed_mask
     return g;
 }
 
-__device__ __forceinline__ TileGeo tile_geo(const PassDesc& d, int64_t t, int n, int64_t batch) {
-    TileGeo g;
-    if (n >= d.tile_bits) {
-        const int sh = n - d.tile_bits;  // tiles per sample = 2^sh
-        g.sample = t >> sh;
-        const uint32_t ti = (uint32_t)(t & ((int64_t(1) << sh) - 1));
-        g.tile_in_sample = (int)ti;
-        uint32_t fv = 0;
-        for (int k = 0; k < d.nfixed; ++k) fv |= ((ti >> k) & 1u) << d.fixed_gbit[k];
-        g.fixed_val = fv;
-        g.base = (g.sample << n) + fv;
-        g.nsamples = 1;
-    } else {
-        int spt = 1 << (d.tile_bits - n);
-        g.sample = t * spt;
-        int64_t rem = batch - g.sample;
-        g.nsamples = rem < spt ? (int)rem : spt;
-        g.fixed_val = 0;
-        g.base = g.sample << n;
-        g.tile_in_sample = 0;
-    }
-    return g;
-}
-
 // global amplitude offset of the first element of run r
 __device__ __forceinline__ int64_t run_offset(const PassDesc& d, int r) {
     int64_t off = 0;
@@ -194,55 +166,6 @@ __device__ __forceinline__ int64_t run_offset(const PassDesc& d, int r) {
             off += (lb < d.nq_tile) ? (int64_t(1) << d.gbit[lb]) : 0;
         }
     return off;
-}
-
-// Per-thread async copies (cp.async, 16 bytes = 2 amplitudes each) of one
-// tile's state image into dst in local-index order.  Every thread of the CTA
-// issues 2^(RB-1) copies; thread tid copies chunks tid, tid + NT, ..., so a
-// warp covers 512 contiguous bytes of a run.  Unlike one engine working
-// through a tile's runs (bulk copies), the load/store units of all warps keep
-// many small copies in flight, which scattered 512-byte runs need.  Local
-// bit 0 is global bit 0 (runs are at least 2 amplitudes), so a chunk is
-// contiguous; higher local bits add their global strides.  The caller
-// commits the copies as one group.
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
-template <int TB, int RB>
-__device__ __forceinline__ void thread_tile_load(const PassDesc& d, const TileGeo& g, const float2* src,
-                                                 float2* dst, int n, int tid) {
-    constexpr int NT = 1 << (TB - RB);
-    constexpr int PER = 1 << (RB - 1);  // chunks per thread
-    const float2* base = src + g.base;
-    if (n < TB) {  // whole samples: the tile image is contiguous
-        const int lim = (int)(((int64_t)g.nsamples << n) >> 1);
-#pragma unroll
-        for (int i = 0; i < PER; ++i) {
-            const int c = tid + i * NT;
-            if (c < lim) cp_async16(dst + 2 * c, base + 2 * c);
-        }
-        return;
-    }
-    uint32_t thr = 0;
-#pragma unroll
-    for (int k = 0; k < TB - RB; ++k) thr |= (uint32_t)((tid >> k) & 1) << d.gbit[1 + k];
-    uint32_t st[RB - 1];
-#pragma unroll
-    for (int k = 0; k < RB - 1; ++k) st[k] = 1u << d.gbit[TB - RB + 1 + k];
-#pragma unroll
-    for (int i = 0; i < PER; ++i) {
-        uint32_t off = thr;
-#pragma unroll
-        for (int k = 0; k < RB - 1; ++k)
-            if ((i >> k) & 1) off ^= st[k];
-        cp_async16(dst + 2 * (tid + i * NT), base + off);
-    }
 }
 
 // float (probability) image of a tile: half the bytes of the state image
@@ -412,44 +335,6 @@ __device__ __forceinline__ void pstore_probs(const PTile<RB>& t, float* pb, int 
         pb[nat_index<RB>(2 * k, tid) ^ x] = p.x;
         pb[nat_index<RB>(2 * k + 1, tid) ^ x] = p.y;
     }
-}
-
-// Store a tile in the natural mapping straight from registers to global
-// memory.  The lanes hold 32 consecutive amplitudes of a run, so a warp
-// store covers 256 contiguous bytes whenever the lanes share their pending
-// X; no shared-memory staging, so the tile's buffer is free at once.
-// Physical register r holds logical amplitude r ^ xm.  Local bits map to
-// distinct global bits, so offsets of the register part combine by XOR.
-template <int RB>
-__device__ __forceinline__ void pstore_global(const PTile<RB>& t, uint32_t xm, const PassDesc& d,
-                                              const TileGeo& g, float2* dst, int n, int tid) {
-    float2* base = dst + g.base;
-    if (n < d.tile_bits) {  // whole samples: the tile image is contiguous
-        const int64_t lim = (int64_t)g.nsamples << n;
-#pragma unroll
-        for (int r = 0; r < (1 << RB); ++r) {
-            const int j = nat_index<RB>(r ^ (int)xm, tid);
-            if (j < lim) base[j] = get_amp<RB>(t, r);
-        }
-        return;
-    }
-    uint32_t rs[RB];
-#pragma unroll
-    for (int k = 0; k < RB; ++k) rs[k] = 1u << d.gbit[5 + k];
-    uint32_t c = 0;
-#pragma unroll
-    for (int k = 0; k < 5; ++k) c |= (uint32_t)((tid >> k) & 1) << d.gbit[k];
-    for (int k = 0; k < d.tile_bits - 5 - RB; ++k) c |= (uint32_t)((tid >> (5 + k)) & 1) << d.gbit[5 + RB + k];
-#pragma unroll
-    for (int k = 0; k < RB; ++k) c ^= ((xm >> k) & 1u) ? rs[k] : 0u;
-    uint32_t off[1 << RB];
-    off[0] = c;
-#pragma unroll
-    for (int k = 0; k < RB; ++k)
-#pragma unroll
-        for (int r = 0; r < (1 << k); ++r) off[r + (1 << k)] = off[r] ^ rs[k];
-#pragma unroll
-    for (int r = 0; r < (1 << RB); ++r) base[off[r]] = get_amp<RB>(t, r);
 }
 
 // Exchange through planar shared memory (re plane, im plane), folding the
