@@ -133,13 +133,40 @@ struct Selector {
 
     int m(int b) const { return remap ? remap[b] : b; }
 
+    // Forward: a Z-diagonal single-qubit gate (RZ, diagonal U) whose next
+    // non-commuting gate on its qubit is a single-qubit gate is held back and
+    // placed together with that gate (right before it), so the two share one
+    // 2x2 slot instead of a diagonal and a 2x2 -- also across passes: if that
+    // gate cannot be placed now, the diagonal waits with it.  Holding is
+    // exact: the diagonal commutes with everything between the two.
+    static bool z_diag_1q(const LGate& g) {
+        return (g.kind == K_ROT && g.axis == 2) || (g.kind == K_U && g.diag);
+    }
+    static bool nondiag_1q(const LGate& g) {
+        return (g.kind == K_ROT && g.axis != 2) || (g.kind == K_U && !g.diag);
+    }
+
     std::vector<int> run(const std::vector<int>& pending, const std::vector<LGate>& G) {
         std::vector<int> placed;
         uint32_t sZ = 0, sX = 0, sG = 0;
+        std::vector<std::vector<int>> held(32);  // held diagonals per qubit (pending positions)
         for (int pi = 0; pi < (int)pending.size(); ++pi) {
             const LGate& g = G[pending[pi]];
             Touch t = touches(g);
             bool ok = true;
+            if (!backward && z_diag_1q(g) && !((sX | sG) & (1u << m(g.b0)))) {
+                // the next gate on the qubit that does not commute with a Z diagonal
+                int next = -1;
+                for (int pj = pi + 1; pj < (int)pending.size() && next < 0; ++pj) {
+                    const Touch tj = touches(G[pending[pj]]);
+                    for (int k = 0; k < tj.count; ++k)
+                        if (tj.bit[k] == g.b0 && tj.type[k] != T_Z) next = pj;
+                }
+                if (next >= 0 && nondiag_1q(G[pending[next]])) {
+                    held[g.b0].push_back(pi);
+                    continue;
+                }
+            }
             for (int k = 0; k < t.count && ok; ++k) {
                 uint32_t bm = 1u << m(t.bit[k]);
                 if (t.type[k] == T_Z)
@@ -157,13 +184,20 @@ struct Selector {
                     if (r & (1u << b)) req |= 1u << m(b);
                 uint32_t nb = req & ~S;
                 if (nb == 0) {
-                    placed.push_back(pi);
                 } else if ((nb & ~addable) == 0 && popc(nb) <= max_add) {
                     S |= nb;
                     max_add -= popc(nb);
-                    placed.push_back(pi);
                 } else {
                     ok = false;
+                }
+                if (ok) {
+                    // diagonals held for this gate go right before it
+                    for (int k = 0; k < t.count; ++k)
+                        if (t.type[k] != T_Z && t.bit[k] >= 0) {
+                            placed.insert(placed.end(), held[t.bit[k]].begin(), held[t.bit[k]].end());
+                            held[t.bit[k]].clear();
+                        }
+                    placed.push_back(pi);
                 }
                 if (ok && backward && g.grad) --max_grad;
             }
@@ -173,9 +207,15 @@ struct Selector {
                     if (t.type[k] == T_Z) sZ |= bm;
                     else if (t.type[k] == T_X) sX |= bm;
                     else sG |= bm;
+                    // diagonals held for this gate stay pending with it
+                    if (t.type[k] != T_Z && t.bit[k] >= 0 && !held[t.bit[k]].empty()) {
+                        sZ |= bm;
+                        held[t.bit[k]].clear();
+                    }
                 }
             }
         }
+        // (every held diagonal's partner comes later in `pending`, so none is left held)
         return placed;
     }
 };
