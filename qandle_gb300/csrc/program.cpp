@@ -133,36 +133,43 @@ struct Selector {
 
     int m(int b) const { return remap ? remap[b] : b; }
 
-    // Forward: a Z-diagonal single-qubit gate (RZ, diagonal U) whose next
-    // non-commuting gate on its qubit is a single-qubit gate is held back and
-    // placed together with that gate (right before it), so the two share one
-    // 2x2 slot instead of a diagonal and a 2x2 -- also across passes: if that
-    // gate cannot be placed now, the diagonal waits with it.  Holding is
-    // exact: the diagonal commutes with everything between the two.
-    static bool z_diag_1q(const LGate& g) {
-        return (g.kind == K_ROT && g.axis == 2) || (g.kind == K_U && g.diag);
+    // Forward: a single-qubit gate that is diagonal in Z (RZ, diagonal U) or
+    // in X (RX) and whose next gate on its qubit of another kind (a touch that
+    // does not commute with it) is a single-qubit gate is held back and placed
+    // together with that gate (right before it), so the two share one 2x2
+    // slot -- also across passes: if that gate cannot be placed now, the held
+    // one waits with it.  Holding is exact: the held gate commutes with
+    // everything between the two (CNOT controls / CZs for Z, CNOT targets for X).
+    static int diag_touch_1q(const LGate& g) {
+        if ((g.kind == K_ROT && g.axis == 2) || (g.kind == K_U && g.diag)) return T_Z;
+        if (g.kind == K_ROT && g.axis == 0) return T_X;
+        return -1;
     }
-    static bool nondiag_1q(const LGate& g) {
-        return (g.kind == K_ROT && g.axis != 2) || (g.kind == K_U && !g.diag);
-    }
+    static bool is_1q(const LGate& g) { return g.kind == K_ROT || g.kind == K_U; }
 
     std::vector<int> run(const std::vector<int>& pending, const std::vector<LGate>& G) {
         std::vector<int> placed;
         uint32_t sZ = 0, sX = 0, sG = 0;
-        std::vector<std::vector<int>> held(32);  // held diagonals per qubit (pending positions)
+        std::vector<std::vector<int>> held(32);  // held gates per qubit (pending positions)
+        int held_type[32];                        // their touch type (T_Z, T_X or kMixed)
+        constexpr int kMixed = -2;
         for (int pi = 0; pi < (int)pending.size(); ++pi) {
             const LGate& g = G[pending[pi]];
             Touch t = touches(g);
             bool ok = true;
-            if (!backward && z_diag_1q(g) && !((sX | sG) & (1u << m(g.b0)))) {
-                // the next gate on the qubit that does not commute with a Z diagonal
+            const int dt = backward ? -1 : diag_touch_1q(g);
+            const uint32_t blockers = dt == T_Z ? (sX | sG) : (sZ | sG);
+            if (dt >= 0 && !(blockers & (1u << m(g.b0)))) {
+                // the next gate on the qubit that does not commute with this one
                 int next = -1;
                 for (int pj = pi + 1; pj < (int)pending.size() && next < 0; ++pj) {
                     const Touch tj = touches(G[pending[pj]]);
                     for (int k = 0; k < tj.count; ++k)
-                        if (tj.bit[k] == g.b0 && tj.type[k] != T_Z) next = pj;
+                        if (tj.bit[k] == g.b0 && tj.type[k] != dt) next = pj;
                 }
-                if (next >= 0 && nondiag_1q(G[pending[next]])) {
+                if (next >= 0 && is_1q(G[pending[next]])) {
+                    // a chain of Z- and X-diagonals commutes with no touch of its qubit
+                    held_type[g.b0] = held[g.b0].empty() || held_type[g.b0] == dt ? dt : kMixed;
                     held[g.b0].push_back(pi);
                     continue;
                 }
@@ -180,6 +187,11 @@ struct Selector {
             if (ok) {
                 uint32_t req = 0;
                 uint32_t r = requirement(g, backward);
+                // gates released before this one bring their requirements (a held
+                // RX needs its qubit in the registers, its partner RZ does not)
+                for (int k = 0; k < t.count; ++k)
+                    if (t.bit[k] >= 0 && !held[t.bit[k]].empty() && t.type[k] != held_type[t.bit[k]])
+                        for (int h : held[t.bit[k]]) r |= requirement(G[pending[h]], backward);
                 for (int b = 0; b < 32; ++b)
                     if (r & (1u << b)) req |= 1u << m(b);
                 uint32_t nb = req & ~S;
@@ -191,9 +203,9 @@ struct Selector {
                     ok = false;
                 }
                 if (ok) {
-                    // diagonals held for this gate go right before it
+                    // gates held for this gate go right before it
                     for (int k = 0; k < t.count; ++k)
-                        if (t.type[k] != T_Z && t.bit[k] >= 0) {
+                        if (t.bit[k] >= 0 && !held[t.bit[k]].empty() && t.type[k] != held_type[t.bit[k]]) {
                             placed.insert(placed.end(), held[t.bit[k]].begin(), held[t.bit[k]].end());
                             held[t.bit[k]].clear();
                         }
@@ -207,9 +219,12 @@ struct Selector {
                     if (t.type[k] == T_Z) sZ |= bm;
                     else if (t.type[k] == T_X) sX |= bm;
                     else sG |= bm;
-                    // diagonals held for this gate stay pending with it
-                    if (t.type[k] != T_Z && t.bit[k] >= 0 && !held[t.bit[k]].empty()) {
-                        sZ |= bm;
+                    // gates held for this gate stay pending with it
+                    if (t.bit[k] >= 0 && !held[t.bit[k]].empty() && t.type[k] != held_type[t.bit[k]]) {
+                        const int ht = held_type[t.bit[k]];
+                        if (ht == T_Z) sZ |= bm;
+                        else if (ht == T_X) sX |= bm;
+                        else sG |= bm;
                         held[t.bit[k]].clear();
                     }
                 }

@@ -180,3 +180,33 @@ def test_controlled_and_inverted_gates_plan_matches_oracle():
     # controlled RX goes through H on the target, a complex64 matrix
     # (1/sqrt(2) to float precision): agreement is at 1e-8, not 1e-10
     assert np.abs(st - ref).max() < 1e-6
+
+
+def _random_mix(seed: int, n: int = 14, ngates: int = 160) -> dict:
+    """Random circuit dense in RX / RZ / RY and CNOT / CZ on few qubits, so
+    that diagonal gates are held across CNOT controls and targets, across
+    phases and across passes."""
+    rng = np.random.default_rng(seed)
+    gates = []
+    for _ in range(ngates):
+        r = rng.random()
+        if r < 0.55:
+            axis = ("rx", "ry", "rz")[rng.integers(3)]
+            gates.append((axis, int(rng.integers(n)), float(rng.uniform(-3, 3)), None))
+        else:
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            gates.append(("cnot", a, b) if r < 0.85 else ("cz", a, b))
+    return {"name": "mix", "n": n, "batch": 2, "gates": gates, "inputs": {}, "measure": "state",
+            "targets": None}
+
+
+@pytest.mark.parametrize("seed", range(12))
+@pytest.mark.parametrize("oi", [0, 1, 2, 4])
+def test_held_diagonals_random_circuits_match_oracle(seed, oi):
+    desc = _random_mix(seed)
+    circ = workloads.build_circuit(desc, engine="fused")
+    lo = engine.lower(circ.circuit)
+    prog = engine.Program(lo, "state", keep_state=False, **OPTS[oi])
+    params, named, umats, embed = _runtime(lo, desc, 2)
+    st, _ = emu.run_forward(prog, desc["n"], 2, params, named, umats, embed=embed)
+    assert np.abs(st - oracle.run(desc)).max() < 1e-10
