@@ -433,6 +433,36 @@ void emit_pass(Program& P, PassPlan& pp, const std::vector<LGate>& G, bool backw
                 if (nat_ok && !(R & (1u << nat.reg[k]))) R |= 1u << nat.reg[k];
             for (int b = 0; b < tb && popc(R) < rb; ++b)
                 if ((qubit_local & (1u << b)) && !(R & (1u << b))) R |= 1u << b;
+            // Every register set of rb tile qubits (at most C(13, 5) = 1287) is
+            // tried; the one under which the most gates can be placed wins (the
+            // greedy set above on ties), so each exchange buys as much work as
+            // it can.
+            if (popc(qubit_local) > rb) {
+                std::vector<int> qb;
+                for (int b = 0; b < tb; ++b)
+                    if (qubit_local & (1u << b)) qb.push_back(b);
+                const int nq = (int)qb.size();
+                size_t best = placed.size();
+                for (uint32_t c = (1u << rb) - 1; c < (1u << nq);) {
+                    uint32_t C = 0;
+                    for (int k = 0; k < nq; ++k)
+                        if (c & (1u << k)) C |= 1u << qb[k];
+                    Selector t;
+                    t.S = C;
+                    t.addable = 0;
+                    t.max_add = 0;
+                    t.backward = backward;
+                    t.remap = local_remap;
+                    std::vector<int> pl = t.run(pending, G);
+                    if (pl.size() > best) {
+                        best = pl.size();
+                        placed = pl;
+                        R = C;
+                    }
+                    const uint32_t lo = c & (0u - c), hi = c + lo;  // next subset of the same size
+                    c = (((hi ^ c) >> 2) / lo) | hi;
+                }
+            }
             Mapping nm = (R == natR) ? nat : mapping_for(R, tb, rb);
             if (!have_map) {
                 // zero / embedding init: produce this mapping directly
