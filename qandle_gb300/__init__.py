@@ -8,7 +8,7 @@ on hand-written CUDA kernels through the C ABI of libqandle_gb300.so.
 There is no CPU execution path: tensors must live on a CUDA device.
 """
 # ruff: noqa: F401 F403
-from . import config, errors, qasm, remap
+from . import config, errors, qasm, remap, splitter
 from .tune import autotune
 from .operators import *
 from .embeddings import *

@@ -23,7 +23,7 @@ import torch
 from . import operators
 from . import measurements
 
-__all__ = ["Circuit", "UnsplittedCircuit"]
+__all__ = ["Circuit", "UnsplittedCircuit", "SplittedCircuit", "Subcircuit"]
 
 
 class Circuit(torch.nn.Module):
@@ -38,15 +38,16 @@ class Circuit(torch.nn.Module):
             self.num_qubits = num_qubits
         else:
             self.num_qubits = len(self._used_qubits(layers))
-        if split_max_qubits:
-            # the fused engine's planner already stages at most a tile of
-            # qubits per pass; circuit cutting is not needed to bound memory
-            warnings.warn("split_max_qubits is handled by the fused planner; running unsplit")
         if engine not in ("fused", "plain"):
             raise ValueError(f"engine must be 'fused' or 'plain', got {engine!r}")
         self.engine = engine
         if circuit is not None:
             self.circuit = circuit
+        elif split_max_qubits > 0 and self.num_qubits > split_max_qubits:
+            from . import splitter
+
+            self.circuit = SplittedCircuit(
+                self.num_qubits, splitter.split(_UnbuiltLayers(self.num_qubits, layers), max_qubits=split_max_qubits))
         else:
             self.circuit = UnsplittedCircuit(self.num_qubits, layers)
         self._executor = None
@@ -136,6 +137,18 @@ class Circuit(torch.nn.Module):
         return Circuit(layers=[], num_qubits=self.num_qubits, circuit=self.circuit.decompose(),
                        engine=self.engine)
 
+    def split(self, max_qubits):
+        """The circuit cut into subcircuits of at most `max_qubits` qubits
+        (qcircuit.py:112-122, qandle_gb300.splitter)."""
+        if isinstance(self.circuit, SplittedCircuit):
+            warnings.warn("Circuit already split, returning original circuit.")
+            return self
+        from . import splitter
+
+        splitdict = splitter.split(self.circuit.decompose(), max_qubits=max_qubits)
+        return Circuit(layers=[], num_qubits=self.num_qubits, circuit=SplittedCircuit(self.num_qubits, splitdict),
+                       engine=self.engine, **self._engine_options)
+
 
 class UnsplittedCircuit(torch.nn.Module):
     """Sequential executor (qcircuit.py:137-212); the plain engine's loop."""
@@ -187,6 +200,15 @@ class UnsplittedCircuit(torch.nn.Module):
                 new_layers.append(layer)
         return UnsplittedCircuit(self.num_qubits, new_layers)
 
+    def split(self, **kwargs):
+        """Subcircuits of this circuit (qcircuit.py:198-206, qandle_gb300.splitter)."""
+        if self.num_qubits == 1:
+            warnings.warn("Can't split circuit with only 1 qubit")
+            return self
+        from . import splitter
+
+        return SplittedCircuit(self.num_qubits, splitter.split(self, **kwargs))
+
     def to_qasm(self):
         reps = []
         for layer in self.layers:
@@ -200,3 +222,117 @@ class UnsplittedCircuit(torch.nn.Module):
             mm = mod.to_matrix(**kwargs)
             m = mm if m is None else m @ mm
         return m
+
+
+def _global_twin(mod: torch.nn.Module, to_global: typing.Dict[int, int], num_qubits: int) -> torch.nn.Module:
+    """The built gate `mod` of a subcircuit, placed on the parent circuit's
+    qubits; a rotation's twin shares the subcircuit gate's theta Parameter,
+    so gradients and optimiser steps reach the subcircuit's parameters."""
+    if isinstance(mod, operators.BuiltCNOT):
+        return operators.BuiltCNOT(control=to_global[mod.c], target=to_global[mod.t], num_qubits=num_qubits)
+    if isinstance(mod, operators.BuiltU):
+        return operators.BuiltU(qubit=to_global[mod.qubit], matrix=mod.original_matrix, num_qubits=num_qubits,
+                                self_description=mod.description)
+    if isinstance(mod, operators.BuiltParametrizedOperator):
+        twin = type(mod)(qubit=to_global[mod.qubit], remapping=mod.remapping, num_qubits=num_qubits,
+                         initialtheta=mod.theta.detach().clone(), name=mod.name)
+        twin.theta = mod.theta
+        return twin
+    if isinstance(mod, operators.BuiltReset):
+        return operators.BuiltReset(qubit=to_global[mod.qubit], num_qubits=num_qubits)
+    raise ValueError(f"{type(mod).__name__} cannot run inside a split circuit")
+
+
+class Subcircuit(torch.nn.Module):
+    """One subcircuit of a split circuit (qcircuit.py:271-313): its layers act
+    on the subcircuit's qubits 0..m-1, `mapping` sends each parent qubit to
+    its subcircuit qubit.  The reference reshapes the state so that the
+    subcircuit's qubits form the fast axis and runs the small circuit; here
+    the same gates run on the parent state at the parent qubits (twins that
+    share the parameters), which is the same linear map."""
+
+    def __init__(self, num_qubits_parent: int, mapping: typing.Dict[int, int], layers: list):
+        super().__init__()
+        self.num_qubits_parent = num_qubits_parent
+        self.mapping = mapping
+        self.layers = torch.nn.ModuleList(UnsplittedCircuit._build_layers(layers, num_qubits=len(mapping)))
+        to_global = {v: k for k, v in mapping.items()}
+        # not registered: the twins' parameters are the layers' own
+        self.__dict__["twins"] = [_global_twin(m, to_global, num_qubits_parent) for m in self.layers]
+
+    def _apply(self, fn, *args, **kwargs):
+        super()._apply(fn, *args, **kwargs)
+        for t in self.twins:
+            t._apply(fn, *args, **kwargs)
+        return self
+
+    def forward(self, x, **kwargs):
+        for mod in self.twins:
+            x = mod(x, **kwargs) if mod.named else mod(x)
+        return x
+
+    def to_qasm(self):
+        """Representations with the subcircuit qubits mapped back (qcircuit.py:297-313)."""
+        import re
+
+        to_global = {v: k for k, v in self.mapping.items()}
+        reps = [mod.to_qasm() for mod in self.layers if hasattr(mod, "to_qasm")]
+        out = []
+        for r in reps:
+            for rr in (r if isinstance(r, list) else [r]):
+                if rr.qubit not in ("", None):
+                    rr.qubit = to_global[rr.qubit]
+                else:
+                    rr.gate_str = re.sub(r"q\[(\d+)\]", lambda mt: f"q[{to_global[int(mt.group(1))]}]",
+                                         rr.gate_str)
+                out.append(rr)
+        return out
+
+
+class SplittedCircuit(UnsplittedCircuit):
+    """A circuit cut into subcircuits by qandle_gb300.splitter (qcircuit.py:215-268).
+    `subcircuits` hold the reference's structure; `layers` are all their gates
+    on the parent qubits in subcircuit order, which is what the executors run
+    (the fused engine as one program, the plain engine gate by gate)."""
+
+    def __init__(self, num_qubits: int, subcircuitdict: dict):
+        torch.nn.Module.__init__(self)
+        self.num_qubits = num_qubits
+        state = torch.zeros(2 ** num_qubits, dtype=torch.complex64)
+        state[0] = 1
+        self.register_buffer("state", state, persistent=False)
+        self._check_qubit_order(subcircuitdict)
+        self.subcircuits = torch.nn.ModuleList(
+            [Subcircuit(num_qubits, subcircuitdict[i].mapping, subcircuitdict[i].layers) for i in subcircuitdict])
+
+    @staticmethod
+    def _check_qubit_order(subcircuitdict):
+        for sc in subcircuitdict.values():
+            keys = sorted(sc.mapping.keys())
+            values = [sc.mapping[k] for k in keys]
+            assert values == sorted(values), f"Mapping {sc.mapping} is not ordered."
+
+    @property
+    def layers(self) -> list:
+        return [t for sc in self.subcircuits for t in sc.twins]
+
+    def to_qasm(self):
+        return [sc.to_qasm() for sc in self.subcircuits]
+
+    def to_matrix(self, **kwargs):
+        raise NotImplementedError("Can't get matrix representation of a splitted circuit.")
+
+    def decompose(self) -> "UnsplittedCircuit":
+        return UnsplittedCircuit(self.num_qubits, self.layers)
+
+
+class _UnbuiltLayers:
+    """The layers given to Circuit(...) before building, as the splitter sees
+    them (qcircuit.py:17-26)."""
+
+    def __init__(self, num_qubits: int, layers: list):
+        self.num_qubits = num_qubits
+        self.layers = layers
+
+    def decompose(self):
+        return self

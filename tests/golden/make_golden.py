@@ -521,6 +521,127 @@ def qasm_cases(qandle):
     return out
 
 
+def split_layers(Q, gates):
+    """Layers from ("cnot", c, t) / (axis, qubit, theta or None, name or None)."""
+    out = []
+    for g in gates:
+        if g[0] == "cnot":
+            out.append(Q.CNOT(g[1], g[2]))
+        else:
+            cls = {"rx": Q.RX, "ry": Q.RY, "rz": Q.RZ}[g[0]]
+            kw = {}
+            if g[2] is not None:
+                kw["theta"] = float(g[2])
+            if g[3] is not None:
+                kw["name"] = g[3]
+            out.append(cls(g[1], **kw))
+    return out
+
+
+def split_record(circuit) -> list:
+    """Subcircuits of a split Circuit as plain data: mapping and gates
+    (("cnot", c, t) / (axis, qubit, theta or None, name or None)), no
+    remapping evaluated."""
+    out = []
+    for sc in circuit.circuit.subcircuits:
+        layers = []
+        for la in sc.layers:
+            kind = type(la).__name__.replace("Built", "").lower()
+            if kind == "cnot":
+                layers.append(["cnot", int(la.c), int(la.t)])
+            else:
+                th = None if la.named else float(la.theta.detach().reshape(-1)[0])
+                layers.append([kind, int(la.qubit), th, la.name])
+        out.append({"mapping": sorted([int(k), int(v)] for k, v in sc.mapping.items()), "layers": layers})
+    return out
+
+
+def split_circuits() -> dict:
+    """name -> (gates, num_qubits, max_qubits, via) for the splitter fixtures;
+    via "method" is Circuit(...).split(k), "constructor" is
+    Circuit(..., split_max_qubits=k)."""
+    cnot10 = [("cnot", 0, 1), ("cnot", 0, 2), ("cnot", 1, 2), ("cnot", 2, 3), ("cnot", 3, 4), ("cnot", 4, 3),
+              ("cnot", 3, 4), ("cnot", 4, 3), ("cnot", 3, 4), ("cnot", 4, 3), ("cnot", 3, 4), ("cnot", 4, 3),
+              ("cnot", 3, 5), ("cnot", 5, 6), ("cnot", 6, 7), ("cnot", 6, 1), ("cnot", 7, 8), ("cnot", 8, 9)]
+    cases = {
+        "cnot10_k5": (cnot10, 10, 5, "method"),
+        "cnot10_k3": (cnot10, 10, 3, "method"),
+        "dummy_k2": ([("rx", 0, 0.3, None), ("cnot", 0, 2), ("ry", 1, -0.7, None), ("cnot", 1, 2)], 3, 2,
+                     "constructor"),
+    }
+    sel = []
+    for d, rng in enumerate((1, 2)):
+        for q in range(6):
+            for r, axis in enumerate(("rz", "ry", "rz")):
+                sel.append((axis, q, round(0.1 * (1 + q + 6 * r + 18 * d), 4), None))
+        for q in range(6):
+            sel.append(("cnot", q, (q + rng) % 6))
+    cases["sel6_k3"] = (sel, 6, 3, "method")
+    cases["sel6_k4"] = (sel, 6, 4, "constructor")
+    for seed in range(6):
+        rng = np.random.default_rng(100 + seed)
+        n = int(rng.integers(5, 9))
+        gates = [("cnot", q, q + 1) for q in range(n - 1)]  # every qubit meets a CNOT
+        for _ in range(int(rng.integers(30, 70))):
+            if rng.random() < 0.5:
+                a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+                gates.append(("cnot", a, b))
+            else:
+                axis = ("rx", "ry", "rz")[int(rng.integers(3))]
+                q = int(rng.integers(n))
+                if rng.random() < 0.15:
+                    gates.append((axis, q, None, f"in{q}"))
+                else:
+                    gates.append((axis, q, round(float(rng.uniform(-3, 3)), 4), None))
+        perm = rng.permutation(len(gates))
+        gates = [gates[i] for i in perm]
+        k = int(rng.integers(2, 6))
+        cases[f"random{seed}_k{k}"] = (gates, n, k, "method" if seed % 2 == 0 else "constructor")
+    return cases
+
+
+def build_split(Q, gates, n, k, via):
+    layers = split_layers(Q, gates)
+    if via == "constructor":
+        return Q.Circuit(layers=layers, num_qubits=n, split_max_qubits=k)
+    return Q.Circuit(layers=layers, num_qubits=n).split(max_qubits=k)
+
+
+def split_inputs(n: int, gates) -> tuple:
+    """Seeded input state [2^n] (complex128, normalised) and named inputs
+    (name -> float) for running a split circuit."""
+    rng = np.random.default_rng(7)
+    psi = rng.normal(size=(1 << n,)) + 1j * rng.normal(size=(1 << n,))
+    psi /= np.linalg.norm(psi)
+    names = sorted({g[3] for g in gates if g[0] != "cnot" and g[3] is not None})
+    return psi, {nm: 0.25 + 0.1 * i for i, nm in enumerate(names)}
+
+
+def splitter_cases(qandle):
+    """The reference splitter's subcircuits (qandle/splitter/main.py) for the
+    circuits of split_circuits(), as JSON, and the split circuit's output state
+    for split_inputs().  The splitter gives its rotations the default
+    remapping (qw_map.tanh, unpinned), so the states are made with the
+    identity as default remapping."""
+    import qandle.config as ref_config
+
+    out = {}
+    saved = ref_config.DEFAULT_MAPPING
+    ref_config.DEFAULT_MAPPING = _qw_none
+    try:
+        for name, (gates, n, k, via) in split_circuits().items():
+            circ = build_split(qandle, gates, n, k, via)
+            out[name] = np.array(json.dumps(split_record(circ)))
+            psi, named = split_inputs(n, gates)
+            with torch.no_grad():
+                st = circ(torch.tensor(psi, dtype=torch.cfloat),
+                          **{nm: torch.tensor(v, dtype=torch.float32) for nm, v in named.items()})
+            out[name + "_state"] = st.numpy().astype(np.complex128)
+    finally:
+        ref_config.DEFAULT_MAPPING = saved
+    return out
+
+
 def _qw_none(x):
     return x
 
@@ -544,6 +665,7 @@ def main():
         "special": special_cases,
         "amplitude": amplitude_cases,
         "qasm": qasm_cases,
+        "splitter": splitter_cases,
     }
     only = [g for g in args.only.split(",") if g]
     for name, fn in groups.items():
