@@ -8,7 +8,7 @@ on hand-written CUDA kernels through the C ABI of libqandle_gb300.so.
 There is no CPU execution path: tensors must live on a CUDA device.
 """
 # ruff: noqa: F401 F403
-from . import config, errors, qasm, remap, splitter
+from . import config, errors, qasm, remap, splitter, utils
 from .tune import autotune
 from .operators import *
 from .embeddings import *
@@ -17,6 +17,9 @@ from .ansaetze import *
 from .qcircuit import *
 from .convolution import QConv
 from .errors import UnbuiltGateError
+from .qasm import QasmRepresentation, convert_to_qasm
+from .splitter import split, SubcircuitContainer
+from .utils import reduce_dot, parse_rot, do_not_implement, get_matrix_transforms
 
 __version__ = "1.0.0"
 
