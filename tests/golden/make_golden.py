@@ -642,6 +642,93 @@ def splitter_cases(qandle):
     return out
 
 
+def ansatz_circuits() -> dict:
+    """name -> (kind, num_qubits, constructor arguments) for the ansatz fixtures."""
+    return {
+        "twolocal_full": ("twolocal", 4, dict(qubits=[0, 1, 2, 3], depth=3)),
+        "twolocal_sub": ("twolocal", 4, dict(qubits=[1, 2, 3], depth=2)),
+        "su_full": ("su", 4, dict(qubits=[0, 1, 2, 3], reps=2, rotations=["rx", "ry"])),
+        "su_sub": ("su", 4, dict(qubits=[0, 2, 3], reps=1, rotations=["ry"])),
+        "su_rz": ("su", 3, dict(qubits=[0, 1, 2], reps=3, rotations=["rz", "rx"])),
+        "budget_cnot": ("budget", 4, dict(param_budget=10, control_gate_spacing=1)),
+        "budget_cz": ("budget", 4, dict(param_budget=9, control_gate_spacing=2, control="cz")),
+        "budget_sub": ("budget", 5, dict(qubits=[0, 2, 4], param_budget=7, control_gate_spacing=1,
+                                         rotations=["ry", "rx", "rz"])),
+        "twolocal_6": ("twolocal", 6, dict(qubits=[0, 1, 2, 3, 4, 5], depth=2)),
+        "su_6": ("su", 6, dict(qubits=[0, 1, 2, 3, 4, 5], reps=2, rotations=["rx", "ry"])),
+        "budget_6": ("budget", 6, dict(param_budget=20, control_gate_spacing=2)),
+    }
+
+
+def build_ansatz(Q, kind: str, n: int, args: dict):
+    """A Circuit holding one ansatz of `kind`, built on n qubits."""
+    args = dict(args)
+    if kind == "twolocal":
+        lay = Q.TwoLocal(**args)
+    elif kind == "su":
+        lay = Q.SU(**args)
+    else:
+        ctl = Q.CZ if args.pop("control", "cnot") == "cz" else Q.CNOT
+        lay = Q.StronglyEntanglingLayerBudget(num_qubits_total=n, control_gate=ctl, remapping=None, **args)
+    return Q.Circuit([lay], num_qubits=n)
+
+
+def ansatz_params(circ) -> list:
+    """Deterministic values for the circuit's rotation angles, in parameters() order."""
+    k = len(list(circ.parameters()))
+    return [round(0.37 * (i + 1) - 1.5 * ((i * 7) % 3), 4) for i in range(k)]
+
+
+def gate_record(gates) -> list:
+    out = []
+    for g in gates:
+        kind = type(g).__name__.replace("Built", "").lower()
+        if kind in ("cnot", "cz"):
+            out.append([kind, int(g.c), int(g.t)])
+        else:
+            out.append([kind, int(g.qubit)])
+    return out
+
+
+def ansatz_cases(qandle):
+    """The reference's ansaetze (qandle/ansaetze/): decompositions, parameter
+    count and output state for ansatz_params() on a seeded unbatched input
+    (the default remapping set to the identity, qw_map.tanh being unpinned)."""
+    import qandle.config as ref_config
+
+    out = {}
+    saved = ref_config.DEFAULT_MAPPING
+    ref_config.DEFAULT_MAPPING = _qw_none
+    try:
+        for name, (kind, n, args) in ansatz_circuits().items():
+            torch.manual_seed(3)
+            circ = build_ansatz(qandle, kind, n, args)
+            vals = ansatz_params(circ)
+            with torch.no_grad():
+                for p, v in zip(circ.parameters(), vals):
+                    p.fill_(v)
+            built = circ.circuit.layers[0]
+            rng = np.random.default_rng(11)
+            psi = rng.normal(size=(1 << n,)) + 1j * rng.normal(size=(1 << n,))
+            psi /= np.linalg.norm(psi)
+            with torch.no_grad():
+                st = circ(torch.tensor(psi, dtype=torch.cfloat))
+            rec = {"params": vals, "built_decompose": gate_record(built.decompose())}
+            if kind != "budget":
+                rec["unbuilt_decompose"] = gate_record(build_unbuilt_ansatz(qandle, kind, args).decompose())
+            out[name] = np.array(json.dumps(rec))
+            out[name + "_state"] = st.numpy().astype(np.complex128)
+    finally:
+        ref_config.DEFAULT_MAPPING = saved
+    return out
+
+
+def build_unbuilt_ansatz(Q, kind: str, args: dict):
+    if kind == "twolocal":
+        return Q.TwoLocal(**args)
+    return Q.SU(**args)
+
+
 def _qw_none(x):
     return x
 
@@ -666,6 +753,7 @@ def main():
         "amplitude": amplitude_cases,
         "qasm": qasm_cases,
         "splitter": splitter_cases,
+        "ansaetze": ansatz_cases,
     }
     only = [g for g in args.only.split(",") if g]
     for name, fn in groups.items():
