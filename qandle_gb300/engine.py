@@ -150,6 +150,10 @@ class Lowered:
         elif hasattr(mod, "mods"):  # StronglyEntanglingLayerBuilt and other built ansaetze
             for m in mod.mods:
                 self.add_layer(m)
+        elif name == "Circuit" and hasattr(mod, "circuit"):  # a nested circuit: its layers, inline
+            if mod.num_qubits != self.n:
+                raise ValueError(f"a nested circuit on {mod.num_qubits} qubits inside one on {self.n}")
+            self.add_layer(mod.circuit)
         elif hasattr(mod, "layers") and hasattr(mod, "num_qubits"):
             for m in mod.layers:
                 self.add_layer(m)

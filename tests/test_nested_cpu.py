@@ -1,0 +1,56 @@
+"""Circuits used as layers of another circuit (qandle allows it: they are
+modules).  The fused engine lowers a nested circuit's layers inline: the
+lowering equals that of the decomposed circuit, and the planned program,
+emulated, equals the oracle."""
+import numpy as np
+import pytest
+import torch
+
+import qandle_gb300 as q
+from oracle import oracle
+from qandle_gb300 import engine
+from tests import program_emulator as emu
+from tests.test_planner import _runtime
+
+
+def _nested(n=6):
+    c1 = q.Circuit(layers=[q.RX(0, theta=0.3, remapping=None), q.CNOT(0, 1)], num_qubits=n)
+    c2 = q.Circuit(layers=[q.RY(1, theta=-0.8, remapping=None),
+                           q.StronglyEntanglingLayer(qubits=list(range(1, n)), remapping=None)], num_qubits=n)
+    inner = q.Circuit(layers=[c2, q.CNOT(n - 1, 0)], num_qubits=n)
+    return q.Circuit(layers=[c1, q.RZ(0, theta=1.1, remapping=None), inner], num_qubits=n)
+
+
+def test_nested_lowering_equals_decomposed():
+    c = _nested()
+    lo, ld = engine.lower(c.circuit), engine.lower(c.decompose().circuit)
+    assert lo.gates == ld.gates
+    assert [float(m.theta.detach()) for m in lo.param_mods] == [float(m.theta.detach()) for m in ld.param_mods]
+    # the nested modules' parameters are the ones the program reads
+    ids = {id(p) for p in c.parameters()}
+    assert all(id(m.theta) in ids for m in lo.param_mods)
+
+
+def test_nested_plan_matches_oracle():
+    n = 6
+    c = _nested(n)
+    lo = engine.lower(c.circuit)
+    prog = engine.Program(lo, "state", keep_state=False)
+    params, named, umats, embed = _runtime(lo, {"n": n, "batch": 1, "inputs": {}}, 1)
+    st, _ = emu.run_forward(prog, n, 1, params, named, umats, embed=embed)
+    gates = []
+    for m in c.decompose().circuit.layers:
+        kind = type(m).__name__.replace("Built", "").lower()
+        if kind == "cnot":
+            gates.append(("cnot", m.c, m.t))
+        else:
+            gates.append((kind, m.qubit, float(m.remapping(m.theta).detach().reshape(-1)[0]), None))
+    ref = oracle.run({"n": n, "batch": 1, "gates": gates, "inputs": {}, "measure": "state", "targets": None})
+    assert np.abs(st - ref).max() < 1e-10
+
+
+def test_nested_width_mismatch_is_refused():
+    small = q.Circuit(layers=[q.CNOT(0, 1)], num_qubits=2)
+    big = q.Circuit(layers=[small, q.CNOT(2, 3)], num_qubits=6)
+    with pytest.raises(ValueError):
+        engine.lower(big.circuit)
