@@ -3,13 +3,13 @@
 //
 // One persistent CTA per SM walks the tiles of a pass.  A tile is 2^TB
 // amplitudes (TB = 13 forward, 12 backward) spanning TB qubits of one sample,
-// or whole samples when n < TB.  Its memory image is 2^(TB - run_bits)
-// contiguous runs of 2^run_bits amplitudes; every thread moves 16-byte pieces
-// of them with cp.async into shared-memory buffers, so later tiles stream in
-// while the current one is computed, and the result goes back straight from
-// registers.  Threads hold 2^RB amplitudes each in registers; gates act in
-// registers, and an OP_MAP exchange through a swizzled shared-memory layout
-// changes which tile qubits are register qubits.  The forward kernel body
+// or whole samples when n < TB.  Its memory image is contiguous blocks of at
+// least 2^run_bits amplitudes; producer warps move them between global memory
+// and a ring of shared-memory tile buffers with bulk (TMA) copies, so later
+// tiles stream in and earlier ones stream out while the compute warps work on
+// the current one.  Compute threads hold 2^RB amplitudes each in registers;
+// gates act in registers, and an OP_MAP exchange through a swizzled
+// shared-memory layout changes which tile qubits are register qubits.  The forward kernel body
 // lives in fwd_kernel.cuh; this file holds its op interpreter, the backward
 // kernel, the helper kernels and the host side.
 //

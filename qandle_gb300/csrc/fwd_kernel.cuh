@@ -4,8 +4,8 @@
 // header, so the same text is handed to NVRTC.
 //
 // A pass walks tiles of 2^TB amplitudes through a ring of three shared-memory
-// buffers.  Producer warps move the tiles: they load tile t+1 with async
-// copies (cp.async) and store tile t-2 while the compute warps work on tile t,
+// buffers.  Producer warps move the tiles with bulk (TMA) copies: they load
+// tile t+1 and store tile t-2 while the compute warps work on tile t,
 // and the two sides hand buffers over through a full and an empty mbarrier per
 // buffer.  A compute thread holds 2^RB amplitudes in registers
 // (planar.cuh); the gate program of the pass runs on them (`Ops`), exchanging
