@@ -9,9 +9,9 @@
 // tiles stream in and earlier ones stream out while the compute warps work on
 // the current one.  Compute threads hold 2^RB amplitudes each in registers;
 // gates act in registers, and an OP_MAP exchange through a swizzled
-// shared-memory layout changes which tile qubits are register qubits.  The forward kernel body
-// lives in fwd_kernel.cuh; this file holds its op interpreter, the backward
-// kernel, the helper kernels and the host side.
+// shared-memory layout changes which tile qubits are register qubits.  The
+// forward kernel body lives in fwd_kernel.cuh; this file holds its op
+// interpreter, the backward kernel, the helper kernels and the host side.
 //
 // The gate programs come from the planner in program.cpp.  The rotation and
 // matrix algebra follows the reference's row-vector convention,
