@@ -97,9 +97,9 @@ class U(UnbuiltOperator):
     def build(self, num_qubits, **kwargs) -> "BuiltU":
         return BuiltU(qubit=self.qubit, matrix=self.matrix, num_qubits=num_qubits)
 
-
     def to_qasm(self):
         return qasm.QasmRepresentation(gate_str="U", qubit=self.qubit)
+
 
 class BuiltU(BuiltOperator):
     """Built fixed gate (operators.py:87-129).  Keeps the 2x2 only."""
@@ -167,13 +167,13 @@ class UnbuiltParametrizedOperator(UnbuiltOperator):
             qubit=self.qubit, initialtheta=self.theta, name=self.name,
             remapping=self.remapping, num_qubits=num_qubits)
 
-
     def to_qasm(self):
         if self.named:
             return qasm.QasmRepresentation(gate_str=self.__class__.__name__.lower(), qubit=self.qubit,
                                            qasm3_inputs=self.name)
         return qasm.QasmRepresentation(gate_str=self.__class__.__name__.lower(), qubit=self.qubit,
                                        gate_value=self.remapping(self.theta).item())
+
 
 class BuiltParametrizedOperator(BuiltOperator, abc.ABC):
     """Built rotation (operators.py:215-305): theta is a Parameter, the angle
@@ -221,13 +221,13 @@ class BuiltParametrizedOperator(BuiltOperator, abc.ABC):
             return torch.stack([_kron_embed(m, self.qubit, self.num_qubits) for m in m2.reshape(-1, 2, 2)])
         return _kron_embed(m2.reshape(2, 2), self.qubit, self.num_qubits)
 
-
     def to_qasm(self):
         if self.named:
             return qasm.QasmRepresentation(gate_str=self.unbuilt_class.__name__.lower(), qubit=self.qubit,
                                            qasm3_inputs=self.name)
         return qasm.QasmRepresentation(gate_str=self.unbuilt_class.__name__.lower(), qubit=self.qubit,
                                        gate_value=self.remapping(self.theta).item())
+
 
 class RX(UnbuiltParametrizedOperator):
     """Parametrised RX gate (operators.py:308-325)."""
@@ -267,9 +267,9 @@ class CNOT(UnbuiltOperator):
     def build(self, num_qubits, **kwargs) -> "BuiltCNOT":
         return BuiltCNOT(control=self.c, target=self.t, num_qubits=num_qubits)
 
-
     def to_qasm(self):
         return qasm.QasmRepresentation(gate_str=f"cx q[{self.c}], q[{self.t}]")
+
 
 class CZ(UnbuiltOperator):
     """CZ gate (operators.py:518-533)."""
@@ -285,9 +285,9 @@ class CZ(UnbuiltOperator):
     def build(self, num_qubits, **kwargs) -> "BuiltCZ":
         return BuiltCZ(control=self.c, target=self.t, num_qubits=num_qubits)
 
-
     def to_qasm(self):
         return qasm.QasmRepresentation(gate_str=f"cz q[{self.c}], q[{self.t}]")
+
 
 class SWAP(UnbuiltOperator):
     """SWAP gate (operators.py:686-699)."""
@@ -302,9 +302,9 @@ class SWAP(UnbuiltOperator):
     def build(self, num_qubits, **kwargs) -> "BuiltSWAP":
         return BuiltSWAP(a=self.a, b=self.b, num_qubits=num_qubits)
 
-
     def to_qasm(self):
         return qasm.QasmRepresentation(gate_str=f"swap q[{self.a}], q[{self.b}]")
+
 
 def _perm_matrix(fn, num_qubits):
     dim = 2 ** num_qubits
@@ -335,9 +335,9 @@ class BuiltCNOT(BuiltOperator):
         c2, t2 = n - self.c - 1, n - self.t - 1
         return _perm_matrix(lambda i: ((i ^ (1 << t2)) if i & (1 << c2) else i, 1.0), n).T.contiguous()
 
-
     def to_qasm(self):
         return CNOT(self.c, self.t).to_qasm()
+
 
 class BuiltCZ(BuiltOperator):
     """Negate amplitudes with both bits set (operators.py:570-601)."""
@@ -360,9 +360,9 @@ class BuiltCZ(BuiltOperator):
         d = torch.tensor([-1.0 if (i & m) == m else 1.0 for i in range(2 ** n)], dtype=torch.complex64)
         return torch.diag(d)
 
-
     def to_qasm(self):
         return CZ(self.c, self.t).to_qasm()
+
 
 class BuiltSWAP(BuiltOperator):
     """Exchange two qubits (operators.py:653-684)."""
@@ -390,9 +390,9 @@ class BuiltSWAP(BuiltOperator):
 
         return _perm_matrix(f, n).T.contiguous()
 
-
     def to_qasm(self):
         return SWAP(self.a, self.b).to_qasm()
+
 
 class Invert(UnbuiltOperator):
     """Inverse of a target operator (operators.py:416-432)."""
@@ -406,9 +406,9 @@ class Invert(UnbuiltOperator):
     def build(self, num_qubits, **kwargs) -> "BuiltInvert":
         return BuiltInvert(target=self.t, num_qubits=num_qubits)
 
-
     def to_qasm(self):
         return qasm.QasmRepresentation(gate_str=f"{self.t}^-1")
+
 
 class BuiltInvert(BuiltOperator):
     """state @ inv(target matrix) (operators.py:435-459).  Rotations run as
@@ -445,9 +445,9 @@ class BuiltInvert(BuiltOperator):
     def to_matrix(self, **kwargs) -> torch.Tensor:
         return torch.linalg.inv(self.target.to_matrix())
 
-
     def to_qasm(self):
         return Invert(self.target).to_qasm()
+
 
 class Controlled(UnbuiltOperator):
     """Apply the target operator where the control qubit is 1 (operators.py:462-478)."""
@@ -462,9 +462,9 @@ class Controlled(UnbuiltOperator):
     def build(self, num_qubits, **kwargs) -> "BuiltControlled":
         return BuiltControlled(control=self.c, target=self.t, num_qubits=num_qubits)
 
-
     def to_qasm(self):
         return qasm.QasmRepresentation(gate_str=f"controlled q[{self.c}], {self.t}")
+
 
 class BuiltControlled(BuiltOperator):
     """Target on the control-1 subspace, control-0 amplitudes kept
@@ -512,9 +512,9 @@ class BuiltControlled(BuiltOperator):
     def to_matrix(self, **kwargs) -> torch.Tensor:
         return self.t.to_matrix()  # what the reference returns (operators.py:514-515)
 
-
     def to_qasm(self):
         return Controlled(self.c, self.t).to_qasm()
+
 
 class Reset(UnbuiltOperator):
     """Reset a qubit to |0> while preserving the norm (operators.py:632-650)."""
@@ -528,9 +528,9 @@ class Reset(UnbuiltOperator):
     def build(self, num_qubits, **kwargs) -> "BuiltReset":
         return BUILT_CLASS_RELATION[self.__class__](qubit=self.qubit, num_qubits=num_qubits)
 
-
     def to_qasm(self):
         return qasm.QasmRepresentation(gate_str="reset", qubit=self.qubit)
+
 
 class BuiltReset(BuiltOperator):
     """Per pair of amplitudes differing in the qubit: a0 * |pair| / (|a0| +
@@ -550,9 +550,9 @@ class BuiltReset(BuiltOperator):
     def to_matrix(self, **kwargs) -> torch.Tensor:
         raise ValueError("Reset gate does not have a matrix representation.")
 
-
     def to_qasm(self):
         return Reset(self.qubit).to_qasm()
+
 
 class rdict(dict):
     """Reversible dict (operators.py:702-706)."""

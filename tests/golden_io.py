@@ -32,6 +32,7 @@ def circuit_desc(z, name):
 
 # ---- Invert / Controlled / Reset cases (special.npz) ----
 
+
 def _u(spec_m):
     return np.array([complex(a, b) for a, b in spec_m], dtype=np.complex64).reshape(2, 2)
 
