@@ -21,7 +21,7 @@ import typing
 
 import torch
 
-from . import config, remap
+from . import config, remap, utils
 from . import operators as op
 from .embeddings import parse_rot
 
@@ -104,11 +104,18 @@ class StronglyEntanglingLayerBuilt(op.BuiltOperator):
         return [g.to_qasm() for g in self.decompose()]
 
     def to_matrix(self, **kwargs):
-        m = None
-        for mod in self.mods:
-            mm = mod.to_matrix(**kwargs)
-            m = mm if m is None else m @ mm
-        return m
+        return _decomposed_matrix(self, **kwargs)
+
+
+def _decomposed_matrix(ansatz, **kwargs) -> torch.Tensor:
+    """to_matrix of a built ansatz as the reference forms it
+    (ansaetze/ansatz.py:26-33): the gates of decompose(), built on the
+    ansatz's qubit count, their matrices combined by utils.reduce_dot (later
+    gates multiply from the left; the result has a batch axis).  For gates
+    that do not commute this is not the matrix of forward() in the row
+    convention; it is kept identical to the reference's result."""
+    gates = [g.build(num_qubits=ansatz.num_qubits) if hasattr(g, "build") else g for g in ansatz.decompose()]
+    return utils.reduce_dot(*[g.to_matrix(**kwargs) for g in gates])
 
 
 def _chain(qubits: typing.List[int]) -> typing.List[op.CNOT]:
@@ -209,11 +216,7 @@ class TwoLocalBuilt(op.BuiltOperator):
         return out
 
     def to_matrix(self, **kwargs):
-        m = None
-        for mod in self.mods:
-            mm = mod.to_matrix(**kwargs)
-            m = mm if m is None else m @ mm
-        return m
+        return _decomposed_matrix(self, **kwargs)
 
 
 class SpecialUnitary(op.UnbuiltOperator):
@@ -293,11 +296,7 @@ class SpecialUnitaryBuilt(op.BuiltOperator):
         return "SU"
 
     def to_matrix(self, **kwargs):  # (the registered transform modules do not shadow methods)
-        m = None
-        for mod in self.mods:
-            mm = mod.to_matrix(**kwargs)
-            m = mm if m is None else m @ mm
-        return m
+        return _decomposed_matrix(self, **kwargs)
 
     def to_qasm(self):
         return [g.to_qasm() for g in self.decompose()]
@@ -369,8 +368,4 @@ class StronglyEntanglingLayerBudget(op.BuiltOperator):
         return self.layers(x)
 
     def to_matrix(self, **kwargs):
-        m = None
-        for mod in self.layers:
-            mm = mod.to_matrix(**kwargs)
-            m = mm if m is None else m @ mm
-        return m
+        return _decomposed_matrix(self, **kwargs)

@@ -20,7 +20,7 @@ import warnings
 
 import torch
 
-from . import operators
+from . import operators, utils
 from . import measurements
 
 __all__ = ["Circuit", "UnsplittedCircuit", "SplittedCircuit", "Subcircuit"]
@@ -217,11 +217,10 @@ class UnsplittedCircuit(torch.nn.Module):
         return reps
 
     def to_matrix(self, **kwargs):
-        m = None
-        for mod in self.layers:
-            mm = mod.to_matrix(**kwargs)
-            m = mm if m is None else m @ mm
-        return m
+        """The layers' matrices combined by utils.reduce_dot, as the reference
+        does (qcircuit.py:208-212): later layers multiply from the left and
+        the result has a batch axis."""
+        return utils.reduce_dot(*[mod.to_matrix(**kwargs) for mod in self.layers])
 
 
 def _global_twin(mod: torch.nn.Module, to_global: typing.Dict[int, int], num_qubits: int) -> torch.nn.Module:

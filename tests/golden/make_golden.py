@@ -17,7 +17,10 @@ place (PennyLane is not installed): per-gate sweeps
 embeddings (test/test_embeddings.py:56-153), measurements
 (test/test_measurements.py:6-48), strongly entangling layers
 (test/test_ansaetze.py:6-83), plus small instances of the four measured
-circuit families and torch-autograd gradients through the reference.
+circuit families and torch-autograd gradients through the reference; the
+special gates (Invert, Controlled, Reset), AmplitudeEmbedding, the OpenQASM
+export, the splitter's subcircuits, the other ansaetze and the to_matrix()
+results of gates, ansaetze and circuits.
 
 Output: one compressed .npz per group, arrays only (no pickles).  Circuit
 descriptions are stored as JSON strings next to their arrays.
@@ -733,6 +736,79 @@ def _qw_none(x):
     return x
 
 
+MATRIX_QUBITS = 3
+MATRIX_NAMED = [0.3, -1.2, 2.0]  # values of the named input "a" for the named rotation
+MATRIX_SEED = 5  # torch seed set before each to_matrix call
+
+
+def matrix_ops(Q) -> dict:
+    """name -> built module whose to_matrix() the fixtures pin, for package
+    `Q` (the reference or qandle_gb300), on MATRIX_QUBITS qubits.  Call with
+    the package's config.DEFAULT_MAPPING set to the identity (qw_map.tanh is
+    unpinned).  Rotation angles are fixed after building."""
+    n = MATRIX_QUBITS
+    m = torch.tensor(workloads.u3_row_matrix(0.3, 1.1, -0.7))
+    w = torch.tensor([[[0.1, 0.2, 0.3], [0.4, 0.5, 0.6], [0.7, 0.8, 0.9]],
+                      [[-0.2, 1.3, 0.4], [0.9, -1.1, 0.2], [0.5, 0.6, -0.7]]])
+    ops = {
+        "rx_q0": Q.RX(qubit=0, theta=0.543321, remapping=None),
+        "ry_q1": Q.RY(qubit=1, theta=0.543321, remapping=None),
+        "rz_q2": Q.RZ(qubit=2, theta=0.543321, remapping=None),
+        "rx_named": Q.RX(qubit=1, name="a", remapping=None),
+        "u_q1": Q.U(qubit=1, matrix=m),
+        "cnot_02": Q.CNOT(0, 2),
+        "cnot_20": Q.CNOT(2, 0),
+        "cz_12": Q.CZ(1, 2),
+        "swap_02": Q.SWAP(a=0, b=2),
+        "invert_ry": Q.Invert(Q.RY(qubit=1, theta=0.7, remapping=None).build(num_qubits=n)),
+        "invert_u": Q.Invert(Q.U(qubit=2, matrix=m).build(num_qubits=n)),
+        "controlled_rx": Q.Controlled(0, Q.RX(qubit=2, theta=0.9, remapping=None)),
+        "measure": Q.MeasureProbability(),
+        "sel": Q.StronglyEntanglingLayer(qubits=[0, 1, 2], depth=2, q_params=w, remapping=None),
+        "sel_sub": Q.StronglyEntanglingLayer(qubits=[0, 2], depth=2, q_params=w[:, :2].clone(), remapping=None),
+        "twolocal": Q.TwoLocal(qubits=[0, 1, 2], depth=2),
+        "su": Q.SU(qubits=[0, 1, 2], reps=2, rotations=["rx", "ry"]),
+    }
+    built = {k: v.build(num_qubits=n) for k, v in ops.items()}
+    built["budget"] = Q.StronglyEntanglingLayerBudget(num_qubits_total=n, param_budget=7, control_gate_spacing=1,
+                                                      rotations=["rz", "ry"], remapping=None)
+    built["circuit"] = Q.Circuit([Q.RX(qubit=0, theta=0.4, remapping=None), Q.CNOT(0, 1),
+                                  Q.RY(qubit=2, theta=-1.3, remapping=None), Q.U(qubit=1, matrix=m),
+                                  Q.CZ(1, 2), Q.SWAP(a=0, b=2), Q.RZ(qubit=1, theta=2.2, remapping=None)],
+                                 num_qubits=n)
+    for name in ("twolocal", "su", "budget"):
+        params = list(built[name].parameters())
+        with torch.no_grad():
+            for i, p in enumerate(params):
+                p.fill_(round(0.37 * (i + 1) - 1.5 * ((i * 7) % 3), 4))
+    return built
+
+
+def matrix_cases(qandle):
+    """to_matrix() of built gates, ansaetze and a circuit (operators.py:60-69,
+    ansaetze/ansatz.py:26-33, qcircuit.py:208-212): the inspection half of the
+    operator API, including the reference's composition order (utils.reduce_dot
+    multiplies later gates from the left) and Controlled returning its
+    target's matrix."""
+    import qandle.config as ref_config
+
+    out = {}
+    saved = ref_config.DEFAULT_MAPPING
+    ref_config.DEFAULT_MAPPING = _qw_none
+    try:
+        for name, mod in matrix_ops(qandle).items():
+            kw = {"a": torch.tensor(MATRIX_NAMED)} if name == "rx_named" else {}
+            # the budget ansatz builds fresh gates from its unbuilt, angle-less
+            # rotations, which draw torch.rand(1) each: seed the draws
+            torch.manual_seed(MATRIX_SEED)
+            with torch.no_grad():
+                mat = mod.to_matrix(**kw)
+            out[name] = mat.detach().numpy()
+    finally:
+        ref_config.DEFAULT_MAPPING = saved
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("QANDLE_REFERENCE_SRC", ""))
@@ -754,6 +830,7 @@ def main():
         "qasm": qasm_cases,
         "splitter": splitter_cases,
         "ansaetze": ansatz_cases,
+        "matrices": matrix_cases,
     }
     only = [g for g in args.only.split(",") if g]
     for name, fn in groups.items():
