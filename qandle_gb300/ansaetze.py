@@ -5,14 +5,17 @@
 * TwoLocal (twolocal.py), SpecialUnitary / SU (specialunitary.py) and
   StronglyEntanglingLayerBudget (stronglyentangling_budget.py).
 
-Every built ansatz exposes ``mods``: its gates, built, in the order that
-gives the reference's forward result, so both engines (and the in-place
+Every built ansatz exposes ``applied_gates``: its gates, built, in the order
+that gives the reference's forward result, so both engines (and the in-place
 per-gate path) run it without a kernel of its own.  The reference's built
 TwoLocal and SU apply their CNOT chain as one matrix product on a column
-vector, ``(C_0 C_1 ... C_k) v``, i.e. the chain's last CNOT first; ``mods``
-keep that order, and ``decompose()`` returns the reference's decomposition,
-which lists the chain first to last.  (Unlike the reference, whose product
-needs an unbatched state, batched states work.)
+vector, ``(C_0 C_1 ... C_k) v``, i.e. the chain's last CNOT first;
+``applied_gates`` keep that order, and ``decompose()`` returns the
+reference's decomposition, which lists the chain first to last.  (Unlike the
+reference, whose product needs an unbatched state, batched states work.)
+The registered submodules carry the reference's names (SEL and TwoLocal
+``mods``, SU and the budget ansatz ``layers``), so state_dicts saved with
+either package load into the other.
 """
 from __future__ import annotations
 
@@ -80,6 +83,10 @@ class StronglyEntanglingLayerBuilt(op.BuiltOperator):
                                                remapping=remapping).build(num_qubits))
             layers.extend(self._get_cnots(self.qubits, self.num_qubits, d % (len(self.qubits) - 1)))
         self.mods = torch.nn.Sequential(*layers)
+
+    @property
+    def applied_gates(self) -> typing.List[torch.nn.Module]:
+        return list(self.mods)
 
     def forward(self, state: torch.Tensor):
         return self.mods(state)
@@ -174,27 +181,31 @@ class TwoLocalBuilt(op.BuiltOperator):
         self.qubits = qubits or list(range(num_qubits))
         if q_params is None or tuple(q_params.shape) != (depth, len(self.qubits)):
             q_params = torch.rand(depth, num_qubits)
-        self.layers_ry = torch.nn.ModuleList([
+        self.mods = torch.nn.ModuleList([
             torch.nn.Sequential(*[op.RY(qubit=w, theta=q_params[d, w]).build(num_qubits)
                                   for w in range(num_qubits)]) for d in range(depth)])
-        mods = []
+        chain = _chain_as_applied(self.qubits, num_qubits)
+        applied = []
         for d in range(depth):
-            mods.extend(self.layers_ry[d])
-            mods.extend(_chain_as_applied(self.qubits, num_qubits))
-        self.__dict__["_mods"] = mods  # the RY modules are registered in layers_ry
+            applied.extend(self.mods[d])
+            applied.extend(chain)
+        # not registered: the RY modules are registered in mods, the chain
+        # gates hold no parameters
+        self.__dict__["_applied"] = applied
+        self.__dict__["_chain"] = chain
 
     @property
-    def mods(self) -> typing.List[torch.nn.Module]:
-        return self._mods
+    def applied_gates(self) -> typing.List[torch.nn.Module]:
+        return self._applied
 
     def _apply(self, fn, *args, **kwargs):
         super()._apply(fn, *args, **kwargs)
-        for m in self._mods:
+        for m in self._chain:
             m._apply(fn, *args, **kwargs)
         return self
 
     def forward(self, state: torch.Tensor) -> torch.Tensor:
-        for m in self.mods:
+        for m in self.applied_gates:
             state = m(state)
         return state
 
@@ -204,14 +215,14 @@ class TwoLocalBuilt(op.BuiltOperator):
     def to_qasm(self):
         out = []
         for d in range(self.depth):
-            out.extend(g.to_qasm() for g in self.layers_ry[d])
+            out.extend(g.to_qasm() for g in self.mods[d])
             out.extend(g.to_qasm() for g in _chain(self.qubits))
         return out
 
     def decompose(self) -> typing.List[op.Operator]:
         out = []
         for d in range(self.depth):
-            out.extend(copy.deepcopy(g) for g in self.layers_ry[d])
+            out.extend(copy.deepcopy(g) for g in self.mods[d])
             out.extend(_chain(self.qubits))
         return out
 
@@ -271,24 +282,26 @@ class SpecialUnitaryBuilt(op.BuiltOperator):
         self.layers = torch.nn.ModuleList([
             torch.nn.Sequential(*[r(w).build(num_qubits=num_qubits) for w in self.qubits for r in rotations])
             for _ in range(reps + 1)])
-        mods = list(self.layers[0])
+        chain = _chain_as_applied(self.qubits, num_qubits)
+        applied = list(self.layers[0])
         for block in self.layers[1:]:
-            mods.extend(_chain_as_applied(self.qubits, num_qubits))
-            mods.extend(block)
-        self.__dict__["_mods"] = mods
+            applied.extend(chain)
+            applied.extend(block)
+        self.__dict__["_applied"] = applied  # rotations registered in layers
+        self.__dict__["_chain"] = chain
 
     @property
-    def mods(self) -> typing.List[torch.nn.Module]:
-        return self._mods
+    def applied_gates(self) -> typing.List[torch.nn.Module]:
+        return self._applied
 
     def _apply(self, fn, *args, **kwargs):
         super()._apply(fn, *args, **kwargs)
-        for m in self._mods:
+        for m in self._chain:
             m._apply(fn, *args, **kwargs)
         return self
 
     def forward(self, state: torch.Tensor) -> torch.Tensor:
-        for m in self.mods:
+        for m in self.applied_gates:
             state = m(state)
         return state
 
@@ -352,8 +365,8 @@ class StronglyEntanglingLayerBudget(op.BuiltOperator):
                 out.append(r(qubit=w, remapping=self.remapping))
 
     @property
-    def mods(self) -> torch.nn.Sequential:
-        return self.layers
+    def applied_gates(self) -> typing.List[torch.nn.Module]:
+        return list(self.layers)
 
     def __str__(self) -> str:
         return "SEL"

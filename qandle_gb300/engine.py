@@ -147,7 +147,10 @@ class Lowered:
         elif name in _MEAS:
             self.measure = _MEAS[name]
             self._measured = True
-        elif hasattr(mod, "mods"):  # StronglyEntanglingLayerBuilt and other built ansaetze
+        elif hasattr(mod, "applied_gates"):  # the built ansaetze
+            for m in mod.applied_gates:
+                self.add_layer(m)
+        elif hasattr(mod, "mods"):  # the reference's built StronglyEntanglingLayer
             for m in mod.mods:
                 self.add_layer(m)
         elif name == "Circuit" and hasattr(mod, "circuit"):  # a nested circuit: its layers, inline

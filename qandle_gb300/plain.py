@@ -413,8 +413,8 @@ def run_layers_inplace(layers, state: torch.Tensor | None, n: int, kwargs: dict,
             st = (mod(st, **kwargs) if getattr(mod, "named", False) else mod(st)).reshape(-1, 1 << n)
             if st.shape[0] != prev:
                 unbatched = False
-        elif hasattr(mod, "mods"):
-            st = run_layers_inplace(list(mod.mods), st, n, kwargs, initial)
+        elif _composite(mod, n) is not None:
+            st = run_layers_inplace(_composite(mod, n), st, n, kwargs, initial)
         else:
             # measurements: their own (out-of-place) forward ends the loop
             return mod(st.reshape(1 << n) if unbatched else st)
@@ -423,11 +423,28 @@ def run_layers_inplace(layers, state: torch.Tensor | None, n: int, kwargs: dict,
     return st.reshape(1 << n) if unbatched else st
 
 
-def _flat_layers(layers):
+def _composite(mod, n: int):
+    """The layers a composite layer runs, in order, or None for a single
+    layer: a built ansatz's applied_gates (the reference's built SEL: its
+    mods), a nested circuit's layers (on the same number of qubits)."""
+    if hasattr(mod, "applied_gates"):
+        return list(mod.applied_gates)
+    if hasattr(mod, "mods"):
+        return list(mod.mods)
+    inner = getattr(mod, "circuit", None)
+    if inner is not None and hasattr(inner, "layers") and hasattr(mod, "num_qubits"):
+        if mod.num_qubits != n:
+            raise ValueError(f"a nested circuit on {mod.num_qubits} qubits inside one on {n}")
+        return list(inner.layers)
+    return None
+
+
+def _flat_layers(layers, n: int):
     out = []
     for mod in layers:
-        if hasattr(mod, "mods"):
-            out.extend(_flat_layers(list(mod.mods)))
+        sub = _composite(mod, n)
+        if sub is not None:
+            out.extend(_flat_layers(sub, n))
         else:
             out.append(mod)
     return out
@@ -443,7 +460,7 @@ def adjoint_per_gate(layers, n: int, grad_p0: torch.Tensor, state: torch.Tensor 
     unnamed rotations in layer order.  Shares no code with the fused engine
     and serves as its per-gate baseline."""
     kwargs = kwargs or {}
-    flat = _flat_layers(layers)
+    flat = _flat_layers(layers, n)
     gates = [m for m in flat if type(m).__name__ not in ("MeasureProbabilityBuilt",)]
     with torch.no_grad():
         psi = run_layers_inplace(gates, state, n, kwargs, initial if initial is not None else state)

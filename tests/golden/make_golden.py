@@ -784,6 +784,55 @@ def matrix_ops(Q) -> dict:
     return built
 
 
+def state_dict_modules(Q) -> dict:
+    """name -> module (package `Q`) whose state_dict layout the fixtures pin.
+    Call with Q.config.DEFAULT_MAPPING set to the identity."""
+    c1 = Q.Circuit([Q.RX(0, theta=0.1, remapping=None), Q.CNOT(0, 1)], num_qubits=3)
+    c2 = Q.Circuit([Q.RY(1, theta=0.2, remapping=None), Q.StronglyEntanglingLayer(qubits=[1, 2], remapping=None)],
+                   num_qubits=3)
+    return {
+        "gates": Q.Circuit([Q.RX(0, theta=0.1, remapping=None), Q.CNOT(0, 1), Q.RY(1, name="a", remapping=None),
+                            Q.U(2, matrix=torch.eye(2, dtype=torch.cfloat)), Q.CZ(1, 2), Q.SWAP(a=0, b=2),
+                            Q.MeasureProbability()], num_qubits=3),
+        "sel": Q.Circuit([Q.AngleEmbedding(name="x", qubits=[0, 1, 2]),
+                          Q.StronglyEntanglingLayer(qubits=[0, 1, 2], depth=2, remapping=None),
+                          Q.MeasureJointProbability()], num_qubits=3),
+        "twolocal": Q.Circuit([Q.TwoLocal(qubits=[0, 1, 2], depth=2)], num_qubits=3),
+        "su": Q.Circuit([Q.SU(qubits=[0, 1, 2], reps=2, rotations=["rx", "ry"])], num_qubits=3),
+        "budget": Q.Circuit([Q.StronglyEntanglingLayerBudget(num_qubits_total=3, param_budget=5, remapping=None)],
+                            num_qubits=3),
+        "special": Q.Circuit([Q.Controlled(0, Q.RX(1, theta=0.2, remapping=None)),
+                              Q.Invert(Q.RY(2, theta=0.3, remapping=None).build(num_qubits=3)), Q.Reset(1)],
+                             num_qubits=3),
+        "amplitude": Q.Circuit([Q.AmplitudeEmbedding(name="x", qubits=[0, 1, 2]),
+                                Q.RX(0, theta=0.1, remapping=None)], num_qubits=3),
+        "split": Q.Circuit([Q.RX(0, theta=0.1, remapping=None), Q.CNOT(0, 1), Q.RY(1, theta=0.2, remapping=None),
+                            Q.CNOT(1, 2), Q.RZ(2, theta=0.3, remapping=None)], num_qubits=3).split(max_qubits=2),
+        "nested": Q.Circuit([c1, Q.RZ(0, theta=0.4, remapping=None), c2], num_qubits=3),
+        "qconv": Q.QConv(in_channels=2, out_channels=3),
+    }
+
+
+def state_dict_cases(qandle):
+    """Keys, shapes and dtypes of the reference's state_dicts and
+    named_parameters for state_dict_modules(): what a checkpoint saved with
+    qandle holds (qcircuit.py, ansaetze/, convolution.py)."""
+    import qandle.config as ref_config
+
+    out = {}
+    saved = ref_config.DEFAULT_MAPPING
+    ref_config.DEFAULT_MAPPING = _qw_none
+    try:
+        for name, mod in state_dict_modules(qandle).items():
+            sd = mod.state_dict()
+            rec = {"state_dict": [[k, list(v.shape), str(v.dtype)] for k, v in sd.items()],
+                   "parameters": [k for k, _ in mod.named_parameters()]}
+            out[name] = np.array(json.dumps(rec))
+    finally:
+        ref_config.DEFAULT_MAPPING = saved
+    return out
+
+
 def matrix_cases(qandle):
     """to_matrix() of built gates, ansaetze and a circuit (operators.py:60-69,
     ansaetze/ansatz.py:26-33, qcircuit.py:208-212): the inspection half of the
@@ -831,6 +880,7 @@ def main():
         "splitter": splitter_cases,
         "ansaetze": ansatz_cases,
         "matrices": matrix_cases,
+        "state_dicts": state_dict_cases,
     }
     only = [g for g in args.only.split(",") if g]
     for name, fn in groups.items():

@@ -2,10 +2,10 @@
 the reference (tests/golden/ansaetze.npz, made by running qandle's ansaetze):
 parameter count, decompositions, and the output state for fixed angles on a
 seeded input -- including the reference's order of the CNOT chain in the
-built TwoLocal / SU (applied last pair first).  States are computed from the
-built ansatz's `mods` (what both engines run) with the complex128 oracle;
-one case per kind is also lowered, planned and emulated as the fused engine
-runs it."""
+built TwoLocal / SU (applied last pair first).  States are computed from
+the built ansatz's `applied_gates` (what both engines run) with the
+complex128 oracle; one case per kind is also lowered, planned and emulated as
+the fused engine runs it."""
 import json
 import os
 
@@ -63,7 +63,7 @@ def test_structure_matches_reference(name):
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_state_matches_reference(name):
     circ, rec, n = _built(name)
-    got = oracle.run(_desc(circ.circuit.layers[0].mods, n), state=_psi(n))[0]
+    got = oracle.run(_desc(circ.circuit.layers[0].applied_gates, n), state=_psi(n))[0]
     ref = np.asarray(GOLDEN[name + "_state"]).reshape(-1)
     assert np.abs(got - ref).max() < 2e-6
 
@@ -75,7 +75,7 @@ def test_fused_plan_matches_reference(name):  # (the fused engine takes n >= 5)
     from tests.test_planner import _runtime
 
     circ, rec, n = _built(name)
-    for m in circ.circuit.layers[0].mods:
+    for m in circ.circuit.layers[0].applied_gates:
         if hasattr(m, "remapping"):
             m.remapping = q.remap.none
     lo = engine.lower(circ.circuit)
@@ -90,7 +90,7 @@ def test_twins_follow_module_moves():
     built = circ.circuit.layers[0]
     circ = circ.to(torch.float64)
     thetas = {id(p) for p in circ.parameters()}
-    for m in built.mods:
+    for m in built.applied_gates:
         if hasattr(m, "theta"):
             assert id(m.theta) in thetas and m.theta.dtype == torch.float64
 

@@ -54,3 +54,19 @@ def test_nested_width_mismatch_is_refused():
     big = q.Circuit(layers=[small, q.CNOT(2, 3)], num_qubits=6)
     with pytest.raises(ValueError):
         engine.lower(big.circuit)
+
+
+def test_per_gate_path_flattens_nested_circuits_and_ansaetze():
+    """The per-gate in-place path (inference without autograd) runs a nested
+    circuit's layers and an ansatz's applied gates in place, in order; the
+    flattened list equals the decomposed circuit's gates."""
+    from qandle_gb300 import plain
+
+    n = 6
+    c = _nested(n)
+    flat = plain._flat_layers(list(c.circuit.layers), n)
+    dec = list(c.decompose().circuit.layers)
+    assert [str(m) for m in flat] == [str(m) for m in dec]
+    small = q.Circuit(layers=[q.CNOT(0, 1)], num_qubits=2)
+    with pytest.raises(ValueError):
+        plain._flat_layers([small], n)
