@@ -156,7 +156,9 @@ class UnbuiltParametrizedOperator(UnbuiltOperator):
         self.remapping = remapping
 
     def __str__(self) -> str:
-        if self.name is not None:
+        # the reference's branches, kept as they are (operators.py:177-184):
+        # an unnamed gate prints its (absent) name, a named one its angle
+        if self.name is None:
             return f"{self.__class__.__name__}{self.qubit} ({self.name})"
         if self.theta is None:
             return f"{self.__class__.__name__}{self.qubit}"
@@ -171,6 +173,9 @@ class UnbuiltParametrizedOperator(UnbuiltOperator):
         if self.named:
             return qasm.QasmRepresentation(gate_str=self.__class__.__name__.lower(), qubit=self.qubit,
                                            qasm3_inputs=self.name)
+        if self.theta is None:
+            raise errors.UnbuiltGateError("This gate has no parameter. Set parameter or build or set name "
+                                          "before converting to OpenQASM2.")
         return qasm.QasmRepresentation(gate_str=self.__class__.__name__.lower(), qubit=self.qubit,
                                        gate_value=self.remapping(self.theta).item())
 
@@ -306,6 +311,16 @@ class SWAP(UnbuiltOperator):
         return qasm.QasmRepresentation(gate_str=f"swap q[{self.a}], q[{self.b}]")
 
 
+def _check_wires(num_qubits: int, *qubits: int) -> None:
+    """The reference forms the shift count n-1-q for every wire of a
+    permutation gate when it builds it (operators.py:546-555, :580-588,
+    :661-671); a wire q >= n makes the count negative and raises ValueError
+    there.  Built gates here raise the same error at the same point."""
+    for q in qubits:
+        if q >= num_qubits:
+            raise ValueError(f"negative shift count: qubit {q} of a gate on {num_qubits} qubits")
+
+
 def _perm_matrix(fn, num_qubits):
     dim = 2 ** num_qubits
     m = torch.zeros(dim, dim, dtype=torch.complex64)
@@ -323,6 +338,7 @@ class BuiltCNOT(BuiltOperator):
         self.c = control
         self.t = target
         self.num_qubits = num_qubits
+        _check_wires(num_qubits, control, target)
 
     def forward(self, state: torch.Tensor) -> torch.Tensor:
         return plain.Permutation.apply(state, self.num_qubits, "cnot", self.c, self.t)
@@ -347,6 +363,7 @@ class BuiltCZ(BuiltOperator):
         self.c = control
         self.t = target
         self.num_qubits = num_qubits
+        _check_wires(num_qubits, control, target)
 
     def forward(self, state: torch.Tensor) -> torch.Tensor:
         return plain.Permutation.apply(state, self.num_qubits, "cz", self.c, self.t)
@@ -372,6 +389,7 @@ class BuiltSWAP(BuiltOperator):
         self.a = a
         self.b = b
         self.num_qubits = num_qubits
+        _check_wires(num_qubits, a, b)
 
     def forward(self, state: torch.Tensor) -> torch.Tensor:
         return plain.Permutation.apply(state, self.num_qubits, "swap", self.a, self.b)
@@ -538,6 +556,10 @@ class BuiltReset(BuiltOperator):
 
     def __init__(self, qubit: int, num_qubits: int):
         super().__init__()
+        if not 0 <= qubit < num_qubits:
+            # the reference's subsystem reshape fails here (an einops
+            # RuntimeError, operators.py:608-610)
+            raise RuntimeError(f"Reset of qubit {qubit} in a circuit of {num_qubits} qubits")
         self.qubit = qubit
         self.num_qubits = num_qubits
 

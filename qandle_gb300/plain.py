@@ -214,6 +214,20 @@ def _amp_embed_torch(x: torch.Tensor, n: int, pad_with, normalize: bool) -> torc
     return torch.complex(x, torch.zeros_like(x))
 
 
+def amp_embed_length(num_features: int, n: int, pad_with) -> int:
+    """How many features of each row the amplitude embedding reads.  With a
+    pad value the reference pads to 2^n with torch's pad, whose negative
+    width cuts the features past 2^n (qandle/embeddings.py:50-62); without
+    one it passes the features through unchanged, which is a state only when
+    there are exactly 2^n of them, so other counts are refused here."""
+    dim = 1 << n
+    if pad_with is None:
+        if num_features != dim:
+            raise ValueError(f"{num_features} features for {n} qubits need pad_with (or exactly {dim})")
+        return dim
+    return min(num_features, dim)
+
+
 class AmpEmbed(torch.autograd.Function):
     """AmplitudeEmbedding: real features padded to 2^n and optionally
     normalised, as a complex64 state (CUDA kernel); the backward
@@ -227,14 +241,12 @@ class AmpEmbed(torch.autograd.Function):
         if not x2.is_cuda:
             raise RuntimeError("qandle_gb300 runs on CUDA tensors only; move the features with .to('cuda')")
         B, L = x2.shape
-        if L > (1 << n):
-            raise ValueError(f"{L} features do not fit {n} qubits")
-        if L != (1 << n) and pad_with is None:
-            raise ValueError(f"{L} features for {n} qubits need pad_with")
+        used = amp_embed_length(L, n, pad_with)
         out = torch.empty(B, 1 << n, dtype=torch.complex64, device=x2.device)
         lib = _lib.load()
-        scr = _scratch(lib.qg_amplitude_embedding_scratch_bytes(B, L) if normalize else 16, x2.device)
-        _lib.call("qg_amplitude_embedding", out.data_ptr(), x2.data_ptr(), L, B, n, L,
+        scr = _scratch(lib.qg_amplitude_embedding_scratch_bytes(B, used) if normalize else 16, x2.device)
+        # rows of x are L apart; the first `used` features of each are read
+        _lib.call("qg_amplitude_embedding", out.data_ptr(), x2.data_ptr(), L, B, n, used,
                   float(pad_with or 0.0), 1 if normalize else 0, scr.data_ptr(), scr.numel(), _lib.stream())
         ctx.save_for_backward(x2)
         ctx.meta = (n, pad_with, normalize, x.shape, x.dtype)

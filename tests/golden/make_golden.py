@@ -500,6 +500,27 @@ def amplitude_cases(qandle):
     return out
 
 
+def amplitude_crop_cases(qandle):
+    """AmplitudeEmbedding with more features than 2^n amplitudes and a
+    pad value: the reference pads with a negative width, which torch's pad
+    turns into cutting the features past 2^n (embeddings.py:50-62), then
+    normalises what is left."""
+    out = {}
+    gen = torch.Generator().manual_seed(23)
+    idx = 0
+    for n, length in ((1, 3), (2, 7), (3, 9), (4, 20)):
+        for normalize in (False, True):
+            x = torch.rand(3, length, generator=gen) + 0.1
+            op = qandle.AmplitudeEmbedding(name="x", qubits=list(range(n)), normalize=normalize,
+                                           pad_with=0.5).build(num_qubits=n)
+            out[f"c{idx}_x"] = x.numpy()
+            out[f"c{idx}_out"] = op(x=x).detach().numpy()
+            out[f"c{idx}_spec"] = np.array(json.dumps({"n": n, "normalize": normalize, "pad": 0.5}))
+            idx += 1
+    out["count"] = np.array(idx)
+    return out
+
+
 def qasm_circuits(qandle_mod):
     """Circuits whose OpenQASM export is compared as text (the random hash in
     embedding and measurement names is normalised)."""
@@ -876,6 +897,7 @@ def main():
         "circuits": circuit_cases,
         "special": special_cases,
         "amplitude": amplitude_cases,
+        "amplitude_crop": amplitude_crop_cases,
         "qasm": qasm_cases,
         "splitter": splitter_cases,
         "ansaetze": ansatz_cases,

@@ -212,3 +212,27 @@ def test_amplitude_formula_vs_reference():
         spec = json.loads(str(z[f"a{i}_spec"]))
         y = plain._amp_embed_torch(torch.tensor(z[f"a{i}_x"]), spec["n"], spec["pad"], spec["normalize"])
         assert np.abs(y.numpy() - z[f"a{i}_out"]).max() < 1e-6, spec
+
+
+def test_amplitude_crop_vs_reference():
+    """More features than amplitudes with a pad value: the reference cuts
+    the features past 2^n (torch's pad with a negative width) before
+    normalising.  The torch restatement equals the reference, and the
+    feature count the kernel is given is 2^n; without a pad value other
+    counts than 2^n are refused."""
+    import torch
+
+    from qandle_gb300 import plain
+
+    z = golden_io.load("amplitude_crop")
+    for i in range(int(z["count"])):
+        spec = json.loads(str(z[f"c{i}_spec"]))
+        x = torch.tensor(z[f"c{i}_x"])
+        y = plain._amp_embed_torch(x, spec["n"], spec["pad"], spec["normalize"])
+        assert np.abs(y.numpy() - z[f"c{i}_out"]).max() < 1e-6, spec
+        assert plain.amp_embed_length(x.shape[-1], spec["n"], spec["pad"]) == 1 << spec["n"]
+    assert plain.amp_embed_length(3, 3, 0.0) == 3
+    assert plain.amp_embed_length(8, 3, None) == 8
+    for length in (3, 9):
+        with pytest.raises(ValueError):
+            plain.amp_embed_length(length, 3, None)
