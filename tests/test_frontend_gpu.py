@@ -6,7 +6,11 @@
   path), equals its decomposition;
 * TwoLocal, SU and the budget ansatz, on the fused engine (6 qubits) and the
   per-gate kernels (4 qubits), give the reference's states
-  (tests/golden/ansaetze.npz).
+  (tests/golden/ansaetze.npz);
+* split circuits, moved to the GPU (their gates on the parent qubits share
+  the subcircuits' parameters), give the reference's split states
+  (tests/golden/splitter.npz), on the fused engine and, at 3 qubits, the
+  per-gate kernels.
 """
 import json
 
@@ -70,3 +74,21 @@ def test_ansatz_state_matches_reference(name):
             st = circ(ps)
         err = float(np.abs(st.detach().cpu().numpy().reshape(-1) - ref).max())
         assert err < 2e-6, (grad, err)
+
+
+@pytest.mark.parametrize("name", ["cnot10_k5", "sel6_k3", "random1_k3", "random2_k3", "dummy_k2"])
+def test_split_circuit_state_matches_reference(name):
+    z = golden_io.load("splitter")
+    gates, n, k, via = mg.split_circuits()[name]
+    split = mg.build_split(q, gates, n, k, via)
+    for la in split.circuit.layers:  # the fixture's states use the identity remapping
+        if hasattr(la, "remapping"):
+            la.remapping = q.remap.none
+    split = split.to(DEV)
+    psi, named = mg.split_inputs(n, gates)
+    kw = {nm: torch.tensor(v, dtype=torch.float32, device=DEV) for nm, v in named.items()}
+    with torch.no_grad():
+        st = split(torch.tensor(psi, dtype=torch.cfloat, device=DEV), **kw)
+    ref = np.asarray(z[name + "_state"]).reshape(-1)
+    err = float(np.abs(st.cpu().numpy().reshape(-1) - ref).max())
+    assert err < 2e-6, err
