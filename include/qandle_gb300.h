@@ -311,6 +311,9 @@ int qg_program_prepare(const qg_program* prog, const void* dev_table, void* work
  * independent (distinct states) and planned with the same tile_bits. */
 int qg_jobs_run_pass(const qg_job* jobs, int njobs, void* stream);
 
+int qg_program_finish(const qg_program* prog, const void* dev_table, void* workspace,
+                      int64_t workspace_bytes, int64_t batch, float* out, void* stream);
+
 /* Status word of a program workspace after the work queued on `stream`: QG_OK,
  * or QG_ETIMEOUT when a pass kernel's bounded wait on a producer / compute
  * hand-off ran out (its results are then invalid).  Synchronises the stream.
@@ -322,8 +325,6 @@ int qg_workspace_status(const void* workspace, void* stream);
  * the wait ran out and reported it (the expected outcome); the context stays
  * usable.  (No reference counterpart.) */
 int qg_selftest_wait_timeout(int64_t limit_ns, void* stream);
-int qg_program_finish(const qg_program* prog, const void* dev_table, void* workspace,
-                      int64_t workspace_bytes, int64_t batch, float* out, void* stream);
 
 /* Adjoint backward.  state: the forward's final state (overwritten: it is
  * un-computed gate by gate); lam: [B][2^n] buffer.  grad_out is the upstream
