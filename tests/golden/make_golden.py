@@ -533,15 +533,32 @@ def qasm_circuits(qandle_mod):
                    Q.CNOT(2, 0), Q.MeasureProbability()], 3),
         "special": ([Q.Reset(qubit=1), Q.Controlled(0, Q.RY(1, theta=0.5, remapping=None)),
                      Q.Invert(Q.RX(2, theta=0.75, remapping=None).build(num_qubits=3))], 3),
+        "sel": ([Q.StronglyEntanglingLayer(qubits=[0, 1, 2], depth=2, remapping=None,
+                                           q_params=torch.arange(18, dtype=torch.float32).reshape(2, 3, 3) / 10)],
+                3),
+        "twolocal": ([Q.TwoLocal(qubits=[0, 1, 2], depth=2, remapping=None, q_params=torch.full((2, 3), 0.3))], 3),
+        "u_swap": ([Q.U(1, matrix=torch.tensor([[0.6, 0.8], [0.8, -0.6]], dtype=torch.cfloat)), Q.SWAP(0, 2),
+                    Q.CNOT(0, 1)], 3),
+        "nested": ([Q.Circuit([Q.RX(0, theta=0.1, remapping=None), Q.CNOT(0, 1)], num_qubits=3),
+                    Q.RZ(2, theta=0.4, remapping=None)], 3),
     }
 
 
 def qasm_cases(qandle):
+    """OpenQASM 2 and 3 text of qasm_circuits() (the built TwoLocal's
+    rotations take the default remapping, set to the identity here)."""
+    import qandle.config as ref_config
+
     out = {}
-    for name, (layers, n) in qasm_circuits(qandle).items():
-        circ = qandle.Circuit(layers, num_qubits=n)
-        out[f"{name}_qasm2"] = np.array(circ.to_openqasm2())
-        out[f"{name}_qasm3"] = np.array(circ.to_openqasm3())
+    saved = ref_config.DEFAULT_MAPPING
+    ref_config.DEFAULT_MAPPING = _qw_none
+    try:
+        for name, (layers, n) in qasm_circuits(qandle).items():
+            circ = qandle.Circuit(layers, num_qubits=n)
+            out[f"{name}_qasm2"] = np.array(circ.to_openqasm2())
+            out[f"{name}_qasm3"] = np.array(circ.to_openqasm3())
+    finally:
+        ref_config.DEFAULT_MAPPING = saved
     return out
 
 

@@ -8,37 +8,39 @@ import pytest
 
 import qandle_gb300 as q
 from tests import golden_io
+from tests.golden import make_golden as mg
 
 
 def _norm(text: str) -> str:
     return re.sub(r"_-?\d{5,}_", "_H_", text)
 
 
-def _circuits():
-    # the same constructions as tests/golden/make_golden.py:qasm_circuits
-    return {
-        "rot_fixed": ([q.RX(0, theta=0.25, remapping=None), q.RY(1, theta=-1.5, remapping=None),
-                       q.RZ(2, theta=3.0, remapping=None), q.CNOT(0, 2), q.CZ(1, 2), q.MeasureProbability()], 3),
-        "named": ([q.AngleEmbedding(name="x", qubits=[0, 1, 2], rotation="ry"), q.RZ(1, name="up", remapping=None),
-                   q.CNOT(2, 0), q.MeasureProbability()], 3),
-        "special": ([q.Reset(qubit=1), q.Controlled(0, q.RY(1, theta=0.5, remapping=None)),
-                     q.Invert(q.RX(2, theta=0.75, remapping=None).build(num_qubits=3))], 3),
-    }
+def _circuit(name):
+    """Circuit `name` of tests/golden/make_golden.py:qasm_circuits, built with
+    this package while the default remapping is the identity (the built
+    TwoLocal's rotations take the default, as when the fixtures were made)."""
+    saved = q.config.DEFAULT_MAPPING
+    q.config.DEFAULT_MAPPING = q.remap.none
+    try:
+        layers, n = mg.qasm_circuits(q)[name]
+        return q.Circuit(layers, num_qubits=n)
+    finally:
+        q.config.DEFAULT_MAPPING = saved
 
 
-@pytest.mark.parametrize("name", ["rot_fixed", "named", "special"])
+@pytest.mark.parametrize("name", ["rot_fixed", "named", "special", "sel", "twolocal", "u_swap", "nested"])
 def test_export_matches_reference(name):
     z = golden_io.load("qasm")
-    layers, n = _circuits()[name]
-    circ = q.Circuit(layers, num_qubits=n)
+    circ = _circuit(name)
     assert _norm(circ.to_openqasm2()) == _norm(str(z[f"{name}_qasm2"]))
     assert _norm(circ.to_openqasm3()) == _norm(str(z[f"{name}_qasm3"]))
 
 
 @pytest.mark.parametrize("name", ["rot_fixed", "named"])
 def test_ingest_round_trip(name):
-    layers, n = _circuits()[name]
-    text = q.Circuit(layers, num_qubits=n).to_openqasm2()
+    circ = _circuit(name)
+    n = circ.num_qubits
+    text = circ.to_openqasm2()
     again = q.Circuit.from_qasm(text)
     assert again.num_qubits == n
     # the embedding comes back as its named rotations
