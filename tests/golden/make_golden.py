@@ -638,6 +638,22 @@ def split_circuits() -> dict:
         gates = [gates[i] for i in perm]
         k = int(rng.integers(2, 6))
         cases[f"random{seed}_k{k}"] = (gates, n, k, "method" if seed % 2 == 0 else "constructor")
+    # a wider random sweep: 3..8 qubits, 5..60 gates, any k >= 2 that splits
+    for seed in range(40):
+        rng = np.random.default_rng(2000 + seed)
+        n = int(rng.integers(3, 9))
+        gates = [("cnot", q, q + 1) for q in range(n - 1)]
+        for _ in range(int(rng.integers(5, 60))):
+            if rng.random() < 0.5:
+                a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+                gates.append(("cnot", a, b))
+            else:
+                axis = ("rx", "ry", "rz")[int(rng.integers(3))]
+                gates.append((axis, int(rng.integers(n)), round(float(rng.uniform(-3, 3)), 4), None))
+        perm = rng.permutation(len(gates))
+        gates = [gates[i] for i in perm]
+        k = int(rng.integers(2, n))
+        cases[f"sweep{seed}_k{k}"] = (gates, n, k, "method" if seed % 2 else "constructor")
     return cases
 
 
@@ -698,7 +714,32 @@ def ansatz_circuits() -> dict:
         "twolocal_6": ("twolocal", 6, dict(qubits=[0, 1, 2, 3, 4, 5], depth=2)),
         "su_6": ("su", 6, dict(qubits=[0, 1, 2, 3, 4, 5], reps=2, rotations=["rx", "ry"])),
         "budget_6": ("budget", 6, dict(param_budget=20, control_gate_spacing=2)),
+        **_ansatz_sweep(),
     }
+
+
+def _ansatz_sweep() -> dict:
+    """Random TwoLocal / SU / budget configurations on 2..6 qubits, qubit
+    subsets in ascending order."""
+    out = {}
+    for seed in range(24):
+        rng = np.random.default_rng(500 + seed)
+        n = int(rng.integers(3, 7))
+        kind = ("twolocal", "su", "budget")[seed % 3]
+        sub = sorted(int(v) for v in rng.choice(n, int(rng.integers(2, n + 1)), replace=False))
+        if kind == "twolocal":
+            args = dict(qubits=sub, depth=int(rng.integers(1, 4)))
+        elif kind == "su":
+            rots = [["rx"], ["ry"], ["rz"], ["rx", "ry"], ["rz", "rx", "ry"]][int(rng.integers(5))]
+            args = dict(qubits=sub, reps=int(rng.integers(0, 3)), rotations=rots)
+        else:
+            args = dict(qubits=sub, param_budget=int(rng.integers(1, 12)),
+                        control_gate_spacing=int(rng.integers(1, 4)),
+                        rotations=[["rz", "ry"], ["ry"], ["rx", "rz", "ry"]][int(rng.integers(3))])
+            if rng.random() < 0.3:
+                args["control"] = "cz"
+        out[f"sweep_{kind}_{seed}"] = (kind, n, args)
+    return out
 
 
 def build_ansatz(Q, kind: str, n: int, args: dict):
