@@ -175,6 +175,49 @@ def gate_cases(qandle):
     return out
 
 
+def random_circuit_descs() -> dict:
+    """name -> description of random circuits over every gate kind of the
+    path (fixed and named rotations, U, CNOT, CZ, SWAP) on 3..8 qubits, batch
+    3, state output, and the seeded input state [3, 2^n]."""
+    out = {}
+    for seed in range(30):
+        rng = np.random.default_rng(3000 + seed)
+        n = int(rng.integers(3, 9))
+        B = 3
+        gates, inputs = [], {}
+        for i in range(int(rng.integers(10, 60))):
+            kind = ("rx", "ry", "rz", "u", "cnot", "cz", "swap")[int(rng.integers(7))]
+            if kind in ("rx", "ry", "rz"):
+                q = int(rng.integers(n))
+                if rng.random() < 0.2:
+                    name = f"a{i}"
+                    inputs[name] = rng.uniform(-3, 3, size=B).astype(np.float32)
+                    gates.append((kind, q, None, name))
+                else:
+                    gates.append((kind, q, float(np.float32(rng.uniform(-3, 3))), None))
+            elif kind == "u":
+                a, b, c = (float(v) for v in rng.uniform(0, 2 * np.pi, 3))
+                gates.append(("u", int(rng.integers(n)), workloads.u3_row_matrix(a, b, c).astype(np.complex64)))
+            else:
+                a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+                gates.append((kind, a, b))
+        psi = rng.normal(size=(B, 1 << n)) + 1j * rng.normal(size=(B, 1 << n))
+        psi = (psi / np.linalg.norm(psi, axis=1, keepdims=True)).astype(np.complex64)
+        out[f"rand{seed}"] = ({"n": n, "batch": B, "gates": gates, "inputs": inputs, "measure": "state"}, psi)
+    return out
+
+
+def random_circuit_cases(qandle):
+    """The reference's output states for random_circuit_descs()."""
+    out = {}
+    for name, (desc, psi) in random_circuit_descs().items():
+        circ = to_reference(qandle, desc)
+        with torch.no_grad():
+            st = circ(torch.tensor(psi), **kwargs_of(desc))
+        out[f"{name}_out"] = st.numpy()
+    return out
+
+
 def embedding_cases(qandle):
     """test_embeddings.py:56-153 (x3, y4, z5, each unbatched and batched),
     plus a qubit subset and a repeated qubit."""
@@ -953,6 +996,7 @@ def main():
         "sel": sel_cases,
         "reupload": reupload_cases,
         "circuits": circuit_cases,
+        "random_circuits": random_circuit_cases,
         "special": special_cases,
         "amplitude": amplitude_cases,
         "amplitude_crop": amplitude_crop_cases,

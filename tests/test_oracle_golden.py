@@ -236,3 +236,15 @@ def test_amplitude_crop_vs_reference():
     for length in (3, 9):
         with pytest.raises(ValueError):
             plain.amp_embed_length(length, 3, None)
+
+
+def test_random_circuits_golden():
+    """30 random circuits over every gate kind of the path (fixed and named
+    rotations, U, CNOT, CZ, SWAP; 3..8 qubits, batch 3, seeded input states):
+    the oracle equals the reference's output states."""
+    from tests.golden import make_golden as mg
+
+    z = golden_io.load("random_circuits")
+    for name, (desc, psi) in mg.random_circuit_descs().items():
+        out = oracle.run(desc, state=psi, batch=desc["batch"])
+        assert np.abs(out - z[f"{name}_out"]).max() < TOL, name

@@ -210,3 +210,27 @@ def test_held_diagonals_random_circuits_match_oracle(seed, oi):
     params, named, umats, embed = _runtime(lo, desc, 2)
     st, _ = emu.run_forward(prog, desc["n"], 2, params, named, umats, embed=embed)
     assert np.abs(st - oracle.run(desc)).max() < 1e-10
+
+
+@pytest.mark.parametrize("opts", [dict(tile_bits=13, low_bits=6), dict(tile_bits=11, low_bits=4, max_high=2)])
+def test_random_circuits_plan_matches_reference(opts):
+    """The reference's output states for 30 random circuits over every gate
+    kind of the path (tests/golden/random_circuits.npz): the front-end
+    circuit, lowered, planned and emulated as the fused engine runs it,
+    gives them for every circuit of 5 qubits or more."""
+    from tests import golden_io
+    from tests.golden import make_golden as mg
+
+    z = golden_io.load("random_circuits")
+    ran = 0
+    for name, (desc, psi) in mg.random_circuit_descs().items():
+        n, B = desc["n"], desc["batch"]
+        if n < 5:
+            continue
+        lo = engine.lower(workloads.build_circuit(desc).circuit)
+        prog = engine.Program(lo, "state", keep_state=False, **opts)
+        params, named, umats, embed = _runtime(lo, desc, B)
+        st, _ = emu.run_forward(prog, n, B, params, named, umats, state=psi.astype(complex), embed=embed)
+        assert np.abs(st - z[f"{name}_out"]).max() < 2e-6, name
+        ran += 1
+    assert ran >= 15
