@@ -218,6 +218,31 @@ def random_circuit_cases(qandle):
     return out
 
 
+def random_grad_cases(qandle):
+    """torch-autograd gradients of the reference for the first 12 random
+    circuits with joint probabilities out and loss sum(W * probs), W seeded
+    [3, 2^n]: d loss / d theta of the unnamed rotations (gate order) and
+    d loss / d named input."""
+    out = {}
+    for i, (name, (desc, psi)) in enumerate(random_circuit_descs().items()):
+        if i >= 12:
+            break
+        d = dict(desc, measure="probs")
+        circ = to_reference(qandle, d)
+        kw = {k: v.clone().requires_grad_(True) for k, v in kwargs_of(d).items()}
+        w = torch.tensor(np.random.default_rng(4000 + i).uniform(-1, 1, size=(d["batch"], 1 << d["n"])),
+                         dtype=torch.float32)
+        probs = circ(torch.tensor(psi), **kw)
+        (probs * w).sum().backward()
+        thetas = ref_thetas(qandle, circ)
+        out[f"{name}_w"] = w.numpy()
+        out[f"{name}_dtheta"] = np.array([float(t.grad) if t.grad is not None else 0.0 for t in thetas],
+                                         dtype=np.float64)
+        for k, v in kw.items():
+            out[f"{name}_dnamed_{k}"] = v.grad.numpy()
+    return out
+
+
 def embedding_cases(qandle):
     """test_embeddings.py:56-153 (x3, y4, z5, each unbatched and batched),
     plus a qubit subset and a repeated qubit."""
@@ -997,6 +1022,7 @@ def main():
         "reupload": reupload_cases,
         "circuits": circuit_cases,
         "random_circuits": random_circuit_cases,
+        "random_grads": random_grad_cases,
         "special": special_cases,
         "amplitude": amplitude_cases,
         "amplitude_crop": amplitude_crop_cases,

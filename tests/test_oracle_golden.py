@@ -248,3 +248,24 @@ def test_random_circuits_golden():
     for name, (desc, psi) in mg.random_circuit_descs().items():
         out = oracle.run(desc, state=psi, batch=desc["batch"])
         assert np.abs(out - z[f"{name}_out"]).max() < TOL, name
+
+
+def test_random_circuit_gradients_vs_reference_autograd():
+    """The oracle's adjoint gradients (unnamed angles, named inputs) equal
+    torch autograd through the reference for 12 random circuits over every
+    gate kind, loss sum(W * joint probabilities)."""
+    from tests.golden import make_golden as mg
+
+    z = golden_io.load("random_grads")
+    checked = 0
+    for name, (desc, psi) in mg.random_circuit_descs().items():
+        if f"{name}_w" not in z.files:
+            continue
+        d = dict(desc, measure="probs")
+        dth, dnamed, _ = oracle.adjoint(d, z[f"{name}_w"].astype(np.float64), "probs", state=psi,
+                                        batch=d["batch"])
+        assert np.abs(dth - z[f"{name}_dtheta"]).max() < 1e-5, name
+        for k in d["inputs"]:
+            assert np.abs(dnamed[k] - z[f"{name}_dnamed_{k}"]).max() < 1e-5, (name, k)
+        checked += 1
+    assert checked == 12

@@ -234,3 +234,35 @@ def test_random_circuits_plan_matches_reference(opts):
         assert np.abs(st - z[f"{name}_out"]).max() < 2e-6, name
         ran += 1
     assert ran >= 15
+
+
+@pytest.mark.parametrize("rb", [5, 4])
+def test_random_circuits_backward_plan_matches_reference_autograd(rb):
+    """The adjoint plan, emulated, gives torch autograd's gradients through
+    the reference (tests/golden/random_grads.npz: loss sum(W * joint
+    probabilities)) for the random circuits of 5 qubits or more, with a
+    checkpoint in the middle."""
+    from tests import golden_io
+    from tests.golden import make_golden as mg
+
+    z = golden_io.load("random_grads")
+    ran = 0
+    for name, (desc, psi) in mg.random_circuit_descs().items():
+        if f"{name}_w" not in z.files or desc["n"] < 5:
+            continue
+        d = dict(desc, measure="probs")
+        n, B = d["n"], d["batch"]
+        lo = engine.lower(workloads.build_circuit(d).circuit)
+        prog = engine.Program(lo, "probs", keep_state=True, segments=2, tile_bits=13, low_bits=5, reg_bits=rb)
+        params, named, umats, embed = _runtime(lo, d, B)
+        st, ck = emu.run_forward(prog, n, B, params, named, umats, state=psi.astype(complex), embed=embed)
+        lam = z[f"{name}_w"].astype(np.float64) * st  # dL/dpsi* for L = sum(W |psi|^2)
+        dp, dn, _ = emu.run_backward(prog, n, B, params, named, umats, st, lam, ck, prog.grad_targets())
+        assert np.abs(dp - z[f"{name}_dtheta"]).max() < 1e-5, name
+        got = {}
+        for c, (nm, j) in enumerate(lo.named_cols):
+            got[nm] = got.get(nm, 0) + dn[:, c]
+        for nm, v in got.items():
+            assert np.abs(v - z[f"{name}_dnamed_{nm}"]).max() < 1e-5, (name, nm)
+        ran += 1
+    assert ran >= 5
