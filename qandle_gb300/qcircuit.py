@@ -53,6 +53,14 @@ class Circuit(torch.nn.Module):
         self._executor = None
         self._engine_options = engine_options
 
+    def __getstate__(self):
+        # the fused executor holds library handles, device tables and a lock;
+        # a copy (copy.deepcopy, pickling, torch.save of the module) leaves it
+        # out and plans again at its first call
+        state = self.__dict__.copy()
+        state["_executor"] = None
+        return state
+
     def forward(self, state=None, **kwargs):
         if self.engine == "plain":
             return self.circuit.forward(state, **kwargs)

@@ -70,3 +70,24 @@ def test_per_gate_path_flattens_nested_circuits_and_ansaetze():
     small = q.Circuit(layers=[q.CNOT(0, 1)], num_qubits=2)
     with pytest.raises(ValueError):
         plain._flat_layers([small], n)
+
+
+def test_circuit_copies_after_planning():
+    """copy.deepcopy, pickling and torch.save of a circuit whose fused
+    executor has planned a program leave the executor out (it holds library
+    handles); the copy has its own parameters and plans again when called."""
+    import copy
+    import io
+    import pickle
+
+    c = q.Circuit([q.RX(i, theta=0.1 * i, remapping=None) for i in range(6)] + [q.CNOT(0, 1)], num_qubits=6)
+    c._executor = engine.FusedExecutor(c.circuit)
+    c._executor.program(False)  # planned on the host
+    d = copy.deepcopy(c)
+    assert d._executor is None and c._executor is not None
+    assert [p.detach().item() for p in d.parameters()] == [p.detach().item() for p in c.parameters()]
+    assert all(a is not b for a, b in zip(d.parameters(), c.parameters()))
+    e = pickle.loads(pickle.dumps(c))
+    assert e._executor is None and len(list(e.parameters())) == 6
+    buf = io.BytesIO()
+    torch.save(c, buf)

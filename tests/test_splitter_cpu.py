@@ -165,3 +165,14 @@ def test_module_moves_reach_the_twins():
                 seen_u = True
                 assert tw._m.dtype == la._m.dtype
     assert seen_u
+
+
+def test_deepcopy_keeps_twins_on_the_copied_parameters():
+    import copy
+
+    gates, n, k, via = CASES["sel6_k3"]
+    d = copy.deepcopy(mg.build_split(q, gates, n, k, via))
+    params = {id(p) for p in d.parameters()}
+    twins = [la for la in d.circuit.layers if hasattr(la, "theta")]
+    assert len(params) == len(twins) == 36
+    assert all(id(t.theta) in params for t in twins)
