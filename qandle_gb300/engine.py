@@ -19,6 +19,7 @@ import warnings
 
 import numpy as np
 import torch
+from torch.autograd.function import once_differentiable
 
 from . import _lib
 
@@ -473,6 +474,7 @@ class _FusedRun(torch.autograd.Function):
         return ex.run_forward(ctx, prog, state_in, params, named, umats, batch, zero_init)
 
     @staticmethod
+    @once_differentiable
     def backward(ctx, gout):
         return (None,) + ctx.ex.run_backward(ctx, gout)
 

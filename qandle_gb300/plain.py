@@ -11,6 +11,7 @@ States are viewed as [B, 2^n]; an unbatched [2^n] state is B = 1.
 from __future__ import annotations
 
 import torch
+from torch.autograd.function import once_differentiable
 
 from . import _lib
 
@@ -52,6 +53,7 @@ class Rotation(torch.autograd.Function):
         return out
 
     @staticmethod
+    @once_differentiable
     def backward(ctx, g):
         out, a = ctx.saved_tensors
         n, qubit, axis, per_sample, ashape, sshape, B = ctx.meta
@@ -89,6 +91,7 @@ class Matrix(torch.autograd.Function):
         return out.reshape(state.shape)
 
     @staticmethod
+    @once_differentiable
     def backward(ctx, g):
         (m,) = ctx.saved_tensors
         n, qubit, sshape = ctx.meta
@@ -123,6 +126,7 @@ class ControlledRotation(torch.autograd.Function):
         return out
 
     @staticmethod
+    @once_differentiable
     def backward(ctx, g):
         out, a = ctx.saved_tensors
         n, control, qubit, axis, per_sample, ashape, sshape, B = ctx.meta
@@ -160,6 +164,7 @@ class ControlledMatrix(torch.autograd.Function):
         return out.reshape(state.shape)
 
     @staticmethod
+    @once_differentiable
     def backward(ctx, g):
         (m,) = ctx.saved_tensors
         n, control, qubit, sshape = ctx.meta
@@ -193,6 +198,7 @@ class Reset(torch.autograd.Function):
         return out.reshape(state.shape)
 
     @staticmethod
+    @once_differentiable
     def backward(ctx, g):
         (st,) = ctx.saved_tensors
         n, qubit, sshape = ctx.meta
@@ -253,6 +259,7 @@ class AmpEmbed(torch.autograd.Function):
         return out.reshape(*lead, 1 << n)
 
     @staticmethod
+    @once_differentiable
     def backward(ctx, g):
         (x2,) = ctx.saved_tensors
         n, pad_with, normalize, xshape, xdtype = ctx.meta
@@ -280,6 +287,7 @@ class Permutation(torch.autograd.Function):
         return out.reshape(state.shape)
 
     @staticmethod
+    @once_differentiable
     def backward(ctx, g):
         n, kind, qa, qb, sshape = ctx.meta
         gin = g.reshape(-1, 1 << n).contiguous().clone()
@@ -308,6 +316,7 @@ class AngleEmbed(torch.autograd.Function):
         return out
 
     @staticmethod
+    @once_differentiable
     def backward(ctx, g):
         (out,) = ctx.saved_tensors
         n, qubits, axis, xshape, B = ctx.meta
@@ -340,6 +349,7 @@ class MeasureP0(torch.autograd.Function):
         return out
 
     @staticmethod
+    @once_differentiable
     def backward(ctx, g):
         (st,) = ctx.saved_tensors
         n, sshape = ctx.meta
@@ -363,6 +373,7 @@ class Probs(torch.autograd.Function):
         return out
 
     @staticmethod
+    @once_differentiable
     def backward(ctx, g):
         (st,) = ctx.saved_tensors
         g = g.to(torch.float32).contiguous()

@@ -74,3 +74,17 @@ def test_constructor_assertions():
                  lambda: q.RX(1.0, theta=0.1)):
         with pytest.raises(AssertionError):
             make()
+
+
+def test_custom_backwards_refuse_double_differentiation():
+    """The kernels' backward passes are first-order only; each is marked
+    once-differentiable, so create_graph=True followed by a second backward
+    raises instead of returning silently wrong higher-order gradients."""
+    from qandle_gb300 import engine, plain
+
+    fns = [engine._FusedRun] + [v for v in vars(plain).values()
+                                if isinstance(v, type) and issubclass(v, torch.autograd.Function)
+                                and v is not torch.autograd.Function]
+    assert len(fns) >= 11
+    for f in fns:
+        assert hasattr(f.backward, "__wrapped__"), f.__name__
