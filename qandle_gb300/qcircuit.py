@@ -143,7 +143,7 @@ class Circuit(torch.nn.Module):
 
     def decompose(self):
         return Circuit(layers=[], num_qubits=self.num_qubits, circuit=self.circuit.decompose(),
-                       engine=self.engine)
+                       engine=self.engine, **self._engine_options)
 
     def split(self, max_qubits):
         """The circuit cut into subcircuits of at most `max_qubits` qubits

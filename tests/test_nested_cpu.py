@@ -91,3 +91,10 @@ def test_circuit_copies_after_planning():
     assert e._executor is None and len(list(e.parameters())) == 6
     buf = io.BytesIO()
     torch.save(c, buf)
+
+
+def test_decompose_and_split_keep_engine_options():
+    c = q.Circuit([q.RX(0, theta=0.1, remapping=None), q.CNOT(0, 1), q.CNOT(1, 2)], num_qubits=3,
+                  engine="plain", tile_bits=12)
+    for d in (c.decompose(), c.split(max_qubits=2)):
+        assert d.engine == "plain" and d._engine_options == {"tile_bits": 12}
