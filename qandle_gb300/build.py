@@ -58,7 +58,11 @@ def _write_jit_headers() -> str:
         lines.append('R"QGJIT(' + text + ')QGJIT",')
     lines += ["};", "}  // namespace qg", ""]
     body = "\n".join(lines)
-    if not os.path.exists(out) or open(out).read() != body:
+    old = None
+    if os.path.exists(out):
+        with open(out) as f:
+            old = f.read()
+    if old != body:
         with open(out, "w") as f:
             f.write(body)
     return out

@@ -13,7 +13,8 @@ HEADERS = [os.path.join(build.INCLUDE, f) for f in os.listdir(build.INCLUDE) if 
 def declared_symbols():
     names = set()
     for h in HEADERS:
-        text = open(h).read()
+        with open(h) as f:
+            text = f.read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         names.update(re.findall(r"\b(qg_\w+)\s*\(", text))
     return sorted(names)

@@ -88,7 +88,7 @@ def test_fused_plan_matches_reference(name):  # (the fused engine takes n >= 5)
 def test_twins_follow_module_moves():
     circ, _, _ = _built("su_full")
     built = circ.circuit.layers[0]
-    circ = circ.to(torch.float64)
+    circ = circ.double()
     thetas = {id(p) for p in circ.parameters()}
     for m in built.applied_gates:
         if hasattr(m, "theta"):

@@ -155,7 +155,7 @@ def test_module_moves_reach_the_twins():
     gates, n, k, via = CASES["dummy_k2"]
     layers = mg.split_layers(q, gates) + [q.U(1, matrix=torch.eye(2, dtype=torch.complex64)), q.CNOT(1, 0)]
     split = q.Circuit(layers, num_qubits=n).split(max_qubits=2)
-    split = split.to(torch.float64)
+    split = split.double()
     seen_u = False
     for sc in split.circuit.subcircuits:
         for la, tw in zip(sc.layers, sc.twins):

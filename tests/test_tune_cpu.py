@@ -13,6 +13,11 @@ def _circuit(desc):
     return workloads.build_circuit(desc, engine="fused")
 
 
+def _load(path):
+    with open(path) as f:
+        return json.load(f)
+
+
 def test_structure_key_ignores_angles_only():
     a = workloads.sel_reupload(n=8, batch=4, layers=2, reupload_every=1)
     b = workloads.sel_reupload(n=8, batch=4, layers=2, reupload_every=1)
@@ -39,12 +44,12 @@ def test_autotune_picks_fastest_and_caches(tmp_path):
     res = tune.autotune(circ, 4, "cpu", candidates=cands, cache_path=cache, timer=timer)
     assert res["options"] == dict(tile_bits=12, low_bits=6) and res["ms"] == 1.5 and not res["cached"]
     assert len(res["timings"]) == 2 and len(calls) == 3
-    stored = json.load(open(cache))
+    stored = _load(cache)
     assert len(stored) == 1
     again = tune.autotune(circ, 4, "cpu", candidates=cands, cache_path=cache, timer=timer)
     assert again["cached"] and again["options"] == res["options"] and len(calls) == 3
     other = tune.autotune(circ, 8, "cpu", candidates=cands, cache_path=cache, timer=timer)
-    assert not other["cached"] and len(json.load(open(cache))) == 2
+    assert not other["cached"] and len(_load(cache)) == 2
 
 
 def test_autotune_needs_a_runnable_candidate(tmp_path):
