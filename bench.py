@@ -9,27 +9,41 @@ the inputs before layers 0 and 5, <Z> per qubit.  Metric: amplitude-updates/s
 = gates x batch x 2^n per forward / time (860 gates, the embedding counted as
 20 rotations).
 
-Also on the line: the plain per-gate form on the same workload, the forward
-replayed from one CUDA graph, the adjoint backward (16 qubits x batch 1024,
-MSE(<Z>, targets)) against the per-gate adjoint, the fusion-width sweep
-(--sweep), the HBM roofline of the pass kernel from CUDA events around every
-pass launch, the end-to-end time through the public API with host buffers,
-SM clocks sampled during the timed region, and the CPU oracle timed on the
-host cores.
+Also on the line:
+* roofline of the pass kernel from CUDA events around every pass launch:
+  HBM (algorithmic bytes) and FP32 (counted FMAs against the FP32 peak that
+  the library's own probe kernel measures), and per-pass figures;
+* the end-to-end time through the public API (Circuit.__call__, which
+  replays a captured CUDA graph) with pinned host inputs and results;
+* the forward replayed from one CUDA graph, the plain per-gate form;
+* config 1 (8 qubits x 64, plain method) on the GPU, and the reference's own
+  torch path on the host cores at that size and at 10 qubits;
+* the adjoint (16 qubits x 1024, MSE(<Z>, targets)) against the per-gate
+  adjoint, with its backward passes' roofline;
+* the deep 28-qubit circuit against the per-gate form;
+* the fusion-width sweep k = 1..6, and the autotuner's choice of tile shape,
+  k and qubit-remap schedule;
+* the serving loop against one per-gate run per request, live, at two
+  Poisson rates;
+* the error against the complex128 oracle for every config;
+* SM clocks sampled during the timed region; the oracle timed on the host.
 
 `--impl reference` times the CPU implementation of the same path (the
-complex128 oracle, all host threads) on a bounded sample per step.
+complex128 oracle, all host threads) on a bounded sample per step, and the
+reference's own torch path at the sizes it can run.
 Under torchrun every rank runs its own batch (weak scaling, no collective on
 the data path); rank 0 prints.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
 import sys
 import tempfile
+import threading
 import time
 
 import numpy as np
@@ -47,17 +61,23 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--sweep", action="store_true", help="fusion-width sweep k = 1..7")
     ap.add_argument("--no-extras", action="store_true", help="headline only")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the fusion-width sweep")
+    ap.add_argument("--no-autotune", action="store_true", help="skip the autotuner record")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving runs")
     ap.add_argument("--cpu-samples", type=int, default=16, help="samples in the CPU baseline")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines (profiling runs)")
     ap.add_argument("--tile-bits", type=int, default=13)
     ap.add_argument("--low-bits", type=int, default=6)
     ap.add_argument("--k", type=int, default=0, help="max strided qubits per pass (0 = tile limit)")
     ap.add_argument("--reg-bits", type=int, default=5, help="amplitudes per thread = 2^reg_bits")
-    ap.add_argument("--serving-requests", type=int, default=48, help="requests in the serving run")
+    ap.add_argument("--reg-search", type=int, default=0, help="qubit-remap schedule: 0 greedy, 1 searched")
+    ap.add_argument("--serving-requests", type=int, default=500, help="requests at the high rate")
+    ap.add_argument("--serving-rate", type=float, default=2000.0)
+    ap.add_argument("--serving-low-requests", type=int, default=60, help="requests at the low rate")
+    ap.add_argument("--serving-low-rate", type=float, default=2.0)
     ap.add_argument("--autotune", action="store_true",
-                    help="time the candidate plans first and run the headline with the fastest")
+                    help="run the headline with the autotuner's options")
     ap.add_argument("--interpreted", action="store_true",
                     help="run the prebuilt op interpreter instead of the per-program compiled passes")
     ap.add_argument("--n", type=int, default=20)
@@ -126,25 +146,83 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
+# ------------------------------------------------------------- CPU baselines --
+
 def cpu_baseline(desc, samples: int):
-    """The oracle (complex128 port, all host threads) on `samples` samples of
-    the workload; returns amplitude-updates/s and what was timed."""
+    """The oracle (complex128 port, all host threads) on the first `samples`
+    samples of the workload.  Returns (record, measured output of those
+    samples) -- the output is the oracle value the GPU result is checked
+    against."""
     from oracle import oracle
     from qandle_gb300 import workloads
 
     threads = len(os.sched_getaffinity(0))
     lo = oracle.Lowered(desc, samples)
     t0 = time.perf_counter()
-    oracle.run(desc, batch=samples, nthreads=threads, lowered=lo)
+    st = oracle.run(desc, batch=samples, nthreads=threads, lowered=lo)
     dt = time.perf_counter() - t0
     amp = workloads.gate_count(desc) * samples * (1 << desc["n"])
-    return {"value": amp / dt, "unit": "amp-updates/s", "cores": threads, "kind": "port",
-            "sample": f"{samples} of {desc['batch']} samples of the {desc['n']}-qubit workload, "
-                      f"{dt:.2f} s"}
+    rec = {"value": amp / dt, "unit": "amp-updates/s", "cores": threads, "kind": "port",
+           "sample": f"{samples} of {desc['batch']} samples of the {desc['n']}-qubit workload, {dt:.2f} s"}
+    return rec, oracle.measure(desc, st)
+
+
+def reference_torch_baseline(gpu_ms: dict | None = None):
+    """The reference's own torch path (qandle 0.1.8 from baseline/_ref) on
+    the host cores, all threads, at config 1 (8 qubits x 64, the plain
+    circuit, joint probabilities) and at 10 qubits x 64 (the largest its
+    dense 2^n x 2^n matrices reach in seconds).  Median of timed forwards
+    after one untimed forward.  `gpu_ms` maps the same keys to our GPU
+    times, for the ratio."""
+    from oracle import oracle
+    from oracle import reference_torch as rt
+    from qandle_gb300 import workloads
+
+    why = rt.unavailable_reason()
+    if why:
+        return {"unavailable": why}
+    import torch
+
+    threads = len(os.sched_getaffinity(0))
+    torch.set_num_threads(threads)
+    qandle = rt.import_reference()
+    out = {"kind": "reference", "cores": threads,
+           "what": "qandle 0.1.8 Circuit.forward (dense matmul per layer) on the host CPU, torch "
+                   f"{torch.__version__}, {threads} threads, remapping=None, qw_map stand-in"}
+    for key, n, reps in (("config1_n8_b64", 8, 3), ("n10_b64", 10, 1)):
+        desc = workloads.plain_small(n=n, batch=64, layers=4)
+        t_build = time.perf_counter()
+        circ = rt.build_circuit(qandle, desc)
+        build_s = time.perf_counter() - t_build
+        kw = rt.inputs(desc)
+        with torch.no_grad():
+            t0 = time.perf_counter()
+            res = circ(**kw)
+            first = time.perf_counter() - t0
+            times = []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                res = circ(**kw)
+                times.append(time.perf_counter() - t0)
+        ms = 1e3 * float(np.median(times))
+        amp = workloads.gate_count(desc) * 64 * (1 << n)
+        rec = {"ms_per_forward": ms, "value": amp / (ms * 1e-3), "unit": "amp-updates/s",
+               "first_forward_ms": 1e3 * first, "build_s": build_s, "timed_forwards": reps,
+               "max_abs_err_vs_oracle": float(np.abs(res.numpy() - oracle.forward(desc)).max())}
+        if gpu_ms and key in gpu_ms:
+            rec["gpu"] = gpu_ms[key]
+            rec["gpu_speedup_plain"] = ms / gpu_ms[key]["plain_ms"]
+            rec["gpu_speedup_fused"] = ms / gpu_ms[key]["fused_ms"]
+        out[key] = rec
+        if first > 60.0:
+            break
+    return out
 
 
 def run_reference(args):
-    """CPU arm: the oracle port on the host cores, each step a bounded sample."""
+    """CPU arm: the oracle port on the host cores, each step a bounded sample
+    of the headline workload; the reference's own torch path beside it at the
+    sizes it can run."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -156,7 +234,7 @@ def run_reference(args):
         cpu_baseline(desc, samples)
     times = []
     for _ in range(args.steps):
-        r = cpu_baseline(desc, samples)
+        r, _ = cpu_baseline(desc, samples)
         times.append(r)
     value = float(np.mean([r["value"] for r in times]))
     amp_step = workloads.gate_count(desc) * samples * (1 << desc["n"])
@@ -170,8 +248,105 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": "amp-updates/s", "cores": times[0]["cores"],
                              "kind": "port", "sample": times[0]["sample"]},
             "e2e": {"value": value, "unit": "amp-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.no_cpu:
+        line["reference_torch"] = reference_torch_baseline()
     print(json.dumps(line), flush=True)
 
+
+# ------------------------------------------------------------- roofline bits --
+
+def fp32_peak(dev) -> dict:
+    """FP32 FMA throughput of the library's probe kernel (packed FMAs, all
+    SMs), median of three launches of a few milliseconds."""
+    import torch
+
+    from qandle_gb300 import _lib
+
+    lib = _lib.load()
+    blocks = lib.qg_fp32_probe_blocks()
+    out = torch.empty(blocks, dtype=torch.float32, device=dev)
+    cnt = ctypes.c_int64()
+    iters = 1 << 16
+
+    def launch():
+        _lib.check(lib.qg_fp32_probe(out.data_ptr(), blocks, iters, ctypes.byref(cnt), _lib.stream()))
+
+    launch()
+    torch.cuda.synchronize(dev)
+    ms = []
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        launch()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms.append(e0.elapsed_time(e1))
+    t = float(np.median(ms))
+    return {"tflops": 2.0 * cnt.value / (t * 1e-3) / 1e12, "fma_per_launch": cnt.value, "ms": t,
+            "kernel": "k_fp32_probe (fma.rn.f32x2, 8 chains per thread, 4 x 256 threads per SM)"}
+
+
+def pass_fmas(prog, backward: bool, amps: int) -> np.ndarray:
+    """Counted FMAs of every pass: a 2x2 on a register qubit is 8 FMAs per
+    amplitude, a diagonal 4; the backward applies each gate to psi and lambda
+    and a gradient partial adds 2 per amplitude."""
+    out = []
+    for pd in prog.passes(backward):
+        ops = pd["ops"]
+        mats = int(np.sum(ops[:, 0] == 2)) if len(ops) else 0
+        diags = int(np.sum(ops[:, 0] == 3)) if len(ops) else 0
+        if backward:
+            grads = int(np.sum((ops[:, 0] == 2) & ((ops[:, 3] & 2) != 0))) if len(ops) else 0
+            f = 16 * mats + 8 * diags + 2 * grads
+        else:
+            f = 8 * mats + 4 * diags
+        out.append(f * amps)
+    return np.array(out, dtype=np.float64)
+
+
+def pass_bytes_fwd(prog, amps: int) -> np.ndarray:
+    """Algorithmic bytes of every forward pass: 8 B per amplitude read, 8 B
+    per amplitude written (state or checkpoint), 4 B per probability."""
+    out = []
+    for pd in prog.passes(False):
+        b = 0
+        if pd["init"] == 0:
+            b += 8 * amps
+        if pd["epi"] & 1:
+            b += 8 * amps
+        if pd["epi"] & 2:
+            b += 4 * amps
+        if pd["ckpt"] >= 0:
+            b += 8 * amps
+        out.append(b)
+    return np.array(out, dtype=np.float64)
+
+
+def pass_bytes_bwd(prog, amps: int) -> np.ndarray:
+    """Algorithmic bytes of every backward pass: psi and lambda read (16 B
+    per amplitude), and written back (16 B) by the passes that store (the
+    last pass of the backward stores nothing unless the input-state gradient
+    is wanted, which this workload does not)."""
+    out = []
+    for pd in prog.passes(True):
+        b = 16 * amps
+        if pd["epi"] & 1:
+            b += 16 * amps
+        out.append(b)
+    return np.array(out, dtype=np.float64)
+
+
+def combined_roof(ms: np.ndarray, bytes_: np.ndarray, fmas: np.ndarray, hbm_gbs: float, fp32_tflops: float):
+    """Per pass the time the better of the two roofs allows:
+    max(bytes / HBM, 2 FMAs / FP32), and its sum against the measured sum."""
+    t_mem = bytes_ / (hbm_gbs * 1e9) * 1e3
+    t_fp = 2.0 * fmas / (fp32_tflops * 1e12) * 1e3
+    t_roof = np.maximum(t_mem, t_fp)
+    return float(t_roof.sum() / ms.sum()), t_mem, t_fp
+
+
+# ------------------------------------------------------------------- main --
 
 def main():
     args = parse()
@@ -211,7 +386,7 @@ def main():
 
     # ---------------- fused forward, inputs resident in HBM ----------------
     opts = dict(tile_bits=args.tile_bits, low_bits=args.low_bits, max_high=args.k, reg_bits=args.reg_bits,
-                compiled=not args.interpreted)
+                reg_search=args.reg_search, compiled=not args.interpreted)
     tuned = None
     if args.autotune:
         from qandle_gb300 import tune
@@ -249,29 +424,17 @@ def main():
     clock_info = clocks.stop()
     ms = max_over_ranks(t0.elapsed_time(t1)) / K
     value = world * amp_step / (ms * 1e-3)
+    headline_out = bound.result().clone()
     pass_ms = np.array([[events[s][2 * p].elapsed_time(events[s][2 * p + 1]) for p in range(P)]
                         for s in range(K)])
-    # algorithmic bytes of each pass launch: 8 B per amplitude read, 8 B per
-    # amplitude written (state), 4 B per probability written
     amps = B * (1 << n)
-    pass_bytes = []
-    for pd in prog.passes(False):
-        b = 0
-        if pd["init"] == 0:
-            b += 8 * amps
-        if pd["epi"] & 1:
-            b += 8 * amps
-        if pd["epi"] & 2:
-            b += 4 * amps
-        if pd["ckpt"] >= 0:
-            b += 8 * amps
-        pass_bytes.append(b)
-    pass_bytes = np.array(pass_bytes, dtype=np.float64)
-    avg_bytes = float(pass_bytes.mean())
+    pbytes = pass_bytes_fwd(prog, amps)
+    pfmas = pass_fmas(prog, False, amps)
+    avg_bytes = float(pbytes.mean())
     avg_pass_ms = float(pass_ms.mean())
     achieved = avg_bytes / (avg_pass_ms * 1e-3) / 1e9
     # per-pass bandwidth of the middle passes (load + store, 16 B / amplitude)
-    mid = [p for p in range(P) if pass_bytes[p] == 16 * amps]
+    mid = [p for p in range(P) if pbytes[p] == 16 * amps]
     mid_gbs = float(16 * amps / (pass_ms[:, mid].mean() * 1e-3) / 1e9) if mid else None
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "fwd_pass_traffic.json")
@@ -279,6 +442,11 @@ def main():
         with open(tpath) as f:
             traffic = json.load(f).get("dram_bytes_per_launch")
     gpu_launches = K * (P + 3)  # matrix build, embedding factors, P passes, <Z> reduction
+    fp32 = fp32_peak(dev)
+    mean_ms = pass_ms.mean(0)
+    comb, t_mem, t_fp = combined_roof(mean_ms, pbytes, pfmas, hbm_peak, fp32["tflops"])
+    fp_frac = 2.0 * pfmas / (mean_ms * 1e-3) / (fp32["tflops"] * 1e12)
+    heavy = [p for p in range(P) if t_fp[p] > t_mem[p]]
 
     line = {
         "metric": "amplitude-updates/s", "value": value, "unit": "amp-updates/s", "n_gpus": world,
@@ -295,13 +463,27 @@ def main():
                                 "qg_fwd_pass (compiled per pass)") + f", 2^{args.tile_bits}-amplitude tiles",
                      "launches_per_step": P,
                      "avg_launch_ms": avg_pass_ms, "algorithmic_bytes_per_launch": avg_bytes,
-                     "middle_pass_GBps": mid_gbs},
+                     "middle_pass_GBps": mid_gbs,
+                     "fp32": {"peak_tflops": fp32["tflops"], "peak_kind": "measured (library probe kernel)",
+                              "achieved_tflops": float(2.0 * pfmas.sum() / (mean_ms.sum() * 1e-3) / 1e12),
+                              "frac": float(2.0 * pfmas.sum() / (mean_ms.sum() * 1e-3) / (fp32["tflops"] * 1e12)),
+                              "fma_per_amp_per_pass": [round(float(f) / amps, 1) for f in pfmas],
+                              "heavy_passes": len(heavy),
+                              "heavy_pass_frac": (float(2.0 * pfmas[heavy].sum() / (mean_ms[heavy].sum() * 1e-3)
+                                                        / (fp32["tflops"] * 1e12)) if heavy else None),
+                              "probe": fp32},
+                     "combined_frac": comb,
+                     "per_pass": [{"ms": round(float(mean_ms[p]), 4), "GBps": round(float(
+                         pbytes[p] / (mean_ms[p] * 1e-3) / 1e9), 1), "hbm_frac": round(float(
+                             pbytes[p] / (mean_ms[p] * 1e-3) / 1e9 / hbm_peak), 3),
+                         "fp32_frac": round(float(fp_frac[p]), 3),
+                         "roof_frac": round(float(max(t_mem[p], t_fp[p]) / mean_ms[p]), 3)} for p in range(P)]},
         "clocks": clock_info,
         "gpu_launches": gpu_launches,
     }
     if tuned is not None:
-        line["autotune"] = {"options": tuned["options"], "cached": tuned["cached"],
-                            "timings_ms": [[o, round(t, 3)] for o, t in tuned["timings"]]}
+        line["autotune_headline"] = {"options": tuned["options"], "cached": tuned["cached"],
+                                     "timings_ms": [[o, round(t, 3)] for o, t in tuned["timings"]]}
 
     # ---------------- end to end through the public API ----------------
     x_host = torch.tensor(desc["inputs"]["x"]).pin_memory()
@@ -326,7 +508,10 @@ def main():
     e2e_ms = max_over_ranks((time.perf_counter() - t_e2e) * 1e3 / K)
     line["e2e"] = {"value": world * amp_step / (e2e_ms * 1e-3), "unit": "amp-updates/s",
                    "h2d_bytes_per_step": int(x_host.numel() * 4), "d2h_bytes_per_step": int(res.numel() * 4),
-                   "ms_per_step": e2e_ms}
+                   "ms_per_step": e2e_ms,
+                   "path": "Circuit.__call__ (inference: replays the captured forward graph)",
+                   "captured": any(b.graph is not None for b in circ._executor._bounds.values())}
+    oracle_err = {}
 
     if not args.no_extras:
         # ---------------- one CUDA graph per forward ----------------
@@ -342,7 +527,8 @@ def main():
         g1.record()
         sync_all()
         gms = g0.elapsed_time(g1) / K
-        line["graph"] = {"value": amp_step / (gms * 1e-3), "ms_per_step": gms}
+        line["graph"] = {"value": amp_step / (gms * 1e-3), "ms_per_step": gms,
+                         "max_abs_diff_vs_launch": float((bound.result() - headline_out).abs().max())}
         del bound
 
         # ---------------- plain per-gate form, same workload ----------------
@@ -359,65 +545,110 @@ def main():
             p1.record()
             sync_all()
         pms = p0.elapsed_time(p1) / steps_p
-        with torch.no_grad():
-            fused_out = circ(**kw)
         line["plain"] = {"value": amp_step / (pms * 1e-3), "ms_per_step": pms,
                          "fused_speedup": pms / ms,
-                         "max_abs_diff_vs_fused": float((fused_out - ref_out).abs().max())}
-        del circ_p
+                         "max_abs_diff_vs_fused": float((headline_out - ref_out).abs().max())}
+        del circ_p, ref_out
         torch.cuda.empty_cache()
 
+        # ---------------- config 1: 8 qubits x 64, plain method ----------------
+        line["config1"], gpu_ms_small = bench_config1(dev, sync_all, oracle_err)
+
         # ---------------- adjoint: 16 qubits x batch 1024, MSE(<Z>, t) ----------------
-        line["adjoint"] = bench_adjoint(dev, sync_all, W)
+        line["adjoint"] = bench_adjoint(dev, sync_all, W, hbm_peak, fp32["tflops"], oracle_err)
         torch.cuda.empty_cache()
 
         # ---------------- deep single state: 28 qubits x batch 1 ----------------
-        line["deep28"] = bench_deep(dev, sync_all, W)
+        line["deep28"] = bench_deep(dev, sync_all, W, oracle_err)
         torch.cuda.empty_cache()
+
+        # ---------------- fusion width sweep, autotuner ----------------
+        if not args.no_sweep:
+            line["k_sweep"] = bench_k_sweep(desc, kw, dev, sync_all, amp_step, ms)
+            torch.cuda.empty_cache()
+        if not args.no_autotune:
+            line["autotune"] = bench_autotune(desc, dev, amp_step, ms)
+            torch.cuda.empty_cache()
 
         # ---------------- serving: Poisson arrivals of mixed-width requests ----------------
-        line["serving"] = bench_serving(dev, args.serving_requests)
-        torch.cuda.empty_cache()
-
-        # ---------------- fusion width sweep ----------------
-        if args.sweep:
-            sweep = {}
-            for k in range(1, 8):
-                c = workloads.build_circuit(desc, engine="fused", max_high=k).to(dev)
-                ex_k = None
-                with torch.no_grad():
-                    c(**kw)
-                ex_k = c._executor
-                bk = engine.BoundForward(ex_k, B, dev)
-                bk.set_inputs(**kw)
-                bk.launch()
-                sync_all()
-                a0 = torch.cuda.Event(enable_timing=True)
-                a1 = torch.cuda.Event(enable_timing=True)
-                a0.record()
-                for _ in range(3):
-                    bk.launch()
-                a1.record()
-                sync_all()
-                kms = a0.elapsed_time(a1) / 3
-                sweep[str(k)] = {"passes": bk.prog.info.forward_passes, "ms_per_step": kms,
-                                 "value": amp_step / (kms * 1e-3)}
-                del bk, c
-            line["k_sweep"] = sweep
+        if not args.no_serving:
+            line["serving"] = {
+                "high_rate": bench_serving(dev, args.serving_requests, args.serving_rate, seed=7,
+                                           oracle_err=oracle_err),
+                "low_rate": bench_serving(dev, args.serving_low_requests, args.serving_low_rate, seed=8,
+                                          oracle_err=oracle_err)}
+            torch.cuda.empty_cache()
+    else:
+        gpu_ms_small = None
 
     if rank == 0:
-        line["cpu_baseline"] = None if args.no_cpu else cpu_baseline(desc, args.cpu_samples)
+        if args.no_cpu:
+            line["cpu_baseline"] = None
+        else:
+            rec, ref = cpu_baseline(desc, args.cpu_samples)
+            line["cpu_baseline"] = rec
+            got = headline_out[:args.cpu_samples].cpu().numpy()
+            oracle_err["config2_z_first_%d_samples" % args.cpu_samples] = float(np.abs(got - ref).max())
+            line["reference_torch"] = reference_torch_baseline(gpu_ms_small)
+        line["oracle_error"] = dict(oracle_err, tolerance=1e-5,
+                                    note="max-abs against the complex128 oracle on the same seeded inputs; "
+                                         "probabilities, P0 and <Z> within 1e-5, gradients within 1e-4")
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
 
 
-def bench_deep(dev, sync_all, W):
-    """28 qubits, batch 1 (2 GiB), 50 layers of U per qubit with CNOT+SWAP
-    brickwork, |psi|^2 out: fused forward against the per-gate form."""
+def bench_config1(dev, sync_all, oracle_err):
+    """Config 1 on the GPU: 8 qubits x 64, AngleEmbedding(rx), 4 layers of
+    RY + CNOT ring, joint probabilities; plain per-gate form and fused
+    engine, each a median over 20 forwards, both checked against the oracle.
+    Also 10 qubits x 64 (the reference's largest size) for the CPU ratio."""
     import torch
 
+    from oracle import oracle
+    from qandle_gb300 import workloads
+
+    out, gpu_ms = {}, {}
+    for key, n in (("config1_n8_b64", 8), ("n10_b64", 10)):
+        desc = workloads.plain_small(n=n, batch=64, layers=4)
+        kw = workloads.circuit_inputs(desc, dev)
+        ref = oracle.forward(desc)
+        rec = {}
+        for eng in ("plain", "fused"):
+            circ = workloads.build_circuit(desc, engine=eng).to(dev)
+            with torch.no_grad():
+                for _ in range(3):
+                    res = circ(**kw)
+                sync_all()
+                times = []
+                for _ in range(20):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    res = circ(**kw)
+                    e1.record()
+                    sync_all()
+                    times.append(e0.elapsed_time(e1))
+            rec[f"{eng}_ms"] = float(np.median(times))
+            err = float(np.abs(res.cpu().numpy() - ref).max())
+            rec[f"{eng}_max_abs_err_vs_oracle"] = err
+            oracle_err[f"{key}_{eng}_probs"] = err
+        amp = workloads.gate_count(desc) * 64 * (1 << n)
+        rec["plain_value"] = amp / (rec["plain_ms"] * 1e-3)
+        rec["fused_value"] = amp / (rec["fused_ms"] * 1e-3)
+        out[key] = rec
+        gpu_ms[key] = {"plain_ms": rec["plain_ms"], "fused_ms": rec["fused_ms"]}
+    return out, gpu_ms
+
+
+def bench_deep(dev, sync_all, W, oracle_err):
+    """28 qubits, batch 1 (2 GiB), 50 layers of U per qubit with CNOT+SWAP
+    brickwork, |psi|^2 out: fused forward against the per-gate form; the
+    20-qubit prefix circuit against the oracle."""
+    import torch
+
+    from oracle import oracle
     from qandle_gb300 import engine, workloads
 
     desc = workloads.deep_u()
@@ -428,7 +659,7 @@ def bench_deep(dev, sync_all, W):
         circ()
     bound = engine.BoundForward(circ._executor, 1, dev)
     bound.set_inputs()  # the circuit's U matrices
-    for _ in range(max(1, W)):
+    for _ in range(max(3, W)):
         bound.launch()
     sync_all()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -445,32 +676,95 @@ def bench_deep(dev, sync_all, W):
     del bound
     circ_p = workloads.build_circuit(desc, engine="plain").to(dev)
     with torch.no_grad():
+        plain_probs = circ_p().reshape(-1)  # warm-up
         sync_all()
-        p0 = torch.cuda.Event(enable_timing=True)
-        p1 = torch.cuda.Event(enable_timing=True)
-        p0.record()
-        plain_probs = circ_p().reshape(-1)
-        p1.record()
-        sync_all()
-    pms = p0.elapsed_time(p1)
+        times = []
+        for _ in range(3):
+            p0 = torch.cuda.Event(enable_timing=True)
+            p1 = torch.cuda.Event(enable_timing=True)
+            p0.record()
+            plain_probs = circ_p().reshape(-1)
+            p1.record()
+            sync_all()
+            times.append(p0.elapsed_time(p1))
+    pms = float(np.median(times))
     diff = float((plain_probs - fused_probs).abs().max())
+    del circ_p, plain_probs, fused_probs
+    torch.cuda.empty_cache()
+    pre = workloads.restrict(desc, 20)
+    cpre = workloads.build_circuit(pre, engine="fused").to(dev)
+    with torch.no_grad():
+        got = cpre().reshape(-1).cpu().numpy()
+    perr = float(np.abs(got - oracle.forward(pre).reshape(-1)).max())
+    oracle_err["config4_prefix20_probs"] = perr
     return {"workload": f"deep_u: {n} qubits x batch 1, 50 layers of U + CNOT/SWAP brickwork, |psi|^2 out "
                         f"({workloads.gate_count(desc)} gates)",
             "plan": circ._executor.program(False).summary(),
             "ms_per_step_fused": fms, "ms_per_step_per_gate": pms, "fused_speedup": pms / fms,
+            "per_gate_timing": "median of 3 after one untimed forward",
             "amp_updates_per_s_fused": amp / (fms * 1e-3), "amp_updates_per_s_per_gate": amp / (pms * 1e-3),
-            "norm_fused": norm, "max_abs_prob_diff_fused_vs_per_gate": diff}
+            "norm_fused": norm, "max_abs_prob_diff_fused_vs_per_gate": diff,
+            "prefix20_max_abs_err_vs_oracle": perr}
 
 
-def bench_serving(dev, count: int, rate: float = 2000.0, seed: int = 7):
-    """Open-loop Poisson arrivals (rate per second) of mixed strongly-
-    entangling requests: n ~ U{4..24}, depth ~ U{2..30}, batch log-uniform in
-    [1, 512], <Z> out.  The continuous-batching server against the same
-    requests served one after another in arrival order by the per-gate form
-    (one launch per gate per request)."""
-    import numpy as np
+def bench_k_sweep(desc, kw, dev, sync_all, amp_step, headline_ms):
+    """Fused forward with at most k strided qubits per pass, k = 1..6 (the
+    default plan takes up to the tile's limit, 7 at 2^13 tiles and 64-
+    amplitude runs)."""
     import torch
 
+    from qandle_gb300 import engine, workloads
+
+    sweep = {}
+    for k in range(1, 7):
+        c = workloads.build_circuit(desc, engine="fused", max_high=k, graphs=False).to(dev)
+        bk = engine.BoundForward(c._executor, desc["batch"], dev)
+        bk.set_inputs(**kw)
+        bk.launch()
+        sync_all()
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record()
+        for _ in range(3):
+            bk.launch()
+        a1.record()
+        sync_all()
+        kms = a0.elapsed_time(a1) / 3
+        sweep[str(k)] = {"passes": bk.prog.info.forward_passes, "exchanges_ops": bk.prog.summary(),
+                         "ms_per_step": kms, "value": amp_step / (kms * 1e-3)}
+        del bk, c
+    sweep["default (k = 7)"] = {"ms_per_step": headline_ms, "value": amp_step / (headline_ms * 1e-3)}
+    return sweep
+
+
+def bench_autotune(desc, dev, amp_step, default_ms):
+    """The autotuner's staged search (tile shapes, then k, then the
+    qubit-remap schedule) on the headline circuit at its batch; its pick
+    against the default plan."""
+    from qandle_gb300 import tune, workloads
+
+    path = os.path.join(tempfile.mkdtemp(prefix="qgtune"), "tune.json")
+    t0 = time.perf_counter()
+    res = tune.autotune(workloads.build_circuit(desc, engine="fused"), desc["batch"], dev, cache_path=path)
+    return {"options": res["options"], "ms": res["ms"], "value": amp_step / (res["ms"] * 1e-3),
+            "default_ms": default_ms, "speedup_vs_default": default_ms / res["ms"],
+            "search_s": time.perf_counter() - t0,
+            "timings_ms": [[o, round(t, 3)] for o, t in res["timings"]]}
+
+
+def bench_serving(dev, count: int, rate: float, seed: int, oracle_err: dict):
+    """Open-loop Poisson arrivals (`rate` per second) of `count` mixed
+    strongly-entangling requests: n ~ U{4..24}, depth ~ U{2..30}, batch
+    log-uniform in [1, 512], <Z> out.  Two live runs on the same arrival
+    times: the continuous-batching server, and a worker that serves the
+    requests one after another in arrival order with the plain per-gate form
+    (one launch per gate per request), starting each when it has arrived and
+    the previous one is done.  Both include their per-request preparation in
+    the latency (the server's lowering and planning, the per-gate form's
+    module construction)."""
+    import torch
+
+    from oracle import oracle
     from qandle_gb300 import serve, workloads
 
     rng = np.random.default_rng(seed)
@@ -487,7 +781,7 @@ def bench_serving(dev, count: int, rate: float = 2000.0, seed: int = 7):
             if wait > 0:
                 time.sleep(wait)
             handles.append(srv.submit(d, arrival=t0 + o))
-        outs = [h.future.result(timeout=900) for h in handles]
+        outs = [h.future.result(timeout=1800) for h in handles]
         t_end = max(h.completed for h in handles)
         steps, launches = srv.steps, srv.launches
     finally:
@@ -500,33 +794,51 @@ def bench_serving(dev, count: int, rate: float = 2000.0, seed: int = 7):
     del handles
     torch.cuda.empty_cache()
 
-    service, diff = [], 0.0
-    for i, d in enumerate(reqs):
-        torch.cuda.synchronize(dev)
-        s = time.perf_counter()
-        out = serve.run_plain(d, dev).cpu()
-        service.append(time.perf_counter() - s)
-        diff = max(diff, float((out - outs[i]).abs().max()))
-        del out
-    done, lat_p = 0.0, []
-    for o, sv in zip(offs, service):
-        done = max(done, o) + sv
-        lat_p.append((done - o) * 1e3)
-    lat_p = np.array(lat_p)
+    # live per-gate FIFO on the same arrival times
+    done_at = [None] * count
+    diff = [0.0]
+    stream = torch.cuda.Stream(device=dev)
+
+    def worker(t_start):
+        with torch.cuda.device(dev), torch.cuda.stream(stream):
+            for i, (d, o) in enumerate(zip(reqs, offs)):
+                wait = t_start + o - time.perf_counter()
+                if wait > 0:
+                    time.sleep(wait)
+                out = serve.run_plain(d, dev).cpu()  # .cpu() waits for the request's kernels
+                done_at[i] = time.perf_counter()
+                diff[0] = max(diff[0], float((out - outs[i]).abs().max()))
+
+    t0p = time.perf_counter()
+    th = threading.Thread(target=worker, args=(t0p,))
+    th.start()
+    th.join()
+    lat_p = np.array([(done_at[i] - (t0p + offs[i])) * 1e3 for i in range(count)])
+    span_p = max(done_at) - t0p
     plain = {"p50_ms": float(np.percentile(lat_p, 50)), "p99_ms": float(np.percentile(lat_p, 99)),
-             "circuits_per_s": count / done, "amp_updates_per_s": amp / done, "wall_s": done}
+             "circuits_per_s": count / span_p, "amp_updates_per_s": amp / span_p, "wall_s": span_p}
+    # the oracle on the requests it finishes quickly (up to 14 qubits)
+    err = 0.0
+    checked = 0
+    for d, o in zip(reqs, outs):
+        if d["n"] <= 14:
+            err = max(err, float(np.abs(o.numpy() - oracle.forward(d)).max()))
+            checked += 1
+    oracle_err[f"serving_{rate:g}_per_s_z_{checked}_requests_n_le_14"] = err
     return {"workload": f"{count} requests, Poisson {rate:g}/s, n ~ U{{4..24}}, depth ~ U{{2..30}}, "
-                        "batch log-uniform [1, 512], <Z> out (seed 7)",
-            "amp_updates": amp, "continuous_batching": fused, "per_gate_fifo": plain,
+                        f"batch log-uniform [1, 512], <Z> out (seed {seed})",
+            "offered_s": float(offs[-1]), "amp_updates": amp, "continuous_batching": fused,
+            "per_gate_fifo_live": plain,
             "throughput_ratio": fused["circuits_per_s"] / plain["circuits_per_s"],
-            "max_abs_diff_vs_per_gate": diff,
-            "note": "per-gate latencies replay the measured service times in arrival order (FIFO)"}
+            "p99_ratio_per_gate_over_batched": plain["p99_ms"] / fused["p99_ms"],
+            "max_abs_diff_vs_per_gate": diff[0], "max_abs_err_vs_oracle_n_le_14": err}
 
 
-def bench_adjoint(dev, sync_all, W):
+def bench_adjoint(dev, sync_all, W, hbm_peak, fp32_tflops, oracle_err):
     import torch
 
     import qandle_gb300 as q
+    from oracle import oracle
     from qandle_gb300 import plain, workloads
 
     desc = workloads.adjoint_brick()
@@ -560,6 +872,24 @@ def bench_adjoint(dev, sync_all, W):
     fms = e0.elapsed_time(e1) / steps
     g_fused = torch.stack([p.grad.reshape(()) for p in params])
 
+    # backward passes timed one by one (CUDA events on the launching stream)
+    ex = circ._executor
+    prog = ex.program(True)
+    NB = prog.info.backward_passes
+    amps = B * (1 << n)
+    bms = []
+    for _ in range(3):
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(2 * NB)]
+        ex.backward_events = evs
+        step()
+        sync_all()
+        bms.append([evs[2 * p].elapsed_time(evs[2 * p + 1]) for p in range(NB)])
+    bms = np.array(bms).mean(0)
+    bbytes = pass_bytes_bwd(prog, amps)
+    bfmas = pass_fmas(prog, True, amps)
+    comb, t_mem, t_fp = combined_roof(bms, bbytes, bfmas, hbm_peak, fp32_tflops)
+    achieved = float(bbytes.mean() / (bms.mean() * 1e-3) / 1e9)
+
     # per-gate adjoint on the same circuit (one kernel pass per gate and state)
     circ_p = workloads.build_circuit(desc, engine="plain").to(dev)
     with torch.no_grad():
@@ -576,6 +906,27 @@ def bench_adjoint(dev, sync_all, W):
     sync_all()
     pms = e2.elapsed_time(e3)
     g_plain = torch.stack([g.reshape(()) for g in g_plain])
+    del circ_p
+    torch.cuda.empty_cache()
+
+    # the same workload at its full depth on 8 samples against the oracle
+    small = workloads.adjoint_brick(batch=8)
+    small["measure"] = "p0"
+    cs = workloads.build_circuit(small, engine="fused", checkpoint_segments=4).to(dev)
+    sts = torch.zeros(8, 1 << n, dtype=torch.complex64, device=dev)
+    sts[:, 0] = 1
+    pz = cs(sts)
+    loss = ((2.0 * pz - 1.0 - torch.tensor(small["targets"], device=dev)) ** 2).mean()
+    loss.backward()
+    dth = np.array([m.theta.grad.item() for m in cs.circuit.layers if isinstance(m, q.BuiltParametrizedOperator)])
+    p0_ref = oracle.forward(small)
+    _, gref = oracle.mse_z_grad(2.0 * p0_ref - 1.0, small["targets"].astype(np.float64))
+    rdp, _, _ = oracle.adjoint(small, gref, "p0")
+    z_err = float(np.abs((2.0 * pz.detach().cpu().numpy() - 1.0) - (2.0 * p0_ref - 1.0)).max())
+    g_err = float(np.abs(dth - rdp).max())
+    oracle_err["config3_z_8_samples"] = z_err
+    oracle_err["config3_grad_8_samples"] = g_err
+
     gates = len(desc["gates"])
     amp = gates * B * (1 << n)
     return {"workload": f"adjoint_brick: {n} qubits x batch {B}, 20 layers, {len(params)} angles, "
@@ -586,6 +937,17 @@ def bench_adjoint(dev, sync_all, W):
             "amp_updates_per_s_per_gate": 3 * amp / (pms * 1e-3),
             "gradients_per_s_fused": len(params) * B / (fms * 1e-3),
             "max_abs_grad_diff_fused_vs_per_gate": float((g_fused - g_plain).abs().max()),
+            "plan": prog.summary(),
+            "roofline": {"bound": "hbm", "kernel": "qg_bwd_pass (compiled per pass), 2^12-amplitude tiles",
+                         "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                         "launches_per_step": NB, "avg_launch_ms": float(bms.mean()),
+                         "algorithmic_bytes_per_launch": float(bbytes.mean()),
+                         "bytes_per_amp": "32 (psi and lambda read and written), 16 on passes that only read",
+                         "backward_ms_per_step": float(bms.sum()),
+                         "fp32_frac": float(2.0 * bfmas.sum() / (bms.sum() * 1e-3) / (fp32_tflops * 1e12)),
+                         "combined_frac": comb,
+                         "passes_fp32_bound": int(np.sum(t_fp > t_mem))},
+            "max_abs_err_vs_oracle_8_samples": {"z": z_err, "grad": g_err},
             "note": "step = forward + backward; amp-updates count each gate once forward and twice "
                     "backward (state and cotangent)"}
 

@@ -126,7 +126,10 @@ int qg_measure_p0(const void* state, float* out, int64_t batch, int n, void* scr
  * (batch * (2^n / 2^min(n,12)) * (min(n,12) + 1)) return QG_ENOMEM.  The
  * first call on a device looks up the array's address (make it before any
  * stream capture); all calls share the array, so calls that overlap on the
- * GPU race. */
+ * GPU race.  The looked-up address is cached per device ordinal for the life
+ * of the process: after cudaDeviceReset on a device, the cached address
+ * belongs to a context that no longer exists, so do not call this entry point
+ * on that device again in the same process. */
 #define QG_P0_NOALLOC_MAX_PARTIALS (1 << 20)
 int qg_measure_p0_noalloc(const void* state, float* out, int64_t batch, int n, void* stream);
 
@@ -200,6 +203,10 @@ typedef struct qg_plan_options {
                            each segment from it */
     int32_t reg_bits;   /* amplitudes per thread = 2^reg_bits (4 or 5): 4 halves the
                            registers per thread and doubles the warps per tile */
+    int32_t reg_search; /* qubit-remap schedule of the forward passes: 0 = greedy (each
+                           new register set is the one the next gates ask for), 1 = try
+                           every register set of the tile's qubits and keep the one that
+                           places the most gates (backward passes always search) */
 } qg_plan_options;
 
 typedef struct qg_program qg_program;
@@ -326,6 +333,15 @@ int qg_workspace_status(const void* workspace, void* stream);
  * usable.  (No reference counterpart.) */
 int qg_selftest_wait_timeout(int64_t limit_ns, void* stream);
 
+/* FP32 roof probe for the roofline of the fused passes (no reference
+ * counterpart): qg_fp32_probe_blocks() blocks of 256 threads each run
+ * independent chains of packed FP32 FMAs for `iters` iterations and write one
+ * float per block into out (at least qg_fp32_probe_blocks() floats).
+ * *fma_count receives the FMAs the launch performs; time it with events on
+ * `stream`.  Changes no device setting. */
+int64_t qg_fp32_probe_blocks(void);
+int qg_fp32_probe(float* out, int64_t out_floats, int64_t iters, int64_t* fma_count, void* stream);
+
 /* Adjoint backward.  state: the forward's final state (overwritten: it is
  * un-computed gate by gate); lam: [B][2^n] buffer.  grad_out is the upstream
  * gradient of the forward output (float [B][n] for P0/<Z>, float [B][2^n]
@@ -337,6 +353,17 @@ int qg_program_backward(const qg_program* prog, const void* dev_table, void* wor
                         const float* params, const float* named, const void* umats,
                         const void* grad_out, float* dparams, float* dnamed, void* dstate,
                         const void* ckpt, void* stream);
+
+/* Same as qg_program_backward, and records pass_events[2p] / [2p+1]
+ * (cudaEvent_t, created by the caller) on `stream` around backward pass p,
+ * so a caller can time the backward pass kernels on the stream they run on.
+ * (No reference counterpart: the reference's backward is torch autograd
+ * through dense matmuls, qandle/operators.py:230,271.) */
+int qg_program_backward_timed(const qg_program* prog, const void* dev_table, void* workspace,
+                              int64_t workspace_bytes, void* state, void* lam, int64_t batch,
+                              const float* params, const float* named, const void* umats,
+                              const void* grad_out, float* dparams, float* dnamed, void* dstate,
+                              const void* ckpt, void* const* pass_events, void* stream);
 
 #ifdef __cplusplus
 }

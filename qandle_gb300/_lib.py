@@ -30,7 +30,7 @@ class Gate(ctypes.Structure):
 class PlanOptions(ctypes.Structure):
     """qg_plan_options."""
     _fields_ = [(f, ctypes.c_int32) for f in ("tile_bits", "low_bits", "max_high", "measure",
-                                              "keep_state", "segments", "reg_bits")]
+                                              "keep_state", "segments", "reg_bits", "reg_search")]
 
 
 class ProgramInfo(ctypes.Structure):
@@ -118,10 +118,15 @@ SIGNATURES = {
     "qg_jobs_run_pass": (c_int, [ctypes.POINTER(Job), c_int, c_void_p]),
     "qg_workspace_status": (c_int, [c_void_p, c_void_p]),
     "qg_selftest_wait_timeout": (c_int, [c_int64, c_void_p]),
+    "qg_fp32_probe_blocks": (c_int64, []),
+    "qg_fp32_probe": (c_int, [c_void_p, c_int64, c_int64, c_void_p, c_void_p]),
     "qg_program_finish": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p]),
     "qg_program_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
                                     c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p]),
+    "qg_program_backward_timed": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
+                                          c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                          c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 

@@ -83,7 +83,11 @@ __device__ __forceinline__ void bwd_producer(const PassDesc& d, const RunArgs& A
         float2* ps = pbuf0 + s * 2 * AMPS;
         float2* ls = ps + AMPS;
         if (i >= 2) {
-            if (!mbar_wait(bar_empty + s, (uint32_t)((i / 2 - 1) & 1))) {
+            // the lanes agree before any of them leaves the loop: a lane that
+            // gave up alone would miss the warp-wide __syncwarp and
+            // __reduce_add_sync below
+            const bool released = mbar_wait(bar_empty + s, (uint32_t)((i / 2 - 1) & 1));
+            if (!__all_sync(0xffffffffu, released)) {
                 failed = true;
                 break;
             }

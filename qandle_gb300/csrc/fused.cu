@@ -632,6 +632,34 @@ __global__ void k_selftest_wait(int* status, uint64_t limit_ns) {
     if (threadIdx.x == 0) *status = done ? 0 : kStatusTimeout;
 }
 
+// FP32 roof probe: every thread runs 8 independent chains of packed FMAs
+// (fma.rn.f32x2, 2 FMAs per instruction) and its block writes one sum, so
+// nothing is dead code.  Four 256-thread blocks per SM keep 8 warps on each
+// scheduler.  b < 1 and c small keep the values finite.
+constexpr int kProbeChains = 8;
+__global__ void __launch_bounds__(256) k_fp32_probe(float* out, int64_t iters) {
+    float2 a[kProbeChains];
+#pragma unroll
+    for (int k = 0; k < kProbeChains; ++k) a[k] = make_float2(1e-3f * (threadIdx.x + k), 1e-3f * k);
+    const float2 b = make_float2(0.999999f, 0.999998f), c = make_float2(1e-7f, 2e-7f);
+    for (int64_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < kProbeChains; ++k) a[k] = vfma(a[k], b, c);
+    }
+    float v = 0.f;
+#pragma unroll
+    for (int k = 0; k < kProbeChains; ++k) v += a[k].x + a[k].y;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __shared__ float part[8];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < 8; ++w) t += part[w];
+        out[blockIdx.x] = t;
+    }
+}
+
 static int64_t num_tiles(int n, int tb, int64_t B) {
     if (n >= tb) return B << (n - tb);
     int64_t spt = int64_t(1) << (tb - n);
@@ -749,6 +777,19 @@ int qg_workspace_status(const void* workspace, void* stream) {
     return h;
 }
 
+int64_t qg_fp32_probe_blocks(void) { return (int64_t)qg::sm_count() * 4; }
+
+int qg_fp32_probe(float* out, int64_t out_floats, int64_t iters, int64_t* fma_count, void* stream) {
+    const int64_t blocks = qg_fp32_probe_blocks();
+    QG_CHECK_ARG(out && fma_count, "null pointer");
+    QG_CHECK_ARG(blocks > 0 && out_floats >= blocks, "out holds fewer floats than qg_fp32_probe_blocks()");
+    QG_CHECK_ARG(iters >= 1 && iters <= (int64_t(1) << 24), "iters must be in [1, 2^24]");
+    qg::k_fp32_probe<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(out, iters);
+    QG_LAUNCH_CHECK();
+    *fma_count = blocks * 256 * iters * qg::kProbeChains * 2;
+    return QG_OK;
+}
+
 int qg_selftest_wait_timeout(int64_t limit_ns, void* stream) {
     QG_CHECK_ARG(limit_ns > 0 && limit_ns <= 2000000000LL, "limit_ns must be in (0, 2e9]");
     cudaStream_t st = (cudaStream_t)stream;
@@ -839,6 +880,15 @@ int qg_program_backward(const qg_program* prog, const void* dev_table, void* wor
                         void* state, void* lam, int64_t batch, const float* params, const float* named,
                         const void* umats, const void* grad_out, float* dparams, float* dnamed, void* dstate,
                         const void* ckpt, void* stream) {
+    return qg_program_backward_timed(prog, dev_table, workspace, workspace_bytes, state, lam, batch, params, named,
+                                     umats, grad_out, dparams, dnamed, dstate, ckpt, nullptr, stream);
+}
+
+int qg_program_backward_timed(const qg_program* prog, const void* dev_table, void* workspace,
+                              int64_t workspace_bytes, void* state, void* lam, int64_t batch, const float* params,
+                              const float* named, const void* umats, const void* grad_out, float* dparams,
+                              float* dnamed, void* dstate, const void* ckpt, void* const* pass_events,
+                              void* stream) {
     using namespace qg;
     QG_CHECK_ARG(prog && dev_table && workspace && state && lam && grad_out, "null pointer");
     QG_CHECK_ARG(batch >= 1, "batch must be >= 1");
@@ -883,11 +933,13 @@ int qg_program_backward(const qg_program* prog, const void* dev_table, void* wor
     int64_t tiles = num_tiles(R.n, tb, batch);
     for (int p = 0; p < R.nbpass; ++p) {
         int store_lam = (p + 1 == R.nbpass) && dstate != nullptr;
+        if (pass_events) QG_CUDA_TRY(cudaEventRecord((cudaEvent_t)pass_events[2 * p], st));
         JitKernel jk;
         int rc = jit_backward_kernel(prog, p, &jk)
                      ? launch_bwd_compiled(jk, dpass, dops, p, A, store_lam, tiles, tb, st)
                      : launch_bwd(dpass, dops, p, A, store_lam, tiles, tb, kBwdRegBits, st);
         if (rc) return rc;
+        if (pass_events) QG_CUDA_TRY(cudaEventRecord((cudaEvent_t)pass_events[2 * p + 1], st));
     }
     int64_t fitems = R.nparams + (int64_t)R.ncols * batch;
     if (fitems > 0) {

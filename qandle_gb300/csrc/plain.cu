@@ -779,7 +779,8 @@ static int rotation_grad(const void* out_state, const void* grad_out, float* dth
 //   beyond that.
 // - Set-up: the first call on a device looks up the array's device address
 //   (cudaGetSymbolAddress, with that device current) and caches it; make that
-//   first call before any stream capture.
+//   first call before any stream capture.  A cudaDeviceReset invalidates the
+//   cached address; the entry point must not be used on that device again.
 // - Sharing: every call uses the same array.  Nothing in it needs to start at
 //   zero (each block writes all its partials before the reduction reads
 //   them), but calls whose kernels overlap on the GPU (different streams,
@@ -798,12 +799,14 @@ extern "C" int qg_measure_p0_noalloc(const void* state, float* out, int64_t batc
     if (n == 0) return QG_OK;
     int c = n < kChunkBits ? n : kChunkBits;
     int64_t nch = (int64_t(1) << n) >> c;
-    int64_t need = batch * nch * (c + 1);
-    if (need > (int64_t)QG_P0_NOALLOC_MAX_PARTIALS) {
+    // per-sample need first, so that a huge batch cannot wrap the product
+    const int64_t per_sample = nch * (c + 1);
+    if (batch > (int64_t)QG_P0_NOALLOC_MAX_PARTIALS / per_sample) {
         qg::set_error("qg_measure_p0_noalloc: batch " + std::to_string(batch) + " at " + std::to_string(n) +
-                      " qubits needs " + std::to_string(need) + " partial sums, the static array holds " +
+                      " qubits needs " + std::to_string(per_sample) +
+                      " partial sums per sample, more than the static array holds (" +
                       std::to_string((int64_t)QG_P0_NOALLOC_MAX_PARTIALS) +
-                      "; use qg_measure_p0 with a caller-provided scratch buffer");
+                      "); use qg_measure_p0 with a caller-provided scratch buffer");
         return QG_ENOMEM;
     }
     int dev = 0;

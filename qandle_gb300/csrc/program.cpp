@@ -433,13 +433,14 @@ void emit_pass(Program& P, PassPlan& pp, const std::vector<LGate>& G, bool backw
                 if (nat_ok && !(R & (1u << nat.reg[k]))) R |= 1u << nat.reg[k];
             for (int b = 0; b < tb && popc(R) < rb; ++b)
                 if ((qubit_local & (1u << b)) && !(R & (1u << b))) R |= 1u << b;
-            // Backward plans: every register set of rb tile qubits (at most
-            // C(12, 4) = 495) is tried; the one under which the most gates can be
-            // placed wins (the greedy set above on ties), so each exchange of psi
-            // and lambda buys as much work as it can.  Forward plans keep the
-            // greedy set: on the 20-qubit forward the search saved 2 of 55
-            // exchanges but ran 1.7 % slower, and serving plans every request.
-            if (backward && popc(qubit_local) > rb) {
+            // Backward plans (and forward plans with reg_search): every register
+            // set of rb tile qubits (at most C(13, 5) = 1287) is tried; the one
+            // under which the most gates can be placed wins (the greedy set above
+            // on ties), so each exchange buys as much work as it can.  Forward
+            // plans default to the greedy set: on the 20-qubit forward the search
+            // saved 2 of 55 exchanges but ran 1.7 % slower, and serving plans
+            // every request; the autotuner times both.
+            if ((backward || P.opt.reg_search) && popc(qubit_local) > rb) {
                 std::vector<int> qb;
                 for (int b = 0; b < tb; ++b)
                     if (qubit_local & (1u << b)) qb.push_back(b);
@@ -1044,6 +1045,7 @@ int qg_program_create(const qg_gate* gates, int ngates, const int32_t* qlist, in
     if (o.tile_bits - 5 - o.reg_bits < 0 || o.tile_bits - 5 - o.reg_bits > 4)
         return qg::set_error("tile_bits - reg_bits must leave 0..4 warp bits"), QG_EINVAL;
     if (o.segments < 1) o.segments = 1;
+    if (o.reg_search != 0 && o.reg_search != 1) return qg::set_error("reg_search must be 0 or 1"), QG_EINVAL;
     std::unique_ptr<Program> P(new Program());
     P->n = n;
     P->opt = o;

@@ -42,7 +42,8 @@ def allreduce_gradients(params: typing.Iterable[torch.Tensor], weight: float = 1
 
     All gradients travel as one flat buffer (one collective per step).
     Parameters without a gradient contribute zeros, so every rank passes the
-    same list.  Pass ``weight = local_batch / global_batch`` when the loss is
+    same list.  The buffer has the widest dtype of the parameters (at least
+    float32).  Pass ``weight = local_batch / global_batch`` when the loss is
     a mean over the global batch."""
     params = [p for p in params]
     if not params:
@@ -52,7 +53,12 @@ def allreduce_gradients(params: typing.Iterable[torch.Tensor], weight: float = 1
     for p in params:
         g = p.grad if p.grad is not None else torch.zeros_like(p)
         grads.append(g.reshape(-1))
-    flat = torch.cat(grads).to(torch.float32) * weight
+    # one buffer in the widest dtype of the list (float32 at least), so
+    # float64 parameters keep their precision through the sum
+    dtype = torch.float32
+    for p in params:
+        dtype = torch.promote_types(dtype, p.dtype)
+    flat = torch.cat([g.to(dtype) for g in grads]) * weight
     if world > 1:
         dist.all_reduce(flat, op=dist.ReduceOp.SUM, group=group)
     off = 0

@@ -12,6 +12,7 @@ fallback.
 """
 from __future__ import annotations
 
+import collections
 import ctypes
 import os
 import threading
@@ -177,7 +178,8 @@ class Program:
     """A planned gate program: host handle plus device copies of its tables."""
 
     def __init__(self, lowered: Lowered, measure: str, keep_state: bool, tile_bits: int = 13,
-                 low_bits: int = 6, max_high: int = 0, segments: int = 1, reg_bits: int = 5):
+                 low_bits: int = 6, max_high: int = 0, segments: int = 1, reg_bits: int = 5,
+                 reg_search: int = 0):
         lib = _lib.load()
         self.n = lowered.n
         self.measure = measure
@@ -194,6 +196,7 @@ class Program:
         opt.keep_state = 1 if keep_state else 0
         opt.segments = segments
         opt.reg_bits = reg_bits
+        opt.reg_search = int(reg_search)
         handle = ctypes.c_void_p()
         _lib.check(lib.qg_program_create(gates, len(lowered.gates), ctypes.cast(ql, ctypes.c_void_p),
                                          self.n, ctypes.byref(opt), ctypes.byref(handle)))
@@ -319,6 +322,7 @@ class Program:
 
 # QG_CHECK_STATUS=1: read the workspace status word after every fused forward
 # and backward (one stream synchronisation per call) and raise on a timeout.
+# Without it the status words are still read, without blocking (_StatusWatch).
 _CHECK_STATUS = os.environ.get("QG_CHECK_STATUS", "0") not in ("", "0")
 
 
@@ -327,6 +331,67 @@ def check_status(workspace: torch.Tensor) -> None:
     timed-out wait (its results are then invalid).  Synchronises the current
     stream."""
     _lib.check(_lib.load().qg_workspace_status(workspace.data_ptr(), _lib.stream()))
+
+
+class _StatusWatch:
+    """Reads the pass kernels' status words without blocking the host.
+
+    After every fused forward or backward, the word at the start of the
+    call's workspace is copied on the same stream into a ring of pinned host
+    slots, and an event marks the copy.  Each later call first looks at the
+    copies that have landed (oldest first, stopping at the first still in
+    flight) and raises RuntimeError for a nonzero word: a pass kernel's
+    bounded wait ran out, so that earlier call's results are invalid.  The
+    copy is ordered before the workspace returns to the allocator, so a later
+    call that reuses the memory and clears the word cannot hide it.  Only a
+    full ring (RING copies in flight) makes a call wait for the oldest."""
+
+    RING = 64
+
+    def __init__(self):
+        self._host = None
+        self._pending = collections.deque()  # (slot, event, what)
+        self._free = list(range(self.RING))
+        self._lock = threading.Lock()
+
+    def _take(self, slot, ev, what):
+        v = int(self._host[slot])
+        self._free.append(slot)
+        if v != 0:
+            raise RuntimeError(f"a fused {what} reported status {v}: a pass kernel's wait timed out "
+                               "(a producer / compute hand-off never completed); its results are invalid")
+
+    def poll(self) -> None:
+        with self._lock:
+            while self._pending and self._pending[0][1].query():
+                self._take(*self._pending.popleft())
+
+    def record(self, workspace: torch.Tensor, what: str) -> None:
+        with self._lock:
+            if self._host is None:
+                self._host = torch.zeros(self.RING, dtype=torch.int32, pin_memory=True)
+            while self._pending and self._pending[0][1].query():
+                self._take(*self._pending.popleft())
+            if not self._free:
+                slot, ev, w = self._pending.popleft()
+                ev.synchronize()
+                self._take(slot, ev, w)
+            slot = self._free.pop()
+            self._host[slot:slot + 1].copy_(workspace[:4].view(torch.int32), non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record()
+            self._pending.append((slot, ev, what))
+
+    def drain(self) -> None:
+        """Wait for every copy in flight and raise for a nonzero word."""
+        with self._lock:
+            while self._pending:
+                slot, ev, w = self._pending.popleft()
+                ev.synchronize()
+                self._take(slot, ev, w)
+
+
+STATUS = _StatusWatch()
 
 
 def _gather_params(lo: Lowered, device) -> torch.Tensor:
@@ -453,7 +518,13 @@ class _Inputs:
         else:
             self.params = torch.zeros(1, dtype=torch.float32, device=device)
         if lo.umats:
-            self.umats = torch.stack([u.to(device) for u in lo.umats]).contiguous()
+            # the lowering holds its own copies of the fixed matrices, so the
+            # stacked table moves to a device once
+            cache = lo.__dict__.setdefault("_umats_dev", {})
+            key = str(device)
+            if key not in cache:
+                cache[key] = torch.stack(lo.umats).to(device).contiguous()
+            self.umats = cache[key]
         else:
             self.umats = torch.zeros(1, 2, 2, dtype=torch.complex64, device=device)
 
@@ -482,9 +553,23 @@ class _FusedRun(torch.autograd.Function):
 class FusedExecutor:
     """Runs a built circuit through the fused engine (used by Circuit)."""
 
+    # inference calls keep at most this many captured forwards (one per
+    # device, batch and input kind), least recently used dropped first
+    MAX_GRAPHS = 2
+
     def __init__(self, circuit, tile_bits: int = 13, low_bits: int = 6, max_high: int = 0,
-                 checkpoint_segments: int = 1, reg_bits: int = 5, compiled: bool = None):
+                 checkpoint_segments: int = 1, reg_bits: int = 5, compiled: bool = None,
+                 graphs: bool = None, reg_search: int = 0):
         self.circuit = circuit
+        # graphs = True: an inference call (no gradient needed, a measured
+        # output) replays one captured CUDA graph of the whole forward, kept
+        # per (device, batch, input kind); the default follows QG_GRAPHS (on
+        # unless set to 0)
+        if graphs is None:
+            graphs = os.environ.get("QG_GRAPHS", "1") != "0"
+        self.graphs = bool(graphs)
+        self._bounds = collections.OrderedDict()
+        self._bounds_lock = threading.Lock()
         # compiled = True: forward passes run as per-program kernels compiled
         # at first use (NVRTC); False: the prebuilt op interpreter.  The
         # default follows QG_COMPILE (on unless set to 0).
@@ -501,9 +586,13 @@ class FusedExecutor:
             self.lowered = None
             self.fusible = False
             warnings.warn(f"{e}; this circuit runs one kernel per gate")
-        self.options = dict(tile_bits=tile_bits, low_bits=low_bits, max_high=max_high, reg_bits=reg_bits)
+        self.options = dict(tile_bits=tile_bits, low_bits=low_bits, max_high=max_high, reg_bits=reg_bits,
+                            reg_search=int(reg_search))
         self.checkpoint_segments = checkpoint_segments
         self._programs = {}
+        # timing hook: a list of 2 x (backward passes) CUDA events makes the
+        # next backward record a pair around every backward pass (then clears)
+        self.backward_events = None
 
     def program(self, training: bool) -> Program:
         key = bool(training)
@@ -526,13 +615,42 @@ class FusedExecutor:
                                "with .to('cuda')")
         if state is not None:
             _lib.require_cuda_state(state)
+        STATUS.poll()
         inp = _Inputs(self.lowered, state, kwargs, dev)
         zero_init = 1 if (state is None and not self._has_embedding()) else 0
         training = torch.is_grad_enabled() and any(
             t is not None and t.requires_grad for t in (state, inp.params, inp.named))
+        if not training and self.graphs and self.lowered.measure != "state":
+            out = self._replay(inp, state, dev)
+            return _out_shape(self.lowered.measure, out, self.n, inp.unbatched)
         out = _FusedRun.apply(self, self.program(training), state, inp.params, inp.named, inp.umats,
                               inp.batch, zero_init)
         return _out_shape(self.lowered.measure, out, self.n, inp.unbatched)
+
+    def _replay(self, inp: "_Inputs", state, dev) -> torch.Tensor:
+        """Inference through a captured forward: the call's values go into the
+        static buffers of a BoundForward for (device, batch, whether a state
+        is given), captured into one CUDA graph at its first use, and the
+        graph is replayed on the current stream.  Returns a copy of the
+        measured output (the static output buffer is reused by the next
+        call)."""
+        key = (str(dev), inp.batch, state is not None)
+        with self._bounds_lock:
+            b = self._bounds.pop(key, None)
+            if b is None:
+                while len(self._bounds) >= self.MAX_GRAPHS:
+                    self._bounds.popitem(last=False)
+                b = BoundForward(self, inp.batch, dev, has_state=state is not None)
+            self._bounds[key] = b
+        b.set_from(inp, state)
+        if b.graph is None:
+            b.capture()
+        b.replay()
+        if _CHECK_STATUS:
+            check_status(b.ws)
+        else:
+            STATUS.record(b.ws, "forward")
+        return b.out.clone()
 
     def _has_embedding(self) -> bool:
         return any(g[0] == _lib.GATE["emb"] for g in self.lowered.gates)
@@ -575,6 +693,8 @@ class FusedExecutor:
                   _lib.ptr(out), _lib.ptr(ckpt), _lib.stream())
         if _CHECK_STATUS:
             check_status(ws)
+        else:
+            STATUS.record(ws, "forward")
         ctx.ex = self
         ctx.prog = prog
         ctx.batch = B
@@ -590,6 +710,7 @@ class FusedExecutor:
         if not prog.keep_state:
             raise RuntimeError("the fused forward ran without gradient tracking")
         st, params, named, umats = ctx.saved_tensors
+        STATUS.poll()  # a forward whose wait ran out has no valid state to differentiate
         if getattr(ctx, "_consumed", False):
             raise RuntimeError("the fused engine's backward can run once per forward "
                                "(retain_graph is not supported)")
@@ -606,12 +727,20 @@ class FusedExecutor:
         dnamed = torch.empty(B, max(1, prog.info.ncols), dtype=torch.float32, device=dev)
         need_state = ctx.needs_input_grad[2] and not prog.info.has_embedding
         dstate = torch.empty_like(st) if need_state else None
-        _lib.call("qg_program_backward", prog.handle, prog.table(dev).data_ptr(), ws.data_ptr(), ws.numel(),
+        evp = None
+        events = self.backward_events
+        if events is not None:
+            # one backward records an event pair around every backward pass
+            self.backward_events = None
+            evp = (ctypes.c_void_p * len(events))(*[e.cuda_event for e in events])
+        _lib.call("qg_program_backward_timed", prog.handle, prog.table(dev).data_ptr(), ws.data_ptr(), ws.numel(),
                   st.data_ptr(), lam.data_ptr(), B, params.data_ptr(), named.data_ptr(), umats.data_ptr(),
                   g.data_ptr(), dparams.data_ptr(), dnamed.data_ptr(), _lib.ptr(dstate),
-                  _lib.ptr(ctx.ckpt), _lib.stream())
+                  _lib.ptr(ctx.ckpt), evp, _lib.stream())
         if _CHECK_STATUS:
             check_status(ws)
+        else:
+            STATUS.record(ws, "backward")
         gstate = None
         if need_state:
             shp = ctx.state_shape
@@ -664,7 +793,12 @@ class BoundForward:
 
     def set_inputs(self, state=None, **kwargs) -> None:
         with torch.no_grad():
-            inp = _Inputs(self.ex.lowered, state, kwargs, self.device)
+            self.set_from(_Inputs(self.ex.lowered, state, kwargs, self.device), state)
+
+    def set_from(self, inp: "_Inputs", state=None) -> None:
+        """Copy the gathered values of one call (and its input state) into
+        the static buffers, on the current stream."""
+        with torch.no_grad():
             if inp.batch != self.batch and inp.batch != 1:
                 raise ValueError(f"bound for batch {self.batch}, got {inp.batch}")
             self.params[:inp.params.numel()].copy_(inp.params)

@@ -5,8 +5,10 @@ reference and runs them on one of two executors:
 
 * ``engine="fused"`` (default): the circuit is lowered once to a gate
   program and run by the fused CUDA engine (qandle_gb300.engine) -- gate
-  fusion into shared-memory passes, one graph replay per call, adjoint
-  backward.
+  fusion into shared-memory passes; an inference call with a measured output
+  replays one captured CUDA graph of the whole forward (kept per device,
+  batch and input kind); a call that needs gradients launches the passes
+  and runs the adjoint backward.
 * ``engine="plain"``: the reference's per-layer loop
   (UnsplittedCircuit.forward, qcircuit.py:163-174) with one CUDA kernel pass
   per gate (qandle_gb300.plain).

@@ -6,10 +6,12 @@ loop keeps every admitted request's state, matrix tables and embedding
 factors on the device and advances all admitted requests together: each
 step is ONE multi-job launch of the fused pass kernel (qg_jobs_run_pass)
 that runs the next pass of every active request, whatever its width.  New
-requests are admitted between steps as soon as the HBM budget
-(sum of 2^n * 8 B * batch over admitted requests) has room, so requests that
-arrive while others are on the GPU join the running batch instead of
-waiting for it to drain.
+requests are admitted between steps as soon as the HBM budget has room, so
+requests that arrive while others are on the GPU join the running batch
+instead of waiting for it to drain.  A request counts against the budget
+with everything it holds on the device while admitted: its state
+(2^n * 8 B * batch), its program workspace (matrix tables, embedding factors,
+measurement partials) and its output.
 
 Each request's tiles are computed by the same code in the same order
 whatever else shares the launch, and its reductions run in a fixed order,
@@ -118,6 +120,9 @@ class Request:
         self.admitted = None
         self.completed = None
         self.future: cf.Future = cf.Future()
+        self.lowered = None   # (lowered, params, named, shift), set at submit
+        self.prog = None
+        self.need = 0         # device bytes while admitted
 
     @property
     def latency(self):
@@ -127,8 +132,8 @@ class Request:
 class Server:
     """Continuous-batching executor on one device.
 
-    hbm_budget: bytes of state the admitted requests may hold together
-    (2^n * 8 B * batch each).  max_active: requests advanced per step (a
+    hbm_budget: device bytes the admitted requests may hold together (state,
+    workspace and output of each).  max_active: requests advanced per step (a
     multiple of the 32 jobs one launch takes means several launches).
     """
 
@@ -139,6 +144,7 @@ class Server:
         self.max_active = max_active
         self.opts = dict(tile_bits=tile_bits, low_bits=low_bits)
         self.programs: dict = {}
+        self._plock = threading.Lock()
         self.stream = torch.cuda.Stream(device=self.device)
         self._queue = collections.deque()
         self._cv = threading.Condition()
@@ -155,10 +161,17 @@ class Server:
     # -- public --
     def submit(self, desc: dict, arrival: float | None = None) -> Request:
         req = Request(desc, arrival)
-        need = self._state_bytes(desc)
+        try:
+            req.lowered = lower_description(desc)
+            req.prog = self._program(req.lowered[0])
+        except (ValueError, RuntimeError) as e:
+            req.future.set_exception(e)
+            return req
+        need = req.need = self._device_bytes(req)
         if need > self.budget:
             req.future.set_exception(MemoryError(
-                f"request needs {need} bytes of state, more than the HBM budget {self.budget}"))
+                f"request needs {need} bytes of device memory (state, workspace, output), more than the "
+                f"HBM budget {self.budget}"))
             return req
         with self._cv:
             self._queue.append(req)
@@ -174,26 +187,33 @@ class Server:
 
     # -- internals --
     @staticmethod
-    def _state_bytes(desc):
-        n = max(desc["n"], 5)
-        return (1 << n) * 8 * (desc["batch"] or 1)
+    def _device_bytes(req: "Request") -> int:
+        """Device bytes a request holds while admitted: state, workspace
+        (each rounded up like the caching allocator's 512-byte blocks) and
+        output."""
+        lo = req.lowered[0]
+        B = req.desc["batch"] or 1
+        rnd = lambda x: (int(x) + 511) // 512 * 512  # noqa: E731
+        ws = _lib.load().qg_program_workspace_bytes(req.prog.handle, B, 0)
+        return rnd((1 << lo.n) * 8 * B) + rnd(max(int(ws), 256)) + rnd(B * lo.n * 4) + rnd(32) * 3
 
     def _program(self, lo: Lowered) -> Program:
         key = structure_key(lo)
-        p = self.programs.get(key)
-        if p is None:
-            p = Program(lo, lo.measure, keep_state=False, **self.opts)
-            self.programs[key] = p
+        with self._plock:
+            p = self.programs.get(key)
+            if p is None:
+                p = Program(lo, lo.measure, keep_state=False, **self.opts)
+                self.programs[key] = p
         return p
 
     def _admit(self, req: Request) -> _Slot:
-        lo, params, named, shift = lower_description(req.desc)
-        prog = self._program(lo)
+        lo, params, named, shift = req.lowered
+        prog = req.prog
         B = req.desc["batch"] or 1
         n = lo.n
         s = _Slot()
         s.req, s.prog, s.batch, s.next_pass, s.shift = req, prog, B, 0, shift
-        s.bytes = (1 << n) * 8 * B
+        s.bytes = req.need
         dev = self.device
         s.state = torch.empty(B, 1 << n, dtype=torch.complex64, device=dev)
         s.ws = prog.workspace(B, False, dev)
@@ -219,7 +239,7 @@ class Server:
                         break
                     # admit against the HBM budget, oldest first
                     while self._queue and len(active) < self.max_active:
-                        need = self._state_bytes(self._queue[0].desc)
+                        need = self._queue[0].need
                         if self._used + need > self.budget:
                             break
                         req = self._queue.popleft()

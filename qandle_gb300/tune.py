@@ -1,15 +1,26 @@
 """Autotuner for the fused engine's plan options.
 
-The best tile shape depends on the circuit and the batch: a 2^13 tile holds
-more qubits per pass (fewer HBM round trips), a 2^12 tile runs two CTAs per
-SM, longer contiguous runs (``low_bits``) make the loads denser but leave
-fewer tile slots for strided qubits, and 16 instead of 32 amplitudes per
-thread trade exchanges for occupancy.  ``autotune`` plans and runs each
-candidate on the device with the circuit's own structure at the given batch,
-times its forward with CUDA events, and returns the fastest option set.
-Results are kept in a JSON file keyed by the circuit's gate structure (gate
-kinds and qubits, not angles), the batch, the device and whether passes are
-compiled, so a later process gets the answer without running anything.
+The best plan depends on the circuit and the batch:
+
+* tile shape: a 2^13 tile holds more qubits per pass (fewer HBM round
+  trips), a 2^12 tile runs two CTAs per SM, longer contiguous runs
+  (``low_bits``) make the loads denser but leave fewer tile slots for strided
+  qubits, and 16 instead of 32 amplitudes per thread trade exchanges for
+  occupancy;
+* fusion width k (``max_high``): the strided qubits a pass may take; a
+  smaller k gives lighter passes (and more of them);
+* qubit-remap schedule (``reg_search``): which tile qubits each exchange
+  brings into the registers -- the greedy set the next gates ask for, or the
+  set (searched over all of them) that places the most gates.
+
+``autotune`` plans and runs candidates on the device with the circuit's own
+structure at the given batch and times each forward with CUDA events.
+Without an explicit candidate list it searches in stages: the tile shapes
+first, then k one and two below the tile's limit on the best shape, then the
+searched remap schedule on the best of those.  Results are kept in a JSON
+file keyed by the circuit's gate structure (gate kinds and qubits, not
+angles), the batch, the device and whether passes are compiled, so a later
+process gets the answer without running anything.
 """
 from __future__ import annotations
 
@@ -23,6 +34,7 @@ import torch
 
 from . import engine
 
+# stage 1 of the search: tile shapes (k at the tile's limit, greedy remap)
 DEFAULT_CANDIDATES: typing.List[dict] = [
     dict(tile_bits=13, low_bits=6, reg_bits=5),
     dict(tile_bits=12, low_bits=6, reg_bits=5),
@@ -30,6 +42,13 @@ DEFAULT_CANDIDATES: typing.List[dict] = [
     dict(tile_bits=13, low_bits=7, reg_bits=5),
     dict(tile_bits=12, low_bits=6, reg_bits=4),
 ]
+
+
+def _k_candidates(best: dict, n: int) -> typing.List[dict]:
+    """Stage 2: k (max_high) one and two below the tile's strided limit."""
+    limit = min(n, best["tile_bits"]) - min(best["low_bits"], n)
+    return [dict(best, max_high=k) for k in (limit - 1, limit - 2) if k >= 1]
+
 
 _lock = threading.Lock()
 
@@ -116,14 +135,25 @@ def autotune(circuit, batch: int, device="cuda", candidates: typing.Optional[typ
     hit = _load(path).get(key)
     if hit is not None:
         return dict(hit, cached=True)
-    cands = candidates or DEFAULT_CANDIDATES
     timings = []
-    for opt in cands:
-        try:
-            ms = timer(opt) if timer is not None else time_candidate(built, batch, device, opt, reps, compiled)
-        except RuntimeError:
-            continue
-        timings.append((dict(opt), float(ms)))
+
+    def run(opts):
+        for opt in opts:
+            if any(o == opt for o, _ in timings):
+                continue
+            try:
+                ms = timer(opt) if timer is not None else time_candidate(built, batch, device, opt, reps, compiled)
+            except RuntimeError:
+                continue
+            timings.append((dict(opt), float(ms)))
+
+    if candidates:
+        run(candidates)
+    else:
+        run(DEFAULT_CANDIDATES)
+        if timings:
+            run(_k_candidates(min(timings, key=lambda t: t[1])[0], built.num_qubits))
+            run([dict(min(timings, key=lambda t: t[1])[0], reg_search=1)])
     if not timings:
         raise RuntimeError("no candidate plan could be run for this circuit")
     best = min(timings, key=lambda t: t[1])

@@ -87,3 +87,16 @@ def test_two_rank_gradient_allreduce_equals_full_batch():
         got = [out[0], out[1]]
     assert np.allclose(got[0], got[1])
     assert np.abs(got[0] - full).max() < 1e-5 * max(1.0, np.abs(full).max())
+
+
+def test_allreduce_keeps_float64_precision():
+    # one process, no process group: the flat buffer still round-trips the
+    # gradients, and a float64 gradient keeps digits float32 would drop
+    p64 = torch.nn.Parameter(torch.zeros(3, dtype=torch.float64))
+    p32 = torch.nn.Parameter(torch.zeros(2, dtype=torch.float32))
+    p64.grad = torch.tensor([1.0 + 1e-12, -2.0, 3.0], dtype=torch.float64)
+    p32.grad = torch.tensor([0.5, 0.25], dtype=torch.float32)
+    qd.allreduce_gradients([p64, p32], weight=1.0)
+    assert p64.grad.dtype == torch.float64
+    assert p64.grad[0].item() == 1.0 + 1e-12
+    assert torch.equal(p32.grad, torch.tensor([0.5, 0.25]))

@@ -53,7 +53,8 @@ CASES = {
     "plain_n12": lambda: workloads.plain_small(n=12, batch=5, layers=3),
 }
 OPTS = [dict(), dict(tile_bits=12, low_bits=4, max_high=2), dict(tile_bits=11, low_bits=5, max_high=1),
-        dict(tile_bits=13, low_bits=7, max_high=6), dict(reg_bits=4), dict(tile_bits=12, reg_bits=4)]
+        dict(tile_bits=13, low_bits=7, max_high=6), dict(reg_bits=4), dict(tile_bits=12, reg_bits=4),
+        dict(max_high=5, reg_search=1)]
 
 
 @pytest.mark.parametrize("compiled", [True, False], ids=["compiled", "interpreted"])

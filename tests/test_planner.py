@@ -50,7 +50,8 @@ CASES = [
 ]
 OPTS = [dict(tile_bits=13, low_bits=6, max_high=0), dict(tile_bits=12, low_bits=4, max_high=2),
         dict(tile_bits=11, low_bits=5, max_high=1), dict(tile_bits=13, low_bits=8, max_high=3),
-        dict(tile_bits=13, low_bits=6, reg_bits=4), dict(tile_bits=12, low_bits=5, reg_bits=4)]
+        dict(tile_bits=13, low_bits=6, reg_bits=4), dict(tile_bits=12, low_bits=5, reg_bits=4),
+        dict(tile_bits=13, low_bits=6, reg_search=1), dict(tile_bits=13, low_bits=6, max_high=4, reg_search=1)]
 
 
 @pytest.mark.parametrize("case", [c[0] for c in CASES])

@@ -42,8 +42,14 @@ def test_budget_refuses_and_queues(cuda_device):
     big = workloads.random_sel_request(rng, n_range=(14, 14), depth_range=(2, 2), batch_max=1)
     big["batch"] = 64
     big["inputs"]["x"] = np.resize(big["inputs"]["x"], (64, 14)).astype(np.float32)
-    need = (1 << 14) * 8 * 64
-    srv = serve.Server(cuda_device, hbm_budget=need)  # room for one such request at a time
+    srv = serve.Server(cuda_device, hbm_budget=1 << 40)
+    # room for one such request at a time: its state, workspace and output
+    probe = serve.Request(big)
+    probe.lowered = serve.lower_description(big)
+    probe.prog = srv._program(probe.lowered[0])
+    need = serve.Server._device_bytes(probe)
+    assert need > (1 << 14) * 8 * 64  # more than the state alone
+    srv.budget = need
     try:
         too_big = dict(big)
         too_big["batch"] = 65

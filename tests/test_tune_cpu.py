@@ -61,3 +61,27 @@ def test_autotune_needs_a_runnable_candidate(tmp_path):
     with pytest.raises(RuntimeError):
         tune.autotune(circ, 4, "cpu", candidates=[dict(tile_bits=13)], cache_path=str(tmp_path / "t.json"),
                       timer=timer)
+
+
+def test_staged_search_tries_k_and_remap_schedule(tmp_path):
+    """Without a candidate list the search runs the tile shapes, then k one
+    and two below the tile's strided limit on the best shape, then the
+    searched remap schedule on the best so far."""
+    circ = _circuit(workloads.sel_reupload(n=16, batch=4, layers=2, reupload_every=1))
+    calls = []
+
+    def timer(opt):
+        calls.append(dict(opt))
+        ms = 2.0 if opt["tile_bits"] == 12 else 3.0
+        if opt.get("max_high") == 5:  # tile 12, low 6: limit 6, so k = 5 and 4 are tried
+            ms -= 0.5
+        if opt.get("reg_search"):
+            ms -= 0.25
+        return ms
+
+    res = tune.autotune(circ, 4, "cpu", cache_path=str(tmp_path / "t.json"), timer=timer)
+    assert calls[:len(tune.DEFAULT_CANDIDATES)] == tune.DEFAULT_CANDIDATES
+    ks = [c.get("max_high") for c in calls if "max_high" in c and not c.get("reg_search")]
+    assert ks == [5, 4]
+    assert calls[-1].get("reg_search") == 1 and calls[-1].get("max_high") == 5
+    assert res["options"] == calls[-1] and res["ms"] == 1.25

@@ -62,3 +62,8 @@ def test_noalloc_refuses_oversize(cuda_device):
                                    400, 20, None)
     assert rc == 4
     assert b"static array" in lib.qg_last_error()
+    # a batch so large that batch * partials-per-sample wraps int64 is refused too
+    rc = lib.qg_measure_p0_noalloc(ctypes.c_void_p(st.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                   1 << 62, 20, None)
+    assert rc == 4
+    assert b"static array" in lib.qg_last_error()
