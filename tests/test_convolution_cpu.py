@@ -22,3 +22,31 @@ def test_parameter_layout():
     assert conv.qubits == 5
     params = list(conv.parameters())
     assert len(params) == 15 and all(p.dtype == torch.float32 for p in params)
+
+
+def test_patch_layout_and_scaling_equal_the_reference():
+    """With the reference's own circuit in place of the engine (CPU, torch),
+    QConv's patch gather, shift, channel slice, scale and output layout give
+    the reference QConv's output exactly -- also with all-zero patches."""
+    import os
+
+    from oracle import reference_torch as rt
+
+    src = "/root/reference/src"
+    path = src if os.path.isdir(os.path.join(src, "qandle")) else rt.REF_DIR
+    if rt.unavailable_reason(path):
+        pytest.skip(rt.unavailable_reason(path))
+    qandle = rt.import_reference(path)
+    torch.manual_seed(0)
+    ref = qandle.QConv(in_channels=2, out_channels=3, kernel_size=3, padding=1)
+    for m in ref.qcircuit.circuit.layers[1].mods:
+        m.remapping = q.remap.none  # the stand-in has no tanh; parity uses remapping=None
+    mine = q.QConv(in_channels=2, out_channels=3, kernel_size=3, padding=1, engine="plain")
+    mine.load_state_dict(ref.state_dict(), strict=True)
+    mine.qcircuit = ref.qcircuit
+    x = torch.rand(2, 2, 5, 6)
+    x[:, :, :2, :2] = 0
+    with torch.no_grad():
+        a, b = mine(x), ref(x)
+    assert a.shape == b.shape == (2, 3, 5, 6)
+    assert torch.equal(a, b)
