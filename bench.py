@@ -55,6 +55,9 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
 
+EXTRAS = ("graph", "plain", "config1", "adjoint", "deep28", "sweep", "autotune", "serving")
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -62,9 +65,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="headline only")
-    ap.add_argument("--no-sweep", action="store_true", help="skip the fusion-width sweep")
-    ap.add_argument("--no-autotune", action="store_true", help="skip the autotuner record")
-    ap.add_argument("--no-serving", action="store_true", help="skip the serving runs")
+    ap.add_argument("--extras", default=",".join(EXTRAS),
+                    help="comma-separated records after the headline (default: all of " + ",".join(EXTRAS) + ")")
+    ap.add_argument("--adjoint-batch", type=int, default=1024)
     ap.add_argument("--cpu-samples", type=int, default=16, help="samples in the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines (profiling runs)")
     ap.add_argument("--tile-bits", type=int, default=13)
@@ -82,7 +85,12 @@ def parse():
                     help="run the prebuilt op interpreter instead of the per-program compiled passes")
     ap.add_argument("--n", type=int, default=20)
     ap.add_argument("--batch", type=int, default=256)
-    return ap.parse_args()
+    args = ap.parse_args()
+    args.extras = set() if args.no_extras else {e for e in args.extras.split(",") if e}
+    unknown = args.extras - set(EXTRAS)
+    if unknown:
+        ap.error(f"unknown extras {sorted(unknown)}")
+    return args
 
 
 def peaks():
@@ -513,7 +521,9 @@ def main():
                    "captured": any(b.graph is not None for b in circ._executor._bounds.values())}
     oracle_err = {}
 
-    if not args.no_extras:
+    ext = args.extras
+    gpu_ms_small = None
+    if "graph" in ext:
         # ---------------- one CUDA graph per forward ----------------
         bound.capture()
         for _ in range(W):
@@ -529,8 +539,9 @@ def main():
         gms = g0.elapsed_time(g1) / K
         line["graph"] = {"value": amp_step / (gms * 1e-3), "ms_per_step": gms,
                          "max_abs_diff_vs_launch": float((bound.result() - headline_out).abs().max())}
-        del bound
+    del bound
 
+    if "plain" in ext:
         # ---------------- plain per-gate form, same workload ----------------
         circ_p = workloads.build_circuit(desc, engine="plain").to(dev)
         with torch.no_grad():
@@ -551,35 +562,36 @@ def main():
         del circ_p, ref_out
         torch.cuda.empty_cache()
 
+    if "config1" in ext:
         # ---------------- config 1: 8 qubits x 64, plain method ----------------
         line["config1"], gpu_ms_small = bench_config1(dev, sync_all, oracle_err)
 
+    if "adjoint" in ext:
         # ---------------- adjoint: 16 qubits x batch 1024, MSE(<Z>, t) ----------------
-        line["adjoint"] = bench_adjoint(dev, sync_all, W, hbm_peak, fp32["tflops"], oracle_err)
+        line["adjoint"] = bench_adjoint(dev, sync_all, W, hbm_peak, fp32["tflops"], oracle_err, args.adjoint_batch)
         torch.cuda.empty_cache()
 
+    if "deep28" in ext:
         # ---------------- deep single state: 28 qubits x batch 1 ----------------
         line["deep28"] = bench_deep(dev, sync_all, W, oracle_err)
         torch.cuda.empty_cache()
 
-        # ---------------- fusion width sweep, autotuner ----------------
-        if not args.no_sweep:
-            line["k_sweep"] = bench_k_sweep(desc, kw, dev, sync_all, amp_step, ms)
-            torch.cuda.empty_cache()
-        if not args.no_autotune:
-            line["autotune"] = bench_autotune(desc, dev, amp_step, ms)
-            torch.cuda.empty_cache()
+    # ---------------- fusion width sweep, autotuner ----------------
+    if "sweep" in ext:
+        line["k_sweep"] = bench_k_sweep(desc, kw, dev, sync_all, amp_step, ms)
+        torch.cuda.empty_cache()
+    if "autotune" in ext:
+        line["autotune"] = bench_autotune(desc, dev, amp_step, ms)
+        torch.cuda.empty_cache()
 
+    if "serving" in ext:
         # ---------------- serving: Poisson arrivals of mixed-width requests ----------------
-        if not args.no_serving:
-            line["serving"] = {
-                "high_rate": bench_serving(dev, args.serving_requests, args.serving_rate, seed=7,
-                                           oracle_err=oracle_err),
-                "low_rate": bench_serving(dev, args.serving_low_requests, args.serving_low_rate, seed=8,
-                                          oracle_err=oracle_err)}
-            torch.cuda.empty_cache()
-    else:
-        gpu_ms_small = None
+        line["serving"] = {
+            "high_rate": bench_serving(dev, args.serving_requests, args.serving_rate, seed=7,
+                                       oracle_err=oracle_err),
+            "low_rate": bench_serving(dev, args.serving_low_requests, args.serving_low_rate, seed=8,
+                                      oracle_err=oracle_err)}
+        torch.cuda.empty_cache()
 
     if rank == 0:
         if args.no_cpu:
@@ -718,6 +730,8 @@ def bench_k_sweep(desc, kw, dev, sync_all, amp_step, headline_ms):
     sweep = {}
     for k in range(1, 7):
         c = workloads.build_circuit(desc, engine="fused", max_high=k, graphs=False).to(dev)
+        with torch.no_grad():
+            c(**kw)  # plans and compiles the k-limited program
         bk = engine.BoundForward(c._executor, desc["batch"], dev)
         bk.set_inputs(**kw)
         bk.launch()
@@ -834,14 +848,14 @@ def bench_serving(dev, count: int, rate: float, seed: int, oracle_err: dict):
             "max_abs_diff_vs_per_gate": diff[0], "max_abs_err_vs_oracle_n_le_14": err}
 
 
-def bench_adjoint(dev, sync_all, W, hbm_peak, fp32_tflops, oracle_err):
+def bench_adjoint(dev, sync_all, W, hbm_peak, fp32_tflops, oracle_err, batch: int = 1024):
     import torch
 
     import qandle_gb300 as q
     from oracle import oracle
     from qandle_gb300 import plain, workloads
 
-    desc = workloads.adjoint_brick()
+    desc = workloads.adjoint_brick(batch=batch)
     desc["measure"] = "p0"
     n, B = desc["n"], desc["batch"]
     targets = torch.tensor(desc["targets"], device=dev)

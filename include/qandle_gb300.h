@@ -323,7 +323,9 @@ int qg_program_finish(const qg_program* prog, const void* dev_table, void* works
 
 /* Status word of a program workspace after the work queued on `stream`: QG_OK,
  * or QG_ETIMEOUT when a pass kernel's bounded wait on a producer / compute
- * hand-off ran out (its results are then invalid).  Synchronises the stream.
+ * hand-off ran out (its results are then invalid; qg_last_error() names the
+ * wait that gave up, its block and tile: the workspace's first 16 bytes hold
+ * status, site, block, tile).  Synchronises the stream.
  * (No reference counterpart: the reference runs no asynchronous kernels.) */
 int qg_workspace_status(const void* workspace, void* stream);
 

@@ -78,6 +78,7 @@ __device__ __forceinline__ void bwd_producer(const PassDesc& d, const RunArgs& A
     const int64_t t0 = blockIdx.x;
     const int64_t mine = (num_tiles - t0 + G - 1) / G;
     bool failed = false;
+    int64_t failed_tile = -1;
     for (int64_t i = 0; i < mine + 2; ++i) {
         const int s = (int)(i & 1);
         float2* ps = pbuf0 + s * 2 * AMPS;
@@ -89,6 +90,7 @@ __device__ __forceinline__ void bwd_producer(const PassDesc& d, const RunArgs& A
             const bool released = mbar_wait(bar_empty + s, (uint32_t)((i / 2 - 1) & 1));
             if (!__all_sync(0xffffffffu, released)) {
                 failed = true;
+                failed_tile = t0 + (i - 2) * G;
                 break;
             }
             if (store_psi || store_lam) {
@@ -138,7 +140,7 @@ __device__ __forceinline__ void bwd_producer(const PassDesc& d, const RunArgs& A
         }
     }
     bulk_wait_all0();  // this lane's stores have completed before it leaves
-    if (failed && lane == 0) atomicExch(A.status, kStatusTimeout);
+    if (failed && lane == 0) report_timeout(A.status, kSiteBwdProducer, failed_tile);
 }
 
 // Body of the backward pass kernel: psi and lambda tiles, gradient partials.
@@ -196,6 +198,7 @@ __device__ __forceinline__ void bwd_pass_body(const PassDesc* __restrict__ passe
     cta_sync<NT>();
     int iter = 0;
     bool ok = true;
+    int64_t failed_tile = -1;
     for (int64_t t = blockIdx.x; t < num_tiles; t += gridDim.x, ++iter) {
         const int slot = iter & 1;
         float2* ps = pbuf0 + slot * 2 * AMPS;
@@ -203,6 +206,7 @@ __device__ __forceinline__ void bwd_pass_body(const PassDesc* __restrict__ passe
         const bool landed = mbar_wait(bar_full + slot, (uint32_t)((iter >> 1) & 1));
         if (!cta_sync_and<NT>(landed)) {
             ok = false;
+            failed_tile = t;
             break;
         }
         const TileGeo g = s_geo[slot];
@@ -242,7 +246,7 @@ __device__ __forceinline__ void bwd_pass_body(const PassDesc* __restrict__ passe
         __syncwarp();
         if ((tid & 31) == 0) mbar_arrive(bar_empty + slot);
     }
-    if (!ok && tid == 0) atomicExch(A.status, kStatusTimeout);
+    if (!ok && tid == 0) report_timeout(A.status, kSiteBwdCompute, failed_tile);
 }
 
 }  // namespace qg

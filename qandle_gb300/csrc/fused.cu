@@ -767,14 +767,17 @@ int qg_program_finish(const qg_program* prog, const void* dev_table, void* works
 
 int qg_workspace_status(const void* workspace, void* stream) {
     QG_CHECK_ARG(workspace, "null pointer");
-    int h = 0;
+    int h[4] = {0, 0, 0, 0};  // status, wait site, block, tile
     cudaStream_t st = (cudaStream_t)stream;
-    QG_CUDA_TRY(cudaMemcpyAsync(&h, workspace, sizeof(int), cudaMemcpyDeviceToHost, st));
+    QG_CUDA_TRY(cudaMemcpyAsync(h, workspace, sizeof(h), cudaMemcpyDeviceToHost, st));
     QG_CUDA_TRY(cudaStreamSynchronize(st));
-    if (h == 0) return QG_OK;
-    qg::set_error(h == QG_ETIMEOUT ? "a kernel wait timed out (a producer / compute hand-off never completed)"
-                                   : "a kernel reported an error status");
-    return h;
+    if (h[0] == 0) return QG_OK;
+    qg::set_error(h[0] == QG_ETIMEOUT
+                      ? "a kernel wait timed out (a producer / compute hand-off never completed): wait site " +
+                            std::to_string(h[1]) + ", block " + std::to_string(h[2]) + ", tile " +
+                            std::to_string(h[3])
+                      : "a kernel reported an error status");
+    return h[0];
 }
 
 int64_t qg_fp32_probe_blocks(void) { return (int64_t)qg::sm_count() * 4; }

@@ -90,11 +90,31 @@ constexpr uint64_t kWaitNs = 2000000000ull;
 __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, uint64_t limit_ns = kWaitNs) {
     if (mbar_try_wait(b, parity)) return true;
     const uint64_t t0 = global_ns();
-    for (uint32_t i = 1; i < (1u << 16); ++i) {
+    // the time limit ends the wait; the try count is a second bound in case
+    // the timer stalls (a try may return at once instead of suspending, so the
+    // count is set high enough never to end a wait before the time limit)
+    for (uint32_t i = 1; i < (1u << 26); ++i) {
         if (mbar_try_wait(b, parity)) return true;
         if (global_ns() - t0 > limit_ns) return false;
     }
     return false;
+}
+
+// Where a bounded wait gave up, recorded next to the status word (the
+// workspace's first 16 bytes: status, site, block, tile) by the first CTA
+// that reports a timeout.
+enum WaitSite : int {
+    kSiteFwdProducer = 1,  // forward producer, waiting for a buffer to be released
+    kSiteFwdCompute = 2,   // forward compute warps, waiting for a tile to land
+    kSiteBwdProducer = 5,  // backward producer / compute warps
+    kSiteBwdCompute = 6,
+};
+__device__ __forceinline__ void report_timeout(int* status, int site, int64_t tile) {
+    if (atomicExch(status, kStatusTimeout) == 0) {
+        status[1] = site;
+        status[2] = (int)blockIdx.x;
+        status[3] = (int)tile;
+    }
 }
 
 // ------------------------------------------------------- tile geometry --
@@ -495,6 +515,7 @@ __device__ __forceinline__ void fwd_producer(const JobTable<MAXJ>& jt, float2* b
     constexpr int KB = ((1 << (TB - 6)) + PT - 1) / PT;
     uint32_t st_off[KB], ld_off[KB];
     int failed_job = -1;
+    int64_t failed_tile = -1;
     for (int64_t i = 0; i < mine + S; ++i) {
         const int s = (int)(i % S);
         float2* buf = bufs + s * AMPS;
@@ -504,6 +525,7 @@ __device__ __forceinline__ void fwd_producer(const JobTable<MAXJ>& jt, float2* b
             const bool released = mbar_wait(bar_empty + s, (uint32_t)((i / S - 1) & 1));
             if (!producer_sync_and<PT>(released)) {
                 failed_job = j;
+                failed_tile = t;
                 break;
             }
             if (st.job != j) {
@@ -574,7 +596,7 @@ __device__ __forceinline__ void fwd_producer(const JobTable<MAXJ>& jt, float2* b
         }
     }
     bulk_wait_all0();  // this thread's stores have completed before it leaves
-    if (failed_job >= 0 && lane == 0) atomicExch(jt.job[failed_job].A.status, kStatusTimeout);
+    if (failed_job >= 0 && ptid == 0) report_timeout(jt.job[failed_job].A.status, kSiteFwdProducer, failed_tile);
 }
 
 // Body of the forward pass kernel.  One persistent CTA per SM walks the tiles
@@ -622,6 +644,7 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
     int cur_job = -1;
     int iter = 0;
     bool ok = true;
+    int64_t failed_tile = -1;
     for (int64_t t = t0; t < total; t += G, ++iter) {
         const int slot = iter % S;
         float2* buf = bufs + slot * AMPS;
@@ -656,6 +679,7 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         const bool landed = mbar_wait(bar_full + slot, (uint32_t)((iter / S) & 1));
         if (!cta_sync_and<NT>(landed)) {
             ok = false;
+            failed_tile = t;
             break;
         }
         const TileGeo g = s_geo[slot];
@@ -808,7 +832,7 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         __syncwarp();
         if (lane == 0) mbar_arrive(bar_empty + slot);
     }
-    if (!ok && tid == 0) atomicExch(sa.status, kStatusTimeout);
+    if (!ok && tid == 0) report_timeout(sa.status, kSiteFwdCompute, failed_tile);
     if (tid < 32) bulk_wait_all0();  // probability stores have completed
 }
 

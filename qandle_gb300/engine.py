@@ -336,9 +336,10 @@ def check_status(workspace: torch.Tensor) -> None:
 class _StatusWatch:
     """Reads the pass kernels' status words without blocking the host.
 
-    After every fused forward or backward, the word at the start of the
-    call's workspace is copied on the same stream into a ring of pinned host
-    slots, and an event marks the copy.  Each later call first looks at the
+    After every fused forward or backward, the first 16 bytes of the call's
+    workspace (the status word and, after a timeout, where the wait gave up)
+    are copied on the same stream into a ring of pinned host slots, and an
+    event marks the copy.  Each later call first looks at the
     copies that have landed (oldest first, stopping at the first still in
     flight) and raises RuntimeError for a nonzero word: a pass kernel's
     bounded wait ran out, so that earlier call's results are invalid.  The
@@ -354,12 +355,17 @@ class _StatusWatch:
         self._free = list(range(self.RING))
         self._lock = threading.Lock()
 
+    # where a wait gave up (the kernels' wait-site codes)
+    SITES = {1: "forward producer", 2: "forward compute warps", 5: "backward producer",
+             6: "backward compute warps"}
+
     def _take(self, slot, ev, what):
-        v = int(self._host[slot])
+        v, site, block, tile = (int(x) for x in self._host[slot])
         self._free.append(slot)
         if v != 0:
             raise RuntimeError(f"a fused {what} reported status {v}: a pass kernel's wait timed out "
-                               "(a producer / compute hand-off never completed); its results are invalid")
+                               f"({self.SITES.get(site, site)}, block {block}, tile {tile}: a producer / "
+                               "compute hand-off never completed); its results are invalid")
 
     def poll(self) -> None:
         with self._lock:
@@ -369,7 +375,7 @@ class _StatusWatch:
     def record(self, workspace: torch.Tensor, what: str) -> None:
         with self._lock:
             if self._host is None:
-                self._host = torch.zeros(self.RING, dtype=torch.int32, pin_memory=True)
+                self._host = torch.zeros(self.RING, 4, dtype=torch.int32, pin_memory=True)
             while self._pending and self._pending[0][1].query():
                 self._take(*self._pending.popleft())
             if not self._free:
@@ -377,7 +383,7 @@ class _StatusWatch:
                 ev.synchronize()
                 self._take(slot, ev, w)
             slot = self._free.pop()
-            self._host[slot:slot + 1].copy_(workspace[:4].view(torch.int32), non_blocking=True)
+            self._host[slot].copy_(workspace[:16].view(torch.int32), non_blocking=True)
             ev = torch.cuda.Event()
             ev.record()
             self._pending.append((slot, ev, what))
@@ -537,6 +543,16 @@ def _out_shape(measure, out, n, unbatched):
     return out
 
 
+def _event_handles(events):
+    """cudaEvent_t handles of torch CUDA events, as a ctypes array (torch
+    creates an event's handle at its first record, so unrecorded events are
+    recorded once on the current stream first)."""
+    for e in events:
+        if not e.cuda_event:
+            e.record()
+    return (ctypes.c_void_p * len(events))(*[e.cuda_event for e in events])
+
+
 class _FusedRun(torch.autograd.Function):
     # grad mode is off inside forward: the caller decides whether to keep the
     # final state for the backward (`prog` is the training or inference plan)
@@ -645,11 +661,9 @@ class FusedExecutor:
         b.set_from(inp, state)
         if b.graph is None:
             b.capture()
-        b.replay()
+        b.replay()  # records the status word
         if _CHECK_STATUS:
             check_status(b.ws)
-        else:
-            STATUS.record(b.ws, "forward")
         return b.out.clone()
 
     def _has_embedding(self) -> bool:
@@ -732,7 +746,7 @@ class FusedExecutor:
         if events is not None:
             # one backward records an event pair around every backward pass
             self.backward_events = None
-            evp = (ctypes.c_void_p * len(events))(*[e.cuda_event for e in events])
+            evp = _event_handles(events)
         _lib.call("qg_program_backward_timed", prog.handle, prog.table(dev).data_ptr(), ws.data_ptr(), ws.numel(),
                   st.data_ptr(), lam.data_ptr(), B, params.data_ptr(), named.data_ptr(), umats.data_ptr(),
                   g.data_ptr(), dparams.data_ptr(), dnamed.data_ptr(), _lib.ptr(dstate),
@@ -809,14 +823,18 @@ class BoundForward:
             if state is not None:
                 self.state.copy_(state.reshape(-1, 1 << self.n).expand(self.batch, -1))
 
-    def launch(self, events=None) -> None:
+    def launch(self, events=None, record_status: bool = True) -> None:
         evp = None
         if events is not None:
-            evp = (ctypes.c_void_p * len(events))(*[e.cuda_event for e in events])
+            evp = _event_handles(events)
+        if record_status:  # (not while a graph is being captured)
+            STATUS.poll()
         _lib.call("qg_program_forward_timed", self.prog.handle, self.table.data_ptr(), self.ws.data_ptr(),
                   self.ws.numel(), self.state.data_ptr(), self.batch, self.zero_init, self.params.data_ptr(),
                   self.named.data_ptr(), self.umats.data_ptr(), _lib.ptr(self.out), None, evp,
                   _lib.stream())
+        if record_status:
+            STATUS.record(self.ws, "forward")
 
     def capture(self) -> None:
         s = torch.cuda.Stream(device=self.device)
@@ -826,10 +844,12 @@ class BoundForward:
         torch.cuda.current_stream(self.device).wait_stream(s)
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
-            self.launch()
+            self.launch(record_status=False)
 
     def replay(self) -> None:
+        STATUS.poll()
         self.graph.replay()
+        STATUS.record(self.ws, "forward")
 
     def result(self) -> torch.Tensor:
         return self.state if self.out is None else self.out

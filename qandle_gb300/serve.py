@@ -252,8 +252,10 @@ class Server:
                     chunk = active[base:base + _lib.MAX_JOBS]
                     jobs = (_lib.Job * len(chunk))()
                     for i, s in enumerate(chunk):
+                        # a program without an embedding starts from |0..0> in its first pass
+                        zero = 1 if (s.next_pass == 0 and not s.prog.info.has_embedding) else 0
                         jobs[i] = _lib.Job(s.prog.handle, s.prog.table(self.device).data_ptr(), s.ws.data_ptr(),
-                                           s.ws.numel(), s.state.data_ptr(), s.batch, s.next_pass, 0,
+                                           s.ws.numel(), s.state.data_ptr(), s.batch, s.next_pass, zero,
                                            s.out.data_ptr())
                     _lib.check(lib.qg_jobs_run_pass(jobs, len(chunk), self.stream.cuda_stream))
                     self.launches += 1
