@@ -40,6 +40,26 @@ __host__ __device__ constexpr int fwd_min_blocks(int tb, int rb) {
     return tb >= 13 ? 1 : tb == 12 ? 2 : 3;
 }
 
+// Shared-memory swizzle of the exchanges.  The exchange planes hold 2^TB
+// floats; local index j goes to slot j ^ L(j >> 5), where L XORs into the low
+// five bits (the 4-byte bank) the image swz_image(k) of every set high bit
+// 5 + k.  Local bit b < 5 has image 1 << b.  A warp's exchange access is free
+// of bank conflicts when its five lane bits have independent images; the
+// images below leave independent lane choices after taking out the register
+// bits for all but 3 of the 1287 register sets of a 2^13 tile with 5
+// register bits (1 of 495 at 2^12 with 4), where bank = (b mod 5) left 450.
+__host__ __device__ constexpr int swz_image(int k) {
+    return k == 0 ? 14 : k == 1 ? 25 : k == 2 ? 7 : k == 3 ? 26 : k == 4 ? 19 : k == 5 ? 31 : k == 6 ? 22 : 11;
+}
+// Bank image of local bit b (the low five bits of its slot offset).
+__host__ __device__ constexpr int bank_image(int b) { return b < 5 ? (1 << b) : swz_image(b - 5); }
+__host__ __device__ constexpr int swz_slot(int j) {
+    int h = j >> 5, x = 0;
+    for (int k = 0; k < 8; ++k)
+        if ((h >> k) & 1) x ^= swz_image(k);
+    return j ^ x;
+}
+
 // Device op codes (int4 per op: x = opcode, y/z/w operands).
 enum Opcode : int32_t {
     OP_MAP = 1,   // exchange through shared memory to a new register/lane/warp mapping

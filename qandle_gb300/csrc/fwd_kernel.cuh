@@ -119,10 +119,11 @@ __device__ __forceinline__ void report_timeout(int* status, int site, int64_t ti
 
 // ------------------------------------------------------- tile geometry --
 
-// Swizzled shared-memory slot of local index j: the low 5 bits are XORed with
-// the 5-bit groups above them, so 32 lanes whose local bits have distinct
-// (bit mod 5) hit the 32 distinct 4-byte banks of a planar exchange.
-__device__ __forceinline__ int swz(int j) { return j ^ (((j >> 5) ^ (j >> 10)) & 31); }
+// Swizzled shared-memory slot of local index j in an exchange plane (see
+// swz_slot in engine.h: the bank bits take the XOR of the images of the high
+// bits, so lanes whose local bits have independent images hit 32 distinct
+// banks).
+__device__ __forceinline__ int swz(int j) { return swz_slot(j); }
 
 struct TileGeo {
     int64_t sample;       // first sample of the tile

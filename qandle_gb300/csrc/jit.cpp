@@ -183,7 +183,7 @@ void natural_mapping(int tb, int rb, int32_t& y, int32_t& z, int32_t& w) {
     w |= (tb - 5 - rb) << 16;
 }
 
-int swz_host(int j) { return j ^ (((j >> 5) ^ (j >> 10)) & 31); }
+int swz_host(int j) { return swz_slot(j); }
 
 // "C0, C1, C2, C3, C4": slot offsets of the register bits under a mapping.
 std::string reg_offsets(const MapBits& m, int rb) {

@@ -296,12 +296,16 @@ Mapping mapping_for(uint32_t R, int tb, int rb) {
     for (int b = 0; b < tb; ++b)
         if (!(R & (1u << b))) rest.push_back(b);
     std::vector<int> lanes;
-    int used = 0;
+    // lanes whose bank images (engine.h, bank_image) are linearly independent
+    // over GF(2), in ascending local-bit order: kept as a reduced basis
+    std::vector<int> basis;
     for (int b : rest) {
-        int cls = b % 5;  // swizzle image of local bit b is e_(b mod 5)
-        if ((int)lanes.size() < 5 && !(used & (1 << cls))) {
+        if ((int)lanes.size() >= 5) break;
+        int v = qg::bank_image(b);
+        for (int e : basis) v = std::min(v, v ^ e);
+        if (v) {
+            basis.push_back(v);
             lanes.push_back(b);
-            used |= 1 << cls;
         }
     }
     for (int b : rest)
