@@ -603,8 +603,9 @@ def main():
             oracle_err["config2_z_first_%d_samples" % args.cpu_samples] = float(np.abs(got - ref).max())
             line["reference_torch"] = reference_torch_baseline(gpu_ms_small)
         line["oracle_error"] = dict(oracle_err, tolerance=1e-5,
-                                    note="max-abs against the complex128 oracle on the same seeded inputs; "
-                                         "probabilities, P0 and <Z> within 1e-5, gradients within 1e-4")
+                                    note="max-abs against the complex128 oracle on the same seeded inputs; the "
+                                         "bar is 1e-5 on probabilities and P0 (<Z> = 2 P0 - 1 doubles the P0 "
+                                         "error), 1e-4 on gradients")
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.barrier()
@@ -936,8 +937,10 @@ def bench_adjoint(dev, sync_all, W, hbm_peak, fp32_tflops, oracle_err, batch: in
     p0_ref = oracle.forward(small)
     _, gref = oracle.mse_z_grad(2.0 * p0_ref - 1.0, small["targets"].astype(np.float64))
     rdp, _, _ = oracle.adjoint(small, gref, "p0")
+    p_err = float(np.abs(pz.detach().cpu().numpy() - p0_ref).max())
     z_err = float(np.abs((2.0 * pz.detach().cpu().numpy() - 1.0) - (2.0 * p0_ref - 1.0)).max())
     g_err = float(np.abs(dth - rdp).max())
+    oracle_err["config3_p0_8_samples"] = p_err
     oracle_err["config3_z_8_samples"] = z_err
     oracle_err["config3_grad_8_samples"] = g_err
 
@@ -961,7 +964,7 @@ def bench_adjoint(dev, sync_all, W, hbm_peak, fp32_tflops, oracle_err, batch: in
                          "fp32_frac": float(2.0 * bfmas.sum() / (bms.sum() * 1e-3) / (fp32_tflops * 1e12)),
                          "combined_frac": comb,
                          "passes_fp32_bound": int(np.sum(t_fp > t_mem))},
-            "max_abs_err_vs_oracle_8_samples": {"z": z_err, "grad": g_err},
+            "max_abs_err_vs_oracle_8_samples": {"p0": p_err, "z": z_err, "grad": g_err},
             "note": "step = forward + backward; amp-updates count each gate once forward and twice "
                     "backward (state and cotangent)"}
 

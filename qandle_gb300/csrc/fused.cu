@@ -198,6 +198,10 @@ __device__ __forceinline__ float pgrad_op(const PTile<RB>& ps, const PTile<RB>& 
 // (the prebuilt kernels; the compiled pass kernels of jit.cpp unroll it).
 struct InterpOps {
     static constexpr bool kStageOps = true;
+    // init, epilogue and end mapping come from the pass descriptor at run time
+    static constexpr int kInit = -1;
+    static constexpr int kEpi = -1;
+    static constexpr int kEndNatural = -1;
     static constexpr uint32_t kStagedBytes = 0;
     __device__ __forceinline__ static void stage(const RunArgs&, const TileGeo&, float4*, uint64_t*, int) {}
     template <int TB, int RB>

@@ -673,7 +673,11 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         const RunArgs& A = sa;
         const int4* ops = jt.job[j].ops;
         const int n = A.n;
-        const bool load_in = d.init == INIT_LOAD && !jt.job[j].zero_init;
+        // a compiled pass knows its init and epilogue kinds (Ops::kInit / kEpi
+        // >= 0): the code of the other kinds is not compiled into it
+        const int init = Ops::kInit >= 0 ? Ops::kInit : d.init;
+        const int epi = Ops::kEpi >= 0 ? Ops::kEpi : d.epi;
+        const bool load_in = init == INIT_LOAD && !jt.job[j].zero_init;
         // the tile's per-sample matrices (compiled passes) in the buffer's
         // share of the op-list area
         const float4* const staged = reinterpret_cast<const float4*>(s_ops) + slot * (2 * kStagedPerSlot);
@@ -691,12 +695,12 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
             pload_nat<RB>(pt, buf, tid);
             decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
         } else {
-            if (d.init == INIT_EMBED)
+            if (init == INIT_EMBED)
                 decode_map<RB>(d, d.init_map[0], d.init_map[1], d.init_map[2], tid, g.fixed_val, tm);
             else
                 decode_map<RB>(d, NatMap<TB, RB>::y, NatMap<TB, RB>::z, NatMap<TB, RB>::w, tid, g.fixed_val, tm);
             int64_t smp = g.sample + tm.sample_off;
-            if (d.init == INIT_EMBED && smp < A.batch) {
+            if (init == INIT_EMBED && smp < A.batch) {
                 // amplitude = prod over qubits of the per-sample factor of its bit
                 const float2* fac = A.embfac + smp * n * 2;
                 float2 c = make_float2(1.f, 0.f);
@@ -720,7 +724,7 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 }
 #pragma unroll
                 for (int r = 0; r < (1 << RB); ++r) set_amp<RB>(pt, r, a[r]);
-            } else if (d.init == INIT_EMBED) {
+            } else if (init == INIT_EMBED) {
 #pragma unroll
                 for (int r = 0; r < (1 << RB); ++r) set_amp<RB>(pt, r, make_float2(0.f, 0.f));
             } else {
@@ -741,11 +745,11 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         // ---- epilogue (the planner left the natural mapping, or for a pass
         // that only stores, a mapping with natural lanes: d.end_map) ----
         const int64_t smp0 = g.sample;
-        if (d.epi & (EPI_PROBS | EPI_P0)) {
+        if (epi & (EPI_PROBS | EPI_P0)) {
             cta_sync<NT>();  // all exchange reads of `buf` are done
             float* pb = reinterpret_cast<float*>(buf);
             pstore_probs<RB>(pt, pb, tid, xm);
-            if (d.epi & EPI_PROBS) {
+            if (epi & EPI_PROBS) {
                 fence_proxy_async();
                 cta_sync<NT>();
                 if (tid < 32) {
@@ -755,7 +759,7 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 }
             }
             cta_sync<NT>();
-            if (d.epi & EPI_P0) {
+            if (epi & EPI_P0) {
                 // phase A: thread t owns the 2^RB consecutive probabilities of chunk t
                 constexpr int CH = 1 << RB;
                 float* ptot = pb + AMPS;          // [NT]
@@ -819,9 +823,12 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 }
             }
         }
-        if (d.epi & EPI_STORE) {
+        if (epi & EPI_STORE) {
             cta_sync<NT>();  // all reads of `buf` (exchanges, probabilities) are done
-            if (d.end_map[0] == NatMap<TB, RB>::y && d.end_map[2] == NatMap<TB, RB>::w)
+            const bool nat_end = Ops::kEndNatural >= 0
+                                     ? Ops::kEndNatural == 1
+                                     : (d.end_map[0] == NatMap<TB, RB>::y && d.end_map[2] == NatMap<TB, RB>::w);
+            if (nat_end)
                 pstore_nat<RB>(pt, buf, tid, xm);
             else
                 pstore_map<RB>(pt, buf, d.end_map, tid, xm);

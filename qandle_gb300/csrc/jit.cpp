@@ -259,11 +259,17 @@ std::string pass_source(const ProgramRun& R, int p) {
             staged_index.clear();
         }
     }
+    int32_t ny, nz, nw;
+    natural_mapping(tb, rb, ny, nz, nw);
+    const int end_natural = (d.end_map[0] == ny && d.end_map[2] == nw) ? 1 : 0;
     std::ostringstream s;
     s << "#include \"jit_ops.cuh\"\n"
          "namespace qg {\n"
          "struct PassOps {\n"
          "  static constexpr bool kStageOps = false;\n"
+      << "  static constexpr int kInit = " << d.init << ";\n"
+      << "  static constexpr int kEpi = " << d.epi << ";\n"
+      << "  static constexpr int kEndNatural = " << end_natural << ";\n"
       << "  static constexpr uint32_t kStagedBytes = " << 32 * staged.size() << ";\n"
          "  __device__ __forceinline__ static void stage(const RunArgs& A, const TileGeo& g, float4* sm, "
          "uint64_t* bar, int lane) {\n";
