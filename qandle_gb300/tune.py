@@ -41,6 +41,7 @@ DEFAULT_CANDIDATES: typing.List[dict] = [
     dict(tile_bits=12, low_bits=7, reg_bits=5),
     dict(tile_bits=13, low_bits=7, reg_bits=5),
     dict(tile_bits=12, low_bits=6, reg_bits=4),
+    dict(tile_bits=13, low_bits=6, reg_bits=4),
 ]
 
 
