@@ -9,8 +9,9 @@
   few samples, against the oracle's adjoint gradient;
 * an OpenQASM 3 request (the serving wire format) through the serving loop,
   against the oracle;
-* INTEGRATION.md's per-circuit snippet on a circuit of the reference's own
-  classes, against the reference's torch forward and autograd.
+* the per-circuit binding a qandle maintainer adds (FusedExecutor injected
+  into a circuit of the reference's own classes), against the reference's
+  torch forward and autograd.
 """
 import numpy as np
 import pytest
@@ -170,7 +171,7 @@ def test_qasm_request_through_server(cuda_device):
 
 
 def test_integration_snippet_on_reference_circuit(cuda_device):
-    """INTEGRATION.md section 2 run as written, on a circuit built from the
+    """The per-circuit binding as a qandle maintainer writes it, on a circuit built from the
     reference's own classes (qandle 0.1.8 installed in baseline/_ref): the
     fused forward equals the reference's torch forward on the CPU, and the
     adjoint gradients equal the reference's torch autograd gradients."""

@@ -6,8 +6,9 @@ stand-in), as a qandle user writes them.  The fused engine lowers them
 (qandle/qcircuit.py:45-46 is the injection point) to exactly the gate records,
 angles and tables of the same circuit built with this package's classes; the
 planned program, executed by the CPU op emulator, reproduces the reference's
-own torch forward; and INTEGRATION.md's per-circuit snippet routes the
-reference's Circuit.forward into the fused executor."""
+own torch forward; and the per-circuit binding a qandle maintainer adds
+(the reference's Circuit.forward replaced by the fused executor) routes
+calls into the engine."""
 import os
 
 import numpy as np
@@ -93,7 +94,7 @@ def test_reference_circuit_plan_reproduces_reference_forward(qandle, name):
 
 
 def test_integration_snippet_routes_into_the_executor(qandle):
-    """the reference's Circuit keeps its object and
+    """The per-circuit binding: the reference's Circuit keeps its object and
     its forward now runs the fused executor (on a CPU tensor the executor
     refuses loudly instead of falling back to the reference's loop)."""
     desc = workloads.sel_reupload(n=8, batch=2, layers=2, reupload_every=1, measure="p0")
