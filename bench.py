@@ -588,7 +588,7 @@ def main():
         # ---------------- serving: Poisson arrivals of mixed-width requests ----------------
         line["serving"] = {
             "high_rate": bench_serving(dev, args.serving_requests, args.serving_rate, seed=7,
-                                       oracle_err=oracle_err),
+                                       oracle_err=oracle_err, policies=("srpt", "all")),
             "low_rate": bench_serving(dev, args.serving_low_requests, args.serving_low_rate, seed=8,
                                       oracle_err=oracle_err)}
         torch.cuda.empty_cache()
@@ -767,27 +767,15 @@ def bench_autotune(desc, dev, amp_step, default_ms):
             "timings_ms": [[o, round(t, 3)] for o, t in res["timings"]]}
 
 
-def bench_serving(dev, count: int, rate: float, seed: int, oracle_err: dict):
-    """Open-loop Poisson arrivals (`rate` per second) of `count` mixed
-    strongly-entangling requests: n ~ U{4..24}, depth ~ U{2..30}, batch
-    log-uniform in [1, 512], <Z> out.  Two live runs on the same arrival
-    times: the continuous-batching server, and a worker that serves the
-    requests one after another in arrival order with the plain per-gate form
-    (one launch per gate per request), starting each when it has arrived and
-    the previous one is done.  Both include their per-request preparation in
-    the latency (the server's lowering and planning, the per-gate form's
-    module construction)."""
+def _serve_live(dev, reqs, offs, amp, policy):
+    """One live run of the continuous-batching server on the given arrival
+    offsets; returns (stats, outputs)."""
     import torch
 
-    from oracle import oracle
-    from qandle_gb300 import serve, workloads
+    from qandle_gb300 import serve
 
-    rng = np.random.default_rng(seed)
-    reqs = [workloads.random_sel_request(rng) for _ in range(count)]
-    offs = np.concatenate([[0.0], np.cumsum(rng.exponential(1.0 / rate, size=count - 1))])
-    amp = float(sum(workloads.gate_count(d) * d["batch"] * (1 << d["n"]) for d in reqs))
-
-    srv = serve.Server(dev, hbm_budget=160 << 30)
+    count = len(reqs)
+    srv = serve.Server(dev, hbm_budget=160 << 30, policy=policy)
     try:
         t0 = time.perf_counter()
         handles = []
@@ -803,11 +791,41 @@ def bench_serving(dev, count: int, rate: float, seed: int, oracle_err: dict):
         srv.close()
     lat = np.array([h.latency for h in handles]) * 1e3
     span = t_end - t0
-    fused = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+    stats = {"policy": policy, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
              "circuits_per_s": count / span, "amp_updates_per_s": amp / span, "wall_s": span,
              "steps": steps, "launches": launches}
     del handles
     torch.cuda.empty_cache()
+    return stats, outs
+
+
+def bench_serving(dev, count: int, rate: float, seed: int, oracle_err: dict, policies=("srpt",)):
+    """Open-loop Poisson arrivals (`rate` per second) of `count` mixed
+    strongly-entangling requests: n ~ U{4..24}, depth ~ U{2..30}, batch
+    log-uniform in [1, 512], <Z> out.  Live runs on the same arrival times:
+    the continuous-batching server (with each scheduling policy asked for;
+    the first is the record's headline), and a worker that serves the
+    requests one after another in arrival order with the plain per-gate form
+    (one launch per gate per request), starting each when it has arrived and
+    the previous one is done.  Both include their per-request preparation in
+    the latency (the server's lowering and planning, the per-gate form's
+    module construction)."""
+    import torch
+
+    from oracle import oracle
+    from qandle_gb300 import serve, workloads
+
+    rng = np.random.default_rng(seed)
+    reqs = [workloads.random_sel_request(rng) for _ in range(count)]
+    offs = np.concatenate([[0.0], np.cumsum(rng.exponential(1.0 / rate, size=count - 1))])
+    amp = float(sum(workloads.gate_count(d) * d["batch"] * (1 << d["n"]) for d in reqs))
+
+    fused, outs = _serve_live(dev, reqs, offs, amp, policies[0])
+    others = {}
+    for pol in policies[1:]:
+        st, o2 = _serve_live(dev, reqs, offs, amp, pol)
+        st["max_abs_diff_vs_" + policies[0]] = max(float((a - b).abs().max()) for a, b in zip(outs, o2))
+        others[pol] = st
 
     # live per-gate FIFO on the same arrival times
     done_at = [None] * count
@@ -843,6 +861,7 @@ def bench_serving(dev, count: int, rate: float, seed: int, oracle_err: dict):
     return {"workload": f"{count} requests, Poisson {rate:g}/s, n ~ U{{4..24}}, depth ~ U{{2..30}}, "
                         f"batch log-uniform [1, 512], <Z> out (seed {seed})",
             "offered_s": float(offs[-1]), "amp_updates": amp, "continuous_batching": fused,
+            "continuous_batching_other_policies": others,
             "per_gate_fifo_live": plain,
             "throughput_ratio": fused["circuits_per_s"] / plain["circuits_per_s"],
             "p99_ratio_per_gate_over_batched": plain["p99_ms"] / fused["p99_ms"],

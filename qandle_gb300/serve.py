@@ -108,9 +108,20 @@ def structure_key(lo: Lowered):
     return (lo.n, lo.measure, tuple(lo.gates), tuple(lo.qlist))
 
 
+def _tiles_per_pass(n: int, batch: int, tile_bits: int) -> int:
+    """Tiles one pass of a request walks (the pass kernels' work unit)."""
+    if n >= tile_bits:
+        return batch << (n - tile_bits)
+    per_tile = 1 << (tile_bits - n)
+    return (batch + per_tile - 1) // per_tile
+
+
 class _Slot:
     __slots__ = ("req", "prog", "state", "ws", "out", "host_out", "batch", "next_pass", "bytes",
-                 "event", "params", "named", "umats", "shift")
+                 "event", "params", "named", "umats", "shift", "tiles", "idle")
+
+    def remaining(self) -> int:
+        return self.tiles * (self.prog.info.forward_passes - self.next_pass)
 
 
 class Request:
@@ -123,6 +134,7 @@ class Request:
         self.lowered = None   # (lowered, params, named, shift), set at submit
         self.prog = None
         self.need = 0         # device bytes while admitted
+        self.work = 0         # tiles over all passes (the scheduling key)
 
     @property
     def latency(self):
@@ -133,20 +145,40 @@ class Server:
     """Continuous-batching executor on one device.
 
     hbm_budget: device bytes the admitted requests may hold together (state,
-    workspace and output of each).  max_active: requests advanced per step (a
-    multiple of the 32 jobs one launch takes means several launches).
+    workspace and output of each).  max_active: requests admitted at once (a
+    step of more than the 32 jobs one launch takes is several launches).
+
+    policy "srpt" (default) schedules by shortest remaining work, counted in
+    pass tiles: admission takes the queued request with the least work that
+    fits the budget (a request queued longer than max_queue_wait_s goes
+    first), and each step advances the active requests with the least
+    remaining work until the step holds step_tiles tiles (at least one
+    request; a request left out for max_idle_steps steps is always taken).
+    Small requests then finish in a few short steps instead of sharing every
+    step with the largest ones.  policy "all" admits oldest first and
+    advances every active request every step.  Either way a request's result
+    does not depend on what else ran: the same kernel computes its tiles in
+    the same order.
     """
 
     def __init__(self, device="cuda", hbm_budget: int = 64 << 30, max_active: int = 64,
-                 tile_bits: int = 13, low_bits: int = 6):
+                 tile_bits: int = 13, low_bits: int = 6, policy: str = "srpt", step_tiles: int = 1 << 16,
+                 max_idle_steps: int = 64, max_queue_wait_s: float = 10.0):
+        if policy not in ("srpt", "all"):
+            raise ValueError(f"policy must be 'srpt' or 'all', got {policy!r}")
         self.device = torch.device(device)
         self.budget = int(hbm_budget)
         self.max_active = max_active
+        self.policy = policy
+        self.step_tiles = int(step_tiles)
+        self.max_idle_steps = int(max_idle_steps)
+        self.max_queue_wait_s = float(max_queue_wait_s)
+        self.tile_bits = tile_bits
         self.opts = dict(tile_bits=tile_bits, low_bits=low_bits)
         self.programs: dict = {}
         self._plock = threading.Lock()
         self.stream = torch.cuda.Stream(device=self.device)
-        self._queue = collections.deque()
+        self._queue = []
         self._cv = threading.Condition()
         self._stop = False
         self._completing = collections.deque()
@@ -168,6 +200,8 @@ class Server:
             req.future.set_exception(e)
             return req
         need = req.need = self._device_bytes(req)
+        lo = req.lowered[0]
+        req.work = _tiles_per_pass(lo.n, desc["batch"] or 1, self.tile_bits) * req.prog.info.forward_passes
         if need > self.budget:
             req.future.set_exception(MemoryError(
                 f"request needs {need} bytes of device memory (state, workspace, output), more than the "
@@ -214,6 +248,8 @@ class Server:
         s = _Slot()
         s.req, s.prog, s.batch, s.next_pass, s.shift = req, prog, B, 0, shift
         s.bytes = req.need
+        s.tiles = _tiles_per_pass(n, B, self.tile_bits)
+        s.idle = 0
         dev = self.device
         s.state = torch.empty(B, 1 << n, dtype=torch.complex64, device=dev)
         s.ws = prog.workspace(B, False, dev)
@@ -237,19 +273,18 @@ class Server:
                         self._cv.wait()
                     if self._stop and not self._queue and not active:
                         break
-                    # admit against the HBM budget, oldest first
                     while self._queue and len(active) < self.max_active:
-                        need = self._queue[0].need
-                        if self._used + need > self.budget:
+                        req = self._next_admission()
+                        if req is None:
                             break
-                        req = self._queue.popleft()
-                        self._used += need
+                        self._queue.remove(req)
+                        self._used += req.need
                         active.append(self._admit(req))
                 if not active:
                     continue
-                # one step: the next pass of every active request
-                for base in range(0, len(active), _lib.MAX_JOBS):
-                    chunk = active[base:base + _lib.MAX_JOBS]
+                step = self._step_selection(active)
+                for base in range(0, len(step), _lib.MAX_JOBS):
+                    chunk = step[base:base + _lib.MAX_JOBS]
                     jobs = (_lib.Job * len(chunk))()
                     for i, s in enumerate(chunk):
                         # a program without an embedding starts from |0..0> in its first pass
@@ -260,8 +295,14 @@ class Server:
                     _lib.check(lib.qg_jobs_run_pass(jobs, len(chunk), self.stream.cuda_stream))
                     self.launches += 1
                 self.steps += 1
+                stepped = set(id(s) for s in step)
                 still = []
                 for s in active:
+                    if id(s) not in stepped:
+                        s.idle += 1
+                        still.append(s)
+                        continue
+                    s.idle = 0
                     s.next_pass += 1
                     if s.next_pass < s.prog.info.forward_passes:
                         still.append(s)
@@ -276,6 +317,33 @@ class Server:
                         self._used -= s.bytes
                         self._completing.append(s)
                 active = still
+
+    def _next_admission(self):
+        """The queued request to admit next, or None when it does not fit the
+        budget now (called with the queue lock held)."""
+        if self.policy == "all":
+            req = self._queue[0]
+            return req if self._used + req.need <= self.budget else None
+        now = time.perf_counter()
+        oldest = self._queue[0]
+        if now - oldest.arrival > self.max_queue_wait_s:
+            # waited too long: it goes first, and nothing passes it
+            return oldest if self._used + oldest.need <= self.budget else None
+        fits = [r for r in self._queue if self._used + r.need <= self.budget]
+        return min(fits, key=lambda r: r.work) if fits else None
+
+    def _step_selection(self, active):
+        """Active requests whose next pass runs in this step."""
+        if self.policy == "all":
+            return list(active)
+        order = sorted(active, key=lambda s: s.remaining())
+        step, tiles = [], 0
+        for s in order:
+            if step and tiles + s.tiles > self.step_tiles and s.idle < self.max_idle_steps:
+                continue
+            step.append(s)
+            tiles += s.tiles
+        return step
 
     def _poll(self):
         while True:

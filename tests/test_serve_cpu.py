@@ -38,3 +38,65 @@ def test_qasm_request_lowers_like_its_description():
     from oracle import oracle
 
     assert np.abs(oracle.forward(req) - oracle.forward(desc)).max() < 1e-12
+
+
+class _Req:
+    def __init__(self, work, need, arrival):
+        self.work, self.need, self.arrival = work, need, arrival
+
+
+class _Prog:
+    class info:
+        forward_passes = 10
+
+
+class _Active:
+    def __init__(self, tiles, next_pass, idle=0):
+        self.tiles, self.next_pass, self.idle, self.prog = tiles, next_pass, idle, _Prog
+
+    def remaining(self):
+        return self.tiles * (self.prog.info.forward_passes - self.next_pass)
+
+
+def _server(policy="srpt", used=0, budget=100):
+    import types
+
+    return types.SimpleNamespace(policy=policy, _used=used, budget=budget, max_queue_wait_s=10.0,
+                                 step_tiles=100, max_idle_steps=4, _queue=[])
+
+
+def test_admission_takes_least_work_that_fits():
+    import time
+
+    now = time.perf_counter()
+    srv = _server(used=60)
+    big, small, too_big = _Req(500, 30, now), _Req(5, 10, now), _Req(1, 50, now)
+    srv._queue = [big, too_big, small]
+    assert serve.Server._next_admission(srv) is small      # least work among those that fit
+    srv._queue = [too_big]
+    assert serve.Server._next_admission(srv) is None        # nothing fits the budget now
+    old = _Req(900, 30, now - 11.0)
+    srv._queue = [old, small]
+    assert serve.Server._next_admission(srv) is old         # waited too long: goes first
+    srv = _server(policy="all", used=0)
+    srv._queue = [big, small]
+    assert serve.Server._next_admission(srv) is big        # oldest first
+
+
+def test_step_takes_least_remaining_work_up_to_the_tile_budget():
+    srv = _server()
+    a, b, c = _Active(tiles=60, next_pass=9), _Active(tiles=30, next_pass=0), _Active(tiles=500, next_pass=5)
+    step = serve.Server._step_selection(srv, [c, b, a])
+    assert step == [a, b]                                   # remaining 60, 300; c (2500) over the budget
+    c.idle = 4
+    assert c in serve.Server._step_selection(srv, [c, b, a])  # left out too long: taken
+    lone = _Active(tiles=1000, next_pass=0)
+    assert serve.Server._step_selection(srv, [lone]) == [lone]  # at least one request per step
+    srv = _server(policy="all")
+    assert serve.Server._step_selection(srv, [c, b, a]) == [c, b, a]
+
+
+def test_tiles_per_pass():
+    assert serve._tiles_per_pass(20, 3, 13) == 3 << 7
+    assert serve._tiles_per_pass(8, 33, 13) == 2             # 32 samples of 2^8 per 2^13 tile
+    assert serve._tiles_per_pass(13, 1, 13) == 1

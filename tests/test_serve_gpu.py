@@ -64,3 +64,21 @@ def test_budget_refuses_and_queues(cuda_device):
     ref = oracle.forward(big)
     for o in outs:
         assert np.abs(o.numpy() - ref).max() < 1e-5
+
+
+def test_policies_give_identical_results(cuda_device):
+    """Shortest-remaining-work scheduling (the default) and oldest-first
+    scheduling of every request each step run each request's tiles with the
+    same kernel in the same order: their results are bit-identical."""
+    reqs = _requests(count=10, seed=5)
+    outs = {}
+    for policy in ("srpt", "all"):
+        srv = serve.Server(cuda_device, hbm_budget=8 << 30, policy=policy, step_tiles=64)
+        try:
+            hs = [srv.submit(d) for d in reqs]
+            outs[policy] = [h.future.result(timeout=120) for h in hs]
+        finally:
+            srv.close()
+        assert srv.steps > 0
+    for d, a, b in zip(reqs, outs["srpt"], outs["all"]):
+        assert torch.equal(a, b), d["n"]
