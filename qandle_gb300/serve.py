@@ -163,7 +163,8 @@ class Server:
 
     def __init__(self, device="cuda", hbm_budget: int = 64 << 30, max_active: int = 64,
                  tile_bits: int = 13, low_bits: int = 6, policy: str = "srpt", step_tiles: int = 1 << 16,
-                 max_idle_steps: int = 64, max_queue_wait_s: float = 10.0):
+                 max_idle_steps: int = 64, max_queue_wait_s: float = 10.0, max_inflight_steps: int = 2,
+                 planning_threads: int = 4):
         if policy not in ("srpt", "all"):
             raise ValueError(f"policy must be 'srpt' or 'all', got {policy!r}")
         self.device = torch.device(device)
@@ -174,7 +175,12 @@ class Server:
         self.max_idle_steps = int(max_idle_steps)
         self.max_queue_wait_s = float(max_queue_wait_s)
         self.tile_bits = tile_bits
+        self.max_inflight_steps = max(1, int(max_inflight_steps))
         self.opts = dict(tile_bits=tile_bits, low_bits=low_bits)
+        # lowering and planning run off the caller's thread, several at once
+        # (the C planner releases the interpreter lock)
+        self._planner = cf.ThreadPoolExecutor(max_workers=max(1, int(planning_threads)))
+        self._planning: dict = {}  # structure key -> Future of its Program
         self.programs: dict = {}
         self._plock = threading.Lock()
         self.stream = torch.cuda.Stream(device=self.device)
@@ -192,27 +198,35 @@ class Server:
 
     # -- public --
     def submit(self, desc: dict, arrival: float | None = None) -> Request:
+        """Queue one request; returns at once.  Its lowering and planning run
+        on the planning threads; a request that cannot be served (a gate the
+        loop does not take, more memory than the whole budget) fails its
+        future instead of entering the queue."""
         req = Request(desc, arrival)
+        self._planner.submit(self._plan, req)
+        return req
+
+    def _plan(self, req: "Request") -> None:
         try:
-            req.lowered = lower_description(desc)
+            req.lowered = lower_description(req.desc)
             req.prog = self._program(req.lowered[0])
+            need = req.need = self._device_bytes(req)
+            lo = req.lowered[0]
+            req.work = _tiles_per_pass(lo.n, req.desc["batch"] or 1, self.tile_bits) * req.prog.info.forward_passes
         except (ValueError, RuntimeError) as e:
             req.future.set_exception(e)
-            return req
-        need = req.need = self._device_bytes(req)
-        lo = req.lowered[0]
-        req.work = _tiles_per_pass(lo.n, desc["batch"] or 1, self.tile_bits) * req.prog.info.forward_passes
+            return
         if need > self.budget:
             req.future.set_exception(MemoryError(
                 f"request needs {need} bytes of device memory (state, workspace, output), more than the "
                 f"HBM budget {self.budget}"))
-            return req
+            return
         with self._cv:
             self._queue.append(req)
             self._cv.notify()
-        return req
 
     def close(self):
+        self._planner.shutdown(wait=True)  # every submitted request is queued or failed
         with self._cv:
             self._stop = True
             self._cv.notify()
@@ -232,12 +246,30 @@ class Server:
         return rnd((1 << lo.n) * 8 * B) + rnd(max(int(ws), 256)) + rnd(B * lo.n * 4) + rnd(32) * 3
 
     def _program(self, lo: Lowered) -> Program:
+        """The planned program of a structure, planned once: a thread that
+        finds another one planning the same structure waits for it."""
         key = structure_key(lo)
         with self._plock:
             p = self.programs.get(key)
-            if p is None:
-                p = Program(lo, lo.measure, keep_state=False, **self.opts)
-                self.programs[key] = p
+            if p is not None:
+                return p
+            fut = self._planning.get(key)
+            mine = fut is None
+            if mine:
+                fut = self._planning[key] = cf.Future()
+        if not mine:
+            return fut.result()
+        try:
+            p = Program(lo, lo.measure, keep_state=False, **self.opts)
+        except BaseException as e:
+            with self._plock:
+                del self._planning[key]
+            fut.set_exception(e)
+            raise
+        with self._plock:
+            self.programs[key] = p
+            del self._planning[key]
+        fut.set_result(p)
         return p
 
     def _admit(self, req: Request) -> _Slot:
@@ -266,6 +298,11 @@ class Server:
     def _run(self):
         lib = _lib.load()
         active: list[_Slot] = []
+        # events of the steps enqueued and not yet finished: at most
+        # max_inflight_steps, so that admission and step selection decide
+        # close to when the GPU runs the work (a request that arrives now can
+        # go ahead of the remaining passes of larger ones)
+        inflight = collections.deque()
         with torch.cuda.device(self.device), torch.cuda.stream(self.stream):
             while True:
                 with self._cv:
@@ -282,6 +319,12 @@ class Server:
                         active.append(self._admit(req))
                 if not active:
                     continue
+                while len(inflight) >= self.max_inflight_steps:
+                    ev = inflight[0]
+                    if ev.query():
+                        inflight.popleft()
+                    else:
+                        time.sleep(20e-6)
                 step = self._step_selection(active)
                 for base in range(0, len(step), _lib.MAX_JOBS):
                     chunk = step[base:base + _lib.MAX_JOBS]
@@ -295,6 +338,9 @@ class Server:
                     _lib.check(lib.qg_jobs_run_pass(jobs, len(chunk), self.stream.cuda_stream))
                     self.launches += 1
                 self.steps += 1
+                ev = torch.cuda.Event()
+                ev.record(self.stream)
+                inflight.append(ev)
                 stepped = set(id(s) for s in step)
                 still = []
                 for s in active:
@@ -322,10 +368,10 @@ class Server:
         """The queued request to admit next, or None when it does not fit the
         budget now (called with the queue lock held)."""
         if self.policy == "all":
-            req = self._queue[0]
+            req = min(self._queue, key=lambda r: r.arrival)
             return req if self._used + req.need <= self.budget else None
         now = time.perf_counter()
-        oldest = self._queue[0]
+        oldest = min(self._queue, key=lambda r: r.arrival)  # planning may queue out of arrival order
         if now - oldest.arrival > self.max_queue_wait_s:
             # waited too long: it goes first, and nothing passes it
             return oldest if self._used + oldest.need <= self.budget else None
