@@ -200,3 +200,49 @@ def test_integration_snippet_on_reference_circuit(cuda_device):
     assert len(got) == len(want_grads) > 0
     err = max(float((g.cpu() - w).abs().max()) for g, w in zip(got, want_grads))
     assert err < TOL, err
+
+
+def test_fp32_probe_counts_its_fmas(cuda_device):
+    """The FP32 roof probe launches one block of 256 threads per quarter SM
+    and reports the FMAs it performed (8 chains x 2 lanes per iteration)."""
+    import ctypes
+
+    from qandle_gb300 import _lib
+
+    lib = _lib.load()
+    blocks = lib.qg_fp32_probe_blocks()
+    assert blocks == 4 * torch.cuda.get_device_properties(cuda_device).multi_processor_count
+    out = torch.zeros(blocks, dtype=torch.float32, device=cuda_device)
+    cnt = ctypes.c_int64()
+    _lib.check(lib.qg_fp32_probe(out.data_ptr(), blocks, 64, ctypes.byref(cnt), _lib.stream()))
+    torch.cuda.synchronize()
+    assert cnt.value == blocks * 256 * 64 * 16
+    assert torch.isfinite(out).all() and (out != 0).all()
+    # too small an output buffer is refused before launch
+    assert lib.qg_fp32_probe(out.data_ptr(), blocks - 1, 64, ctypes.byref(cnt), _lib.stream()) != 0
+
+
+def test_timed_backward_records_every_pass(cuda_device):
+    """The adjoint with pass events gives the same gradients as without, and
+    an event pair around each backward pass."""
+    desc = workloads.adjoint_brick(n=14, batch=4, layers=4)
+    desc["measure"] = "p0"
+    circ = workloads.build_circuit(desc, engine="fused").to(cuda_device)
+    st = torch.zeros(4, 1 << 14, dtype=torch.complex64, device=cuda_device)
+    st[:, 0] = 1
+    circ(st).sum().backward()
+    params = [m.theta for m in circ.circuit.layers if isinstance(m, q.BuiltParametrizedOperator)]
+    g0 = torch.stack([p.grad.reshape(()) for p in params]).clone()
+    for p in params:
+        p.grad = None
+    ex = circ._executor
+    nb = ex.program(True).info.backward_passes
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(2 * nb)]
+    ex.backward_events = evs
+    circ(st).sum().backward()
+    torch.cuda.synchronize()
+    assert ex.backward_events is None  # used by one backward
+    g1 = torch.stack([p.grad.reshape(()) for p in params])
+    assert torch.equal(g0, g1)
+    ms = [evs[2 * i].elapsed_time(evs[2 * i + 1]) for i in range(nb)]
+    assert all(m >= 0 for m in ms) and sum(ms) > 0
