@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--serving-rate", type=float, default=2000.0)
     ap.add_argument("--serving-low-requests", type=int, default=60, help="requests at the low rate")
     ap.add_argument("--serving-low-rate", type=float, default=2.0)
+    ap.add_argument("--serving-repeated-requests", type=int, default=300,
+                    help="requests drawn from a few fixed structures, at the high rate")
     ap.add_argument("--autotune", action="store_true",
                     help="run the headline with the autotuner's options")
     ap.add_argument("--interpreted", action="store_true",
@@ -588,9 +590,11 @@ def main():
         # ---------------- serving: Poisson arrivals of mixed-width requests ----------------
         line["serving"] = {
             "high_rate": bench_serving(dev, args.serving_requests, args.serving_rate, seed=7,
-                                       oracle_err=oracle_err, policies=("srpt", "all")),
+                                       oracle_err=oracle_err, policies=("srpt", "all", "srpt_interpreted")),
             "low_rate": bench_serving(dev, args.serving_low_requests, args.serving_low_rate, seed=8,
-                                      oracle_err=oracle_err)}
+                                      oracle_err=oracle_err),
+            "repeated_structures": bench_serving_repeated(dev, args.serving_repeated_requests, args.serving_rate,
+                                                          seed=9, structures=6, oracle_err=oracle_err)}
         torch.cuda.empty_cache()
 
     if rank == 0:
@@ -767,15 +771,21 @@ def bench_autotune(desc, dev, amp_step, default_ms):
             "timings_ms": [[o, round(t, 3)] for o, t in res["timings"]]}
 
 
-def _serve_live(dev, reqs, offs, amp, policy):
+def _serve_live(dev, reqs, offs, amp, policy, compile_min_tiles=1024, warm=()):
     """One live run of the continuous-batching server on the given arrival
-    offsets; returns (stats, outputs)."""
+    offsets; returns (stats, outputs).  The server starts cold (its
+    structures are planned, and large ones compiled, inside the run) unless
+    `warm` lists descriptions to prepare before the first arrival."""
     import torch
 
     from qandle_gb300 import serve
 
     count = len(reqs)
-    srv = serve.Server(dev, hbm_budget=160 << 30, policy=policy)
+    srv = serve.Server(dev, hbm_budget=160 << 30, policy=policy, compile_min_tiles=compile_min_tiles)
+    t_warm = time.perf_counter()
+    for d in warm:
+        srv.prepare(d)
+    t_warm = time.perf_counter() - t_warm
     try:
         t0 = time.perf_counter()
         handles = []
@@ -786,14 +796,21 @@ def _serve_live(dev, reqs, offs, amp, policy):
             handles.append(srv.submit(d, arrival=t0 + o))
         outs = [h.future.result(timeout=1800) for h in handles]
         t_end = max(h.completed for h in handles)
-        steps, launches = srv.steps, srv.launches
+        steps, launches, claunches = srv.steps, srv.launches, srv.compiled_launches
+        compiled = sum(1 for h in handles if h.prog is not None and srv.compile_min_tiles is not None
+                       and serve._tiles_per_pass(h.lowered[0].n, h.desc["batch"] or 1, srv.tile_bits)
+                       >= srv.compile_min_tiles)
     finally:
         srv.close()
     lat = np.array([h.latency for h in handles]) * 1e3
     span = t_end - t0
     stats = {"policy": policy, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
              "circuits_per_s": count / span, "amp_updates_per_s": amp / span, "wall_s": span,
-             "steps": steps, "launches": launches}
+             "steps": steps, "launches": launches, "compiled_launches": claunches,
+             "compile_min_tiles": srv.compile_min_tiles, "requests_at_or_above_compile_min_tiles": compiled,
+             "structures_compiled": srv.compiled_programs, "compile_errors": srv.compile_errors[:3]}
+    if warm:
+        stats["prepared_before_arrivals_s"] = t_warm
     del handles
     torch.cuda.empty_cache()
     return stats, outs
@@ -820,10 +837,16 @@ def bench_serving(dev, count: int, rate: float, seed: int, oracle_err: dict, pol
     offs = np.concatenate([[0.0], np.cumsum(rng.exponential(1.0 / rate, size=count - 1))])
     amp = float(sum(workloads.gate_count(d) * d["batch"] * (1 << d["n"]) for d in reqs))
 
-    fused, outs = _serve_live(dev, reqs, offs, amp, policies[0])
+    def live(variant):
+        # "<policy>" compiles large structures in the background;
+        # "<policy>_interpreted" runs everything on the interpreted kernel
+        pol, _, interp = variant.partition("_")
+        return _serve_live(dev, reqs, offs, amp, pol, compile_min_tiles=None if interp else 1024)
+
+    fused, outs = live(policies[0])
     others = {}
     for pol in policies[1:]:
-        st, o2 = _serve_live(dev, reqs, offs, amp, pol)
+        st, o2 = live(pol)
         st["max_abs_diff_vs_" + policies[0]] = max(float((a - b).abs().max()) for a, b in zip(outs, o2))
         others[pol] = st
 
@@ -866,6 +889,48 @@ def bench_serving(dev, count: int, rate: float, seed: int, oracle_err: dict, pol
             "throughput_ratio": fused["circuits_per_s"] / plain["circuits_per_s"],
             "p99_ratio_per_gate_over_batched": plain["p99_ms"] / fused["p99_ms"],
             "max_abs_diff_vs_per_gate": diff[0], "max_abs_err_vs_oracle_n_le_14": err}
+
+
+def bench_serving_repeated(dev, count: int, rate: float, seed: int, structures: int, oracle_err: dict):
+    """Open-loop Poisson arrivals of `count` requests drawn from a few fixed
+    circuit structures, as a deployment serving a handful of models sees
+    them: strongly-entangling circuits, each structure with its own n ~
+    U{12..24} (distinct) and depth ~ U{2..30}; each request with its own
+    batch (log-uniform [1, 512]), angles and inputs, <Z> out.  Live runs on
+    the same arrivals, shortest remaining work first: a cold server that
+    plans and compiles inside the run, a warm server (every structure
+    prepared before the first arrival), and the interpreted kernel only."""
+    from oracle import oracle
+    from qandle_gb300 import workloads
+
+    rng = np.random.default_rng(seed)
+    ns = rng.choice(np.arange(12, 25), size=structures, replace=False)
+    pool = [(int(n), int(rng.integers(2, 31))) for n in ns]
+    reqs = []
+    for _ in range(count):
+        n, depth = pool[int(rng.integers(len(pool)))]
+        reqs.append(workloads.random_sel_request(rng, n_range=(n, n), depth_range=(depth, depth)))
+    offs = np.concatenate([[0.0], np.cumsum(rng.exponential(1.0 / rate, size=count - 1))])
+    amp = float(sum(workloads.gate_count(d) * d["batch"] * (1 << d["n"]) for d in reqs))
+    warm = [workloads.random_sel_request(np.random.default_rng(0), n_range=(n, n), depth_range=(dp, dp), batch_max=1)
+            for n, dp in pool]
+    cold, outs = _serve_live(dev, reqs, offs, amp, "srpt")
+    warm_st, outs_w = _serve_live(dev, reqs, offs, amp, "srpt", warm=warm)
+    interp, outs_i = _serve_live(dev, reqs, offs, amp, "srpt", compile_min_tiles=None)
+    for st, o in ((cold, outs), (warm_st, outs_w)):
+        st["max_abs_diff_vs_interpreted"] = max(float((a - b).abs().max()) for a, b in zip(o, outs_i))
+    err, checked = 0.0, 0
+    for d, o in zip(reqs, outs_w):
+        if d["n"] <= 14:
+            err = max(err, float(np.abs(o.numpy() - oracle.forward(d)).max()))
+            checked += 1
+    oracle_err[f"serving_repeated_z_{checked}_requests_n_le_14"] = err
+    return {"workload": f"{count} requests, Poisson {rate:g}/s, {structures} structures (n, depth) = {pool}, "
+                        f"batch log-uniform [1, 512], <Z> out (seed {seed})",
+            "offered_s": float(offs[-1]), "amp_updates": amp, "compiled_cold": cold, "compiled_warm": warm_st,
+            "interpreted": interp,
+            "throughput_ratio_warm_over_interpreted": warm_st["circuits_per_s"] / interp["circuits_per_s"],
+            "max_abs_err_vs_oracle_n_le_14": err}
 
 
 def bench_adjoint(dev, sync_all, W, hbm_peak, fp32_tflops, oracle_err, batch: int = 1024):

@@ -317,6 +317,11 @@ int qg_program_prepare(const qg_program* prog, const void* dev_table, void* work
 /* One kernel launch running pass jobs[i].pass of every job.  The jobs must be
  * independent (distinct states) and planned with the same tile_bits. */
 int qg_jobs_run_pass(const qg_job* jobs, int njobs, void* stream);
+/* Pass job->pass of one job as its own launch of the program's compiled pass
+ * kernel (qg_program_compile) for the current device: the kernel
+ * qg_program_forward runs for that pass.  Returns QG_EINVAL, launching
+ * nothing, when that kernel is not compiled and loaded on this device. */
+int qg_job_run_pass_compiled(const qg_job* job, void* stream);
 
 int qg_program_finish(const qg_program* prog, const void* dev_table, void* workspace,
                       int64_t workspace_bytes, int64_t batch, float* out, void* stream);

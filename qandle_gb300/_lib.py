@@ -116,6 +116,7 @@ SIGNATURES = {
     "qg_program_prepare": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p,
                                    c_void_p, c_void_p]),
     "qg_jobs_run_pass": (c_int, [ctypes.POINTER(Job), c_int, c_void_p]),
+    "qg_job_run_pass_compiled": (c_int, [ctypes.POINTER(Job), c_void_p]),
     "qg_workspace_status": (c_int, [c_void_p, c_void_p]),
     "qg_selftest_wait_timeout": (c_int, [c_int64, c_void_p]),
     "qg_fp32_probe_blocks": (c_int64, []),

@@ -851,6 +851,26 @@ int qg_jobs_run_pass(const qg_job* jobs, int njobs, void* stream) {
     return launch_fwd_table(jt, tb, rb, (cudaStream_t)stream);
 }
 
+int qg_job_run_pass_compiled(const qg_job* job, void* stream) {
+    using namespace qg;
+    QG_CHECK_ARG(job, "job is null");
+    ProgramRun R;
+    RunArgs A;
+    FwdLayout L;
+    int rc = fwd_args(job->prog, job->table, job->workspace, job->workspace_bytes, job->state, job->batch, job->out,
+                      nullptr, R, A, L);
+    if (rc) return rc;
+    QG_CHECK_ARG(job->pass >= 0 && job->pass < R.nfpass, "pass index out of range");
+    QG_CHECK_ARG(R.segments <= 1, "checkpointed programs run through qg_program_forward");
+    JitKernel jk;
+    QG_CHECK_ARG(jit_forward_kernel(job->prog, job->pass, &jk),
+                 "the program's pass kernels are not compiled for the current device (qg_program_compile)");
+    const char* tab = (const char*)job->table;
+    return launch_fwd_compiled(jk, (const PassDesc*)(tab + R.off_fpass), (const int4*)(tab + R.off_fops),
+                               R.fpass[job->pass], job->pass, A, job->pass == 0 ? job->zero_init : 0,
+                               num_tiles(R.n, R.tile_bits, job->batch), R.reg_bits, (cudaStream_t)stream);
+}
+
 int qg_program_forward_timed(const qg_program* prog, const void* dev_table, void* workspace,
                              int64_t workspace_bytes, void* state, int64_t batch, int zero_init, const float* params,
                              const float* named, const void* umats, float* out, void* ckpt,

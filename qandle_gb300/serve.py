@@ -5,7 +5,10 @@ RZ RY RZ layers, CNOT rings, <Z> out) of 4..24 qubits and any batch.  The
 loop keeps every admitted request's state, matrix tables and embedding
 factors on the device and advances all admitted requests together: each
 step is ONE multi-job launch of the fused pass kernel (qg_jobs_run_pass)
-that runs the next pass of every active request, whatever its width.  New
+that runs the next pass of every active request, whatever its width, plus
+one launch of its own compiled pass kernel for each large request whose
+program was compiled (in the background, once per structure) before it was
+admitted.  New
 requests are admitted between steps as soon as the HBM budget has room, so
 requests that arrive while others are on the GPU join the running batch
 instead of waiting for it to drain.  A request counts against the budget
@@ -15,7 +18,9 @@ measurement partials) and its output.
 
 Each request's tiles are computed by the same code in the same order
 whatever else shares the launch, and its reductions run in a fixed order,
-so a request's result is bit-identical alone and in the mix.
+so a request's result is bit-identical alone and in the mix.  Which code
+(the interpreted kernel or its program's compiled kernels) is fixed when the
+request is admitted; the two agree within float rounding.
 
 There is no CPU path: the loop drives the CUDA library through its C ABI.
 """
@@ -24,6 +29,8 @@ from __future__ import annotations
 import collections
 import concurrent.futures as cf
 import ctypes
+import heapq
+import itertools
 import threading
 import time
 
@@ -118,7 +125,7 @@ def _tiles_per_pass(n: int, batch: int, tile_bits: int) -> int:
 
 class _Slot:
     __slots__ = ("req", "prog", "state", "ws", "out", "host_out", "batch", "next_pass", "bytes",
-                 "event", "params", "named", "umats", "shift", "tiles", "idle")
+                 "event", "params", "named", "umats", "shift", "tiles", "idle", "compiled")
 
     def remaining(self) -> int:
         return self.tiles * (self.prog.info.forward_passes - self.next_pass)
@@ -159,12 +166,20 @@ class Server:
     advances every active request every step.  Either way a request's result
     does not depend on what else ran: the same kernel computes its tiles in
     the same order.
+
+    compile_min_tiles: a request whose passes walk at least this many tiles
+    has its program's passes compiled (NVRTC) on a background thread, once
+    per structure; when they are ready at its admission its passes run as
+    launches of those kernels, which execute fewer instructions than the
+    interpreted multi-job kernel.  Smaller requests, and large ones admitted
+    before their kernels are ready, run interpreted.  None turns compiling
+    off.
     """
 
     def __init__(self, device="cuda", hbm_budget: int = 64 << 30, max_active: int = 64,
                  tile_bits: int = 13, low_bits: int = 6, policy: str = "srpt", step_tiles: int = 1 << 16,
                  max_idle_steps: int = 64, max_queue_wait_s: float = 10.0, max_inflight_steps: int = 2,
-                 planning_threads: int = 4):
+                 planning_threads: int = 4, compile_min_tiles: int | None = 1024):
         if policy not in ("srpt", "all"):
             raise ValueError(f"policy must be 'srpt' or 'all', got {policy!r}")
         self.device = torch.device(device)
@@ -182,6 +197,19 @@ class Server:
         self._planner = cf.ThreadPoolExecutor(max_workers=max(1, int(planning_threads)))
         self._planning: dict = {}  # structure key -> Future of its Program
         self.programs: dict = {}
+        # compiling runs on one thread (NVRTC already compiles a program's
+        # passes in parallel), largest work first; a structure is compiled at
+        # most once
+        self.compile_min_tiles = None if not compile_min_tiles else int(compile_min_tiles)
+        self._compile_heap: list = []  # (-work, seq, program)
+        self._compile_seq = itertools.count()
+        self._compile_cv = threading.Condition()
+        self._compile_stop = False
+        self._compiling: set = set()
+        self.compile_errors: list = []
+        self.compiled_programs = 0
+        self._compiler = threading.Thread(target=self._compile_loop, daemon=True)
+        self._compiler.start()
         self._plock = threading.Lock()
         self.stream = torch.cuda.Stream(device=self.device)
         self._queue = []
@@ -191,6 +219,7 @@ class Server:
         self._used = 0
         self.steps = 0
         self.launches = 0
+        self.compiled_launches = 0
         self._worker = threading.Thread(target=self._run, daemon=True)
         self._poller = threading.Thread(target=self._poll, daemon=True)
         self._worker.start()
@@ -206,16 +235,38 @@ class Server:
         self._planner.submit(self._plan, req)
         return req
 
+    def prepare(self, desc: dict) -> Program:
+        """Plan a request structure now and, unless compiling is off,
+        compile its passes (blocking): a deployment warms the server with its
+        circuits before traffic arrives.  Later requests of the structure
+        skip planning, and those of at least compile_min_tiles tiles per pass
+        run on the compiled kernels."""
+        lo = lower_description(desc)[0]
+        prog = self._program(lo)
+        if self.compile_min_tiles is not None:
+            with self._plock:
+                first = id(prog) not in self._compiling
+                self._compiling.add(id(prog))
+            with torch.cuda.device(self.device):
+                prog.ensure_compiled(self.device)
+            if first:
+                with self._plock:
+                    self.compiled_programs += 1
+        return prog
+
     def _plan(self, req: "Request") -> None:
         try:
             req.lowered = lower_description(req.desc)
             req.prog = self._program(req.lowered[0])
             need = req.need = self._device_bytes(req)
             lo = req.lowered[0]
-            req.work = _tiles_per_pass(lo.n, req.desc["batch"] or 1, self.tile_bits) * req.prog.info.forward_passes
+            tiles = _tiles_per_pass(lo.n, req.desc["batch"] or 1, self.tile_bits)
+            req.work = tiles * req.prog.info.forward_passes
         except (ValueError, RuntimeError) as e:
             req.future.set_exception(e)
             return
+        if self.compile_min_tiles is not None and tiles >= self.compile_min_tiles and need <= self.budget:
+            self._compile_later(req.prog, req.work)
         if need > self.budget:
             req.future.set_exception(MemoryError(
                 f"request needs {need} bytes of device memory (state, workspace, output), more than the "
@@ -232,6 +283,37 @@ class Server:
             self._cv.notify()
         self._worker.join()
         self._poller.join()
+        with self._compile_cv:
+            self._compile_stop = True  # a compile in progress finishes; queued ones are dropped
+            self._compile_cv.notify()
+        self._compiler.join()
+
+    def _compile_later(self, prog: Program, work: int) -> None:
+        """Queue the compile of a program's forward passes (once per
+        program), ahead of programs whose request has less work."""
+        with self._plock:
+            if id(prog) in self._compiling:
+                return
+            self._compiling.add(id(prog))
+        with self._compile_cv:
+            heapq.heappush(self._compile_heap, (-int(work), next(self._compile_seq), prog))
+            self._compile_cv.notify()
+
+    def _compile_loop(self):
+        while True:
+            with self._compile_cv:
+                while not self._compile_heap and not self._compile_stop:
+                    self._compile_cv.wait()
+                if self._compile_stop:
+                    return
+                prog = heapq.heappop(self._compile_heap)[2]
+            try:
+                with torch.cuda.device(self.device):
+                    prog.ensure_compiled(self.device)
+                with self._plock:
+                    self.compiled_programs += 1
+            except RuntimeError as e:  # NVRTC missing or failing: the interpreter serves it
+                self.compile_errors.append(str(e).splitlines()[0])
 
     # -- internals --
     @staticmethod
@@ -282,6 +364,9 @@ class Server:
         s.bytes = req.need
         s.tiles = _tiles_per_pass(n, B, self.tile_bits)
         s.idle = 0
+        # the request's code path is fixed here, for all of its passes
+        s.compiled = (self.compile_min_tiles is not None and s.tiles >= self.compile_min_tiles
+                      and id(prog) in self._compiling and prog.compiled(self.device))
         dev = self.device
         s.state = torch.empty(B, 1 << n, dtype=torch.complex64, device=dev)
         s.ws = prog.workspace(B, False, dev)
@@ -326,17 +411,20 @@ class Server:
                     else:
                         time.sleep(20e-6)
                 step = self._step_selection(active)
-                for base in range(0, len(step), _lib.MAX_JOBS):
-                    chunk = step[base:base + _lib.MAX_JOBS]
+                interp = [s for s in step if not s.compiled]
+                for base in range(0, len(interp), _lib.MAX_JOBS):
+                    chunk = interp[base:base + _lib.MAX_JOBS]
                     jobs = (_lib.Job * len(chunk))()
                     for i, s in enumerate(chunk):
-                        # a program without an embedding starts from |0..0> in its first pass
-                        zero = 1 if (s.next_pass == 0 and not s.prog.info.has_embedding) else 0
-                        jobs[i] = _lib.Job(s.prog.handle, s.prog.table(self.device).data_ptr(), s.ws.data_ptr(),
-                                           s.ws.numel(), s.state.data_ptr(), s.batch, s.next_pass, zero,
-                                           s.out.data_ptr())
+                        jobs[i] = self._job(s)
                     _lib.check(lib.qg_jobs_run_pass(jobs, len(chunk), self.stream.cuda_stream))
                     self.launches += 1
+                for s in step:
+                    if s.compiled:
+                        job = self._job(s)
+                        _lib.check(lib.qg_job_run_pass_compiled(ctypes.byref(job), self.stream.cuda_stream))
+                        self.launches += 1
+                        self.compiled_launches += 1
                 self.steps += 1
                 ev = torch.cuda.Event()
                 ev.record(self.stream)
@@ -363,6 +451,12 @@ class Server:
                         self._used -= s.bytes
                         self._completing.append(s)
                 active = still
+
+    def _job(self, s: _Slot) -> "_lib.Job":
+        # a program without an embedding starts from |0..0> in its first pass
+        zero = 1 if (s.next_pass == 0 and not s.prog.info.has_embedding) else 0
+        return _lib.Job(s.prog.handle, s.prog.table(self.device).data_ptr(), s.ws.data_ptr(), s.ws.numel(),
+                        s.state.data_ptr(), s.batch, s.next_pass, zero, s.out.data_ptr())
 
     def _next_admission(self):
         """The queued request to admit next, or None when it does not fit the

@@ -82,3 +82,38 @@ def test_policies_give_identical_results(cuda_device):
         assert srv.steps > 0
     for d, a, b in zip(reqs, outs["srpt"], outs["all"]):
         assert torch.equal(a, b), d["n"]
+
+
+def test_compiled_requests_match_oracle_and_interpreted(cuda_device):
+    """Requests whose programs were compiled before admission run as launches
+    of their compiled pass kernels: results within 1e-5 of the oracle and of
+    the interpreted multi-job kernel's."""
+    import time
+
+    reqs = _requests(count=6, seed=21, n_range=(10, 14), depth_range=(2, 4), batch_max=16)
+    srv = serve.Server(cuda_device, hbm_budget=8 << 30, compile_min_tiles=1)
+    try:
+        first = [srv.submit(d) for d in reqs]
+        first_out = [r.future.result(timeout=300) for r in first]
+        t0 = time.time()
+        while srv.compiled_programs + len(srv.compile_errors) < len(srv.programs) and time.time() - t0 < 300:
+            time.sleep(0.05)
+        assert not srv.compile_errors, srv.compile_errors
+        assert srv.compiled_programs == len(srv.programs)
+        before = srv.compiled_launches
+        again = [srv.submit(d) for d in reqs]
+        again_out = [r.future.result(timeout=300) for r in again]
+    finally:
+        srv.close()
+    assert srv.compiled_launches - before == sum(r.prog.info.forward_passes for r in again)
+    plain = serve.Server(cuda_device, hbm_budget=8 << 30, compile_min_tiles=None)
+    try:
+        interp_out = [plain.submit(d).future.result(timeout=300) for d in reqs]
+    finally:
+        plain.close()
+    assert plain.compiled_launches == 0
+    for d, a, b, c in zip(reqs, first_out, again_out, interp_out):
+        ref = oracle.forward(d)
+        assert np.abs(b.numpy() - ref).max() < 1e-5, (d["n"], d["batch"])
+        assert np.abs(a.numpy() - ref).max() < 1e-5, (d["n"], d["batch"])
+        assert (b - c).abs().max().item() < 1e-5
