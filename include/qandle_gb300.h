@@ -261,9 +261,13 @@ int qg_program_compile(qg_program* prog, int flags);
 /* flags: QG_COMPILE_NO_LOAD compiles every pass and discards the result (no
  * device needed: a host-side check that the program's kernels build);
  * QG_COMPILE_BACKWARD also compiles the backward passes, which
- * qg_program_backward then launches. */
+ * qg_program_backward then launches; QG_COMPILE_BACKGROUND compiles on a
+ * quarter of the host's cores at a lower scheduling priority (a compile
+ * beside latency-sensitive work, e.g. a serving loop).  Any host thread may
+ * call it: the device's primary context is made current on it. */
 #define QG_COMPILE_NO_LOAD 1
 #define QG_COMPILE_BACKWARD 2
+#define QG_COMPILE_BACKGROUND 4
 /* 0: nothing compiled for `prog` on the current device; 1: forward passes;
  * 3: forward and backward passes. */
 int qg_program_compiled(const qg_program* prog);

@@ -19,6 +19,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <dlfcn.h>
+#include <sys/resource.h>
+#include <sys/syscall.h>
 #include <unistd.h>
 #include <nvrtc.h>
 
@@ -617,6 +619,14 @@ bool jit_backward_kernel(const void* prog, int pass, JitKernel* out) { return ji
 int jit_launch(const JitKernel& k, unsigned grid, unsigned block, size_t smem, void* stream, void** params) {
     CUresult r = driver().launch((CUfunction)k.fn, grid, 1, 1, block, 1, 1, (unsigned)smem, (CUstream)stream,
                                  params, nullptr);
+    if (r == CUDA_ERROR_INVALID_CONTEXT) {
+        // first launch from a thread that has made no runtime call: make the
+        // primary context of the current device current and launch again
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaSetDevice(dev) == cudaSuccess)
+            r = driver().launch((CUfunction)k.fn, grid, 1, 1, block, 1, 1, (unsigned)smem, (CUstream)stream, params,
+                                nullptr);
+    }
     if (r != CUDA_SUCCESS) {
         set_error("cuLaunchKernel: " + cu_error(r));
         return QG_ECUDA;
@@ -635,6 +645,7 @@ int qg_program_compile(qg_program* prog, int flags) {
     if (!prog) return set_error("qg_program_compile: null pointer"), QG_EINVAL;
     const bool load = !(flags & QG_COMPILE_NO_LOAD);
     const bool with_bwd = (flags & QG_COMPILE_BACKWARD) != 0;
+    const bool background = (flags & QG_COMPILE_BACKGROUND) != 0;
     const Nvrtc& N = nvrtc();
     if (!N.why.empty()) return set_error("qg_program_compile: " + N.why), QG_ECUDA;
     int dev = -1;
@@ -642,6 +653,10 @@ int qg_program_compile(qg_program* prog, int flags) {
         const Driver& D = driver();
         if (!D.why.empty()) return set_error("qg_program_compile: " + D.why), QG_ECUDA;
         QG_CUDA_TRY(cudaGetDevice(&dev));
+        // a thread that has made no runtime call yet has no current context
+        // for the driver calls below: cudaSetDevice makes the device's
+        // primary context current on this thread
+        QG_CUDA_TRY(cudaSetDevice(dev));
     }
     ProgramRun R;
     program_run_info(prog, &R);
@@ -680,12 +695,17 @@ int qg_program_compile(qg_program* prog, int flags) {
     std::vector<int> rcs(todo.size(), QG_OK);
     {
         unsigned hw = std::thread::hardware_concurrency();
-        size_t nthreads = std::min<size_t>(todo.size(), hw ? hw : 4);
+        if (!hw) hw = 4;
+        // a background compile leaves most cores to the caller's other work
+        size_t nthreads = std::min<size_t>(todo.size(), background ? std::max(1u, hw / 4) : hw);
         std::vector<std::thread> pool;
         std::mutex qmu;
         size_t next = 0;
         for (size_t t = 0; t < nthreads; ++t)
             pool.emplace_back([&] {
+                // background compiles run at a lower scheduling priority (the
+                // nice value of a Linux thread is its own)
+                if (background) (void)setpriority(PRIO_PROCESS, (id_t)syscall(SYS_gettid), 10);
                 for (;;) {
                     size_t i;
                     {

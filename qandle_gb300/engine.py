@@ -229,16 +229,17 @@ class Program:
         lib.qg_program_pass_source(self.handle, bw, p, buf, size)
         return buf.value.decode()
 
-    def compile(self, device=None, load: bool = True, backward: bool = None) -> None:
+    def compile(self, device=None, load: bool = True, backward: bool = None, background: bool = False) -> None:
         """Compile the passes into per-pass kernels (NVRTC) for ``device``:
         the forward passes, and the backward passes too when ``backward``
         (default: when the program keeps its state for a backward).  With
-        ``load=False`` only check that they build (no GPU needed).  Raises
-        RuntimeError with the compiler's log on failure."""
+        ``load=False`` only check that they build (no GPU needed);
+        ``background`` compiles on a quarter of the cores at a lower
+        priority.  Raises RuntimeError with the compiler's log on failure."""
         lib = _lib.load()
         if backward is None:
             backward = self.keep_state
-        flags = (0 if load else 1) | (2 if backward else 0)
+        flags = (0 if load else 1) | (2 if backward else 0) | (4 if background else 0)
         if load:
             with torch.cuda.device(device):
                 _lib.check(lib.qg_program_compile(self.handle, flags))
@@ -252,13 +253,13 @@ class Program:
             v = _lib.load().qg_program_compiled(self.handle)
         return v == 3 if self.keep_state else v >= 1
 
-    def ensure_compiled(self, device) -> None:
+    def ensure_compiled(self, device, background: bool = False) -> None:
         key = str(device)
         if key in self._compiled:
             return
         with self._lock:
             if key not in self._compiled:
-                self.compile(device)
+                self.compile(device, background=background)
                 self._compiled.add(key)
 
     def table(self, device) -> torch.Tensor:

@@ -309,7 +309,7 @@ class Server:
                 prog = heapq.heappop(self._compile_heap)[2]
             try:
                 with torch.cuda.device(self.device):
-                    prog.ensure_compiled(self.device)
+                    prog.ensure_compiled(self.device, background=True)
                 with self._plock:
                     self.compiled_programs += 1
             except RuntimeError as e:  # NVRTC missing or failing: the interpreter serves it
