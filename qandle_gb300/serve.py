@@ -7,8 +7,7 @@ factors on the device and advances all admitted requests together: each
 step is ONE multi-job launch of the fused pass kernel (qg_jobs_run_pass)
 that runs the next pass of every active request, whatever its width, plus
 one launch of its own compiled pass kernel for each large request whose
-program was compiled (in the background, once per structure) before it was
-admitted.  New
+program has been compiled (in the background, once per structure).  New
 requests are admitted between steps as soon as the HBM budget has room, so
 requests that arrive while others are on the GPU join the running batch
 instead of waiting for it to drain.  A request counts against the budget
@@ -18,9 +17,11 @@ measurement partials) and its output.
 
 Each request's tiles are computed by the same code in the same order
 whatever else shares the launch, and its reductions run in a fixed order,
-so a request's result is bit-identical alone and in the mix.  Which code
-(the interpreted kernel or its program's compiled kernels) is fixed when the
-request is admitted; the two agree within float rounding.
+so a request's result is bit-identical alone and in the mix.  The
+interpreted kernel and a program's compiled kernels run the same op list
+through the same arithmetic (only the dispatch on register positions
+differs), so a request that moves to the compiled kernels once they are
+ready, at a pass boundary, gets the same bits as one that never does.
 
 There is no CPU path: the loop drives the CUDA library through its C ABI.
 """
@@ -169,11 +170,10 @@ class Server:
 
     compile_min_tiles: a request whose passes walk at least this many tiles
     has its program's passes compiled (NVRTC) on a background thread, once
-    per structure; when they are ready at its admission its passes run as
-    launches of those kernels, which execute fewer instructions than the
-    interpreted multi-job kernel.  Smaller requests, and large ones admitted
-    before their kernels are ready, run interpreted.  None turns compiling
-    off.
+    per structure, largest work first; from the first step after they are
+    ready its passes run as launches of those kernels, which execute fewer
+    instructions than the interpreted multi-job kernel.  Smaller requests
+    share the interpreted launches.  None turns compiling off.
     """
 
     def __init__(self, device="cuda", hbm_budget: int = 64 << 30, max_active: int = 64,
@@ -205,7 +205,8 @@ class Server:
         self._compile_seq = itertools.count()
         self._compile_cv = threading.Condition()
         self._compile_stop = False
-        self._compiling: set = set()
+        self._compiling: set = set()  # programs queued or compiled (ids)
+        self._ready: set = set()      # programs whose compiled kernels are loaded (ids)
         self.compile_errors: list = []
         self.compiled_programs = 0
         self._compiler = threading.Thread(target=self._compile_loop, daemon=True)
@@ -249,8 +250,9 @@ class Server:
                 self._compiling.add(id(prog))
             with torch.cuda.device(self.device):
                 prog.ensure_compiled(self.device)
-            if first:
-                with self._plock:
+            with self._plock:
+                self._ready.add(id(prog))
+                if first:
                     self.compiled_programs += 1
         return prog
 
@@ -311,6 +313,7 @@ class Server:
                 with torch.cuda.device(self.device):
                     prog.ensure_compiled(self.device, background=True)
                 with self._plock:
+                    self._ready.add(id(prog))
                     self.compiled_programs += 1
             except RuntimeError as e:  # NVRTC missing or failing: the interpreter serves it
                 self.compile_errors.append(str(e).splitlines()[0])
@@ -364,9 +367,7 @@ class Server:
         s.bytes = req.need
         s.tiles = _tiles_per_pass(n, B, self.tile_bits)
         s.idle = 0
-        # the request's code path is fixed here, for all of its passes
-        s.compiled = (self.compile_min_tiles is not None and s.tiles >= self.compile_min_tiles
-                      and id(prog) in self._compiling and prog.compiled(self.device))
+        s.compiled = False  # set at the first step after its program's kernels are ready
         dev = self.device
         s.state = torch.empty(B, 1 << n, dtype=torch.complex64, device=dev)
         s.ws = prog.workspace(B, False, dev)
@@ -411,6 +412,10 @@ class Server:
                     else:
                         time.sleep(20e-6)
                 step = self._step_selection(active)
+                if self._ready:
+                    for s in step:
+                        if not s.compiled and id(s.prog) in self._ready and s.tiles >= self.compile_min_tiles:
+                            s.compiled = True
                 interp = [s for s in step if not s.compiled]
                 for base in range(0, len(interp), _lib.MAX_JOBS):
                     chunk = interp[base:base + _lib.MAX_JOBS]

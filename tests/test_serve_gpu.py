@@ -85,9 +85,11 @@ def test_policies_give_identical_results(cuda_device):
 
 
 def test_compiled_requests_match_oracle_and_interpreted(cuda_device):
-    """Requests whose programs were compiled before admission run as launches
-    of their compiled pass kernels: results within 1e-5 of the oracle and of
-    the interpreted multi-job kernel's."""
+    """Requests whose programs have been compiled run as launches of their
+    compiled pass kernels: results within 1e-5 of the oracle and
+    bit-identical to the interpreted multi-job kernel's (same op list, same
+    arithmetic), so a request that switches between the two at a pass
+    boundary gets the same bits."""
     import time
 
     reqs = _requests(count=6, seed=21, n_range=(10, 14), depth_range=(2, 4), batch_max=16)
@@ -116,4 +118,22 @@ def test_compiled_requests_match_oracle_and_interpreted(cuda_device):
         ref = oracle.forward(d)
         assert np.abs(b.numpy() - ref).max() < 1e-5, (d["n"], d["batch"])
         assert np.abs(a.numpy() - ref).max() < 1e-5, (d["n"], d["batch"])
-        assert (b - c).abs().max().item() < 1e-5
+        assert torch.equal(b, c), (d["n"], d["batch"])
+        assert torch.equal(a, c), (d["n"], d["batch"])
+
+
+def test_prepare_compiles_before_traffic(cuda_device):
+    """Server.prepare plans and compiles a structure before its requests
+    arrive: every pass of a later request of that structure (at or above
+    compile_min_tiles) is a compiled launch, and the result is the oracle's."""
+    rng = np.random.default_rng(4)
+    desc = workloads.random_sel_request(rng, n_range=(12, 12), depth_range=(3, 3), batch_max=8)
+    srv = serve.Server(cuda_device, hbm_budget=8 << 30, compile_min_tiles=1)
+    try:
+        prog = srv.prepare(desc)
+        assert prog.compiled(cuda_device) and srv.compiled_programs == 1
+        out = srv.submit(desc).future.result(timeout=120)
+    finally:
+        srv.close()
+    assert srv.compiled_launches == prog.info.forward_passes
+    assert np.abs(out.numpy() - oracle.forward(desc)).max() < 1e-5
