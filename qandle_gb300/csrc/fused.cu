@@ -127,8 +127,12 @@ __device__ __forceinline__ void papply_op(const int4 op, PTile<RB>* const (&ts)[
         case OP_CX: {
             if (op.z & LOC_REG) {
                 const int c = op.z & 7;
-                if ((xm >> c) & 1) pmaterialize<RB, NTILE>(ts, xm, c);  // the control must be materialised
-                // a pending X on the target commutes with the CNOT and stays pending
+                // the same rules as the compiled passes' jcx, so that both
+                // kernels apply every later 2x2 to the same operands in the
+                // same order: the register CNOT runs on the physical bits and
+                // a pending X on the control stays pending (X_c CX X_c = X_t
+                // CX: it moves a pending X onto the target); a pending X on
+                // the target commutes with the CNOT
 #pragma unroll
                 for (int i = 0; i < NTILE; ++i)
                     for_pos<RB>(op.y, [&](auto P) {
@@ -137,6 +141,7 @@ __device__ __forceinline__ void papply_op(const int4 op, PTile<RB>* const (&ts)[
                                 pcx<decltype(P)::value, decltype(C)::value, RB>(*ts[i]);
                         });
                     });
+                xm ^= ((xm >> c) & 1u) << op.y;
             } else {
                 xm ^= (uint32_t)loc_bit_thread(op.z, tm.tglob) << op.y;
             }
@@ -166,8 +171,8 @@ __device__ __forceinline__ void papply_op(const int4 op, PTile<RB>* const (&ts)[
         }
         case OP_SWAP: {
             if (op.y == op.z) break;
-            if ((xm >> op.y) & 1) pmaterialize<RB, NTILE>(ts, xm, op.y);
-            if ((xm >> op.z) & 1) pmaterialize<RB, NTILE>(ts, xm, op.z);
+            // as the compiled passes' jswap: swap the physical bits and their
+            // pending X flags
 #pragma unroll
             for (int i = 0; i < NTILE; ++i)
                 for_pos<RB>(op.y, [&](auto P0) {
@@ -176,6 +181,8 @@ __device__ __forceinline__ void papply_op(const int4 op, PTile<RB>* const (&ts)[
                             pswapbits<decltype(P0)::value, decltype(P1)::value, RB>(*ts[i]);
                     });
                 });
+            const uint32_t dx = ((xm >> op.y) ^ (xm >> op.z)) & 1u;
+            xm ^= dx * ((1u << op.y) | (1u << op.z));
             break;
         }
         default:

@@ -147,6 +147,18 @@ def _grad_case(desc, dev, opts, weights_seed=3):
     return np.array(thetas), (x.grad.cpu().numpy() if x is not None else None), w.cpu().numpy()
 
 
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("oi", [0, 1, 4, 6])
+def test_compiled_equals_interpreted_bitwise(cuda_device, case, oi):
+    """The compiled pass kernels and the op interpreter run the same op list
+    with the same pending-X rules and arithmetic: identical bits (the
+    serving loop moves a request between them at a pass boundary)."""
+    desc = CASES[case]()
+    a = _run(desc, cuda_device, compiled=True, **OPTS[oi])
+    b = _run(desc, cuda_device, compiled=False, **OPTS[oi])
+    assert np.array_equal(a, b), (case, OPTS[oi], np.abs(a - b).max())
+
+
 @pytest.mark.parametrize("case,opts", [
     ("brick_n10", dict()), ("brick_n14", dict()), ("brick_n16", dict(checkpoint_segments=3)),
     ("sel_n9", dict()), ("sel_n14", dict(checkpoint_segments=2)), ("sel_n15", dict(tile_bits=12, low_bits=4)),
