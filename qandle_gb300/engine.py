@@ -208,7 +208,8 @@ class Program:
         self._table_host = torch.frombuffer(bytearray(host), dtype=torch.uint8)
         self._tables = {}
         self._compiled = set()
-        self._lock = threading.Lock()
+        self._lock = threading.Lock()          # device tables
+        self._compile_lock = threading.Lock()  # compiles (seconds; must not hold up table lookups)
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -257,7 +258,7 @@ class Program:
         key = str(device)
         if key in self._compiled:
             return
-        with self._lock:
+        with self._compile_lock:
             if key not in self._compiled:
                 self.compile(device, background=background)
                 self._compiled.add(key)
