@@ -358,6 +358,81 @@ __device__ __forceinline__ void pstore_probs(const PTile<RB>& t, float* pb, int 
     }
 }
 
+// P0 partials of a tile that holds TB qubits of one sample (n >= TB), from
+// the registers of the natural mapping (local bits 0..4 the lane, 5..4+RB the
+// register index, the rest the warp; physical register r holds logical
+// amplitude r ^ xm).  dst[b] = the sum of |amp|^2 over the tile's amplitudes
+// whose local bit b is 0 (b < TB), dst[TB] = the tile's total.  Each thread
+// sums its 2^RB probabilities per register bit value; each warp reduces its
+// RB + 6 values (register-bit sums, the total, and the total of the lanes
+// whose bit j is 0, j < 5) with a transposing butterfly (16 shuffles: lane L
+// ends with the warp's sum of value L / 2); red[w][i] holds warp w's values,
+// and threads 0..TB add them over the warps.  The caller synchronises the
+// compute warps between the writes to red and the final sums.
+template <int TB, int RB>
+__device__ __forceinline__ void p0_warp_sums(const PTile<RB>& t, uint32_t xm, float (*red)[16], int tid, int lane) {
+    constexpr int H = 1 << (RB - 1);
+    float T[H];
+    float z0 = 0.f, o0 = 0.f;
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+        const float2 p = vfma(t.I[h], t.I[h], vmul(t.R[h], t.R[h]));  // registers 2h, 2h + 1
+        T[h] = p.x + p.y;
+        z0 += p.x;
+        o0 += p.y;
+    }
+    float v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = 0.f;
+    v[0] = (xm & 1u) ? o0 : z0;
+#pragma unroll
+    for (int k = 1; k < RB; ++k) {
+        float z = 0.f, o = 0.f;
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+            if ((h >> (k - 1)) & 1) o += T[h];
+            else z += T[h];
+        }
+        v[k] = ((xm >> k) & 1u) ? o : z;
+    }
+    const float tot = z0 + o0;
+    v[RB] = tot;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) v[RB + 1 + j] = ((lane >> j) & 1) ? 0.f : tot;
+    // transposing butterfly: after the step over lane bit b the lane keeps
+    // the half of its values selected by that bit, summed with its partner's
+#pragma unroll
+    for (int w = 8; w >= 1; w >>= 1) {
+        const int off = 2 * w;  // lane bits 4, 3, 2, 1
+        const bool hi = (lane & off) != 0;
+#pragma unroll
+        for (int i = 0; i < w; ++i) {
+            const float send = hi ? v[i] : v[i + w];
+            const float keep = hi ? v[i + w] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+    }
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+    if (!(lane & 1) && (lane >> 1) < RB + 6) red[tid >> 5][lane >> 1] = v[0];
+}
+
+template <int TB, int RB>
+__device__ __forceinline__ void p0_tile_from_warps(const float (*red)[16], int tid, float* dst) {
+    constexpr int NW = 1 << (TB - RB - 5);
+    if (tid > TB) return;
+    float acc = 0.f;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+        float x;
+        if (tid < 5) x = red[w][RB + 1 + tid];                  // lane bit
+        else if (tid < 5 + RB) x = red[w][tid - 5];             // register bit
+        else if (tid < TB) x = ((w >> (tid - 5 - RB)) & 1) ? 0.f : red[w][RB];  // warp bit
+        else x = red[w][RB];                                    // total
+        acc += x;
+    }
+    dst[tid] = acc;
+}
+
 // Exchange through planar shared memory (re plane, im plane), folding the
 // pending X of the thread into the write addresses.
 template <int RB, int K = 0>
@@ -623,6 +698,9 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
     __shared__ PassDesc sd;
     __shared__ RunArgs sa;
     __shared__ TileGeo s_geo[S];  // geometry of the tile in each buffer (written by the producer)
+    // per-warp P0 sums of the register epilogue, by tile parity (every tile
+    // passes a compute-warp barrier after warp 0 read the previous parity)
+    __shared__ float s_red[2][1 << (TB - RB - 5)][16];
 
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -706,6 +784,8 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
                 float2 c = make_float2(1.f, 0.f);
                 uint32_t regmask = 0;
                 for (int k = 0; k < RB; ++k) regmask |= 1u << d.gbit[tm.regl[k]];
+                // (a loop unrolled to 32 bits, to issue every factor's load
+                // ahead of the products, measured slower)
                 for (int b = 0; b < n; ++b) {
                     if (regmask & (1u << b)) continue;
                     c = cmul(c, fac[2 * (n - 1 - b) + ((tm.tglob >> b) & 1)]);
@@ -745,7 +825,14 @@ __device__ __forceinline__ void fwd_pass_body(const JobTable<MAXJ>& jt) {
         // ---- epilogue (the planner left the natural mapping, or for a pass
         // that only stores, a mapping with natural lanes: d.end_map) ----
         const int64_t smp0 = g.sample;
-        if (epi & (EPI_PROBS | EPI_P0)) {
+        if ((epi & EPI_P0) && !(epi & EPI_PROBS) && d.nq_tile == TB) {
+            // one sample per tile: sums from the registers, no pass through `buf`
+            float(*red)[16] = s_red[iter & 1];
+            p0_warp_sums<TB, RB>(pt, xm, red, tid, lane);
+            cta_sync<NT>();
+            p0_tile_from_warps<TB, RB>(
+                red, tid, A.p0part + ((smp0 * (int64_t(1) << (n - TB)) + g.tile_in_sample) * (TB + 1)));
+        } else if (epi & (EPI_PROBS | EPI_P0)) {
             cta_sync<NT>();  // all exchange reads of `buf` are done
             float* pb = reinterpret_cast<float*>(buf);
             pstore_probs<RB>(pt, pb, tid, xm);
