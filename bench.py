@@ -1047,7 +1047,13 @@ def bench_adjoint(dev, sync_all, W, hbm_peak, fp32_tflops, oracle_err, batch: in
                          "backward_ms_per_step": float(bms.sum()),
                          "fp32_frac": float(2.0 * bfmas.sum() / (bms.sum() * 1e-3) / (fp32_tflops * 1e12)),
                          "combined_frac": comb,
-                         "passes_fp32_bound": int(np.sum(t_fp > t_mem))},
+                         "passes_fp32_bound": int(np.sum(t_fp > t_mem)),
+                         "per_pass": [{"ms": round(float(bms[p]), 4),
+                                       "fma_per_amp": round(float(bfmas[p]) / amps, 1),
+                                       "hbm_frac": round(float(bbytes[p] / (bms[p] * 1e-3) / 1e9 / hbm_peak), 3),
+                                       "fp32_frac": round(float(2.0 * bfmas[p] / (bms[p] * 1e-3)
+                                                                / (fp32_tflops * 1e12)), 3)}
+                                      for p in range(NB)]},
             "max_abs_err_vs_oracle_8_samples": {"p0": p_err, "z": z_err, "grad": g_err},
             "note": "step = forward + backward; amp-updates count each gate once forward and twice "
                     "backward (state and cotangent)"}
