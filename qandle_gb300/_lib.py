@@ -30,7 +30,8 @@ class Gate(ctypes.Structure):
 class PlanOptions(ctypes.Structure):
     """qg_plan_options."""
     _fields_ = [(f, ctypes.c_int32) for f in ("tile_bits", "low_bits", "max_high", "measure",
-                                              "keep_state", "segments", "reg_bits", "reg_search")]
+                                              "keep_state", "segments", "reg_bits", "reg_search",
+                                              "bwd_max_grad")]
 
 
 class ProgramInfo(ctypes.Structure):

@@ -611,7 +611,12 @@ void plan_segment(Program& P, const std::vector<LGate>& G, std::vector<int> pend
     while (!pending.empty()) {
         Selector s;
         s.backward = backward;
-        if (backward) s.max_grad = max_grad_per_pass(kBwdRegBits);
+        if (backward) {
+            // gradient partials per pass: the kernel's shared memory holds
+            // max_grad_per_pass; the plan may ask for fewer (shorter passes)
+            s.max_grad = max_grad_per_pass(kBwdRegBits);
+            if (P.opt.bwd_max_grad > 0) s.max_grad = std::min(s.max_grad, P.opt.bwd_max_grad);
+        }
         if (n <= tb) {
             s.S = (n >= 32) ? 0xffffffffu : ((1u << n) - 1);
             s.addable = 0;
@@ -1050,6 +1055,7 @@ int qg_program_create(const qg_gate* gates, int ngates, const int32_t* qlist, in
         return qg::set_error("tile_bits - reg_bits must leave 0..4 warp bits"), QG_EINVAL;
     if (o.segments < 1) o.segments = 1;
     if (o.reg_search != 0 && o.reg_search != 1) return qg::set_error("reg_search must be 0 or 1"), QG_EINVAL;
+    if (o.bwd_max_grad < 0) return qg::set_error("bwd_max_grad must be >= 0"), QG_EINVAL;
     std::unique_ptr<Program> P(new Program());
     P->n = n;
     P->opt = o;

@@ -70,15 +70,16 @@ def test_forward_plan_matches_oracle(case, oi):
     assert prog.info.forward_passes >= 1
 
 
-@pytest.mark.parametrize("rb", [5, 4])
+@pytest.mark.parametrize("rb,cap", [(5, 0), (4, 0), (5, 7)])
 @pytest.mark.parametrize("case", ["sel_n10", "brick_n14", "deep_n14", "sel_n15"])
-def test_backward_plan_matches_oracle(case, rb):
+def test_backward_plan_matches_oracle(case, rb, cap):
     desc = dict(CASES)[case]()
     desc["measure"] = "p0"
     n, B = desc["n"], desc["batch"]
     circ = workloads.build_circuit(desc, engine="fused")
     lo = engine.lower(circ.circuit)
-    prog = engine.Program(lo, "p0", keep_state=True, segments=3, tile_bits=13, low_bits=5, reg_bits=rb)
+    prog = engine.Program(lo, "p0", keep_state=True, segments=3, tile_bits=13, low_bits=5, reg_bits=rb,
+                          bwd_max_grad=cap)
     params, named, umats, embed = _runtime(lo, desc, B)
     st, ck = emu.run_forward(prog, n, B, params, named, umats, embed=embed)
     w = np.linspace(-1.0, 1.0, B * n).reshape(B, n)
@@ -104,6 +105,24 @@ def test_backward_plan_matches_oracle(case, rb):
             arr[:, j] += dn[:, c]
     for name, arr in got.items():
         assert np.abs(arr - rdn[name]).max() < 1e-9, name
+
+
+def test_backward_rotation_cap_splits_passes():
+    """bwd_max_grad caps the gradient-carrying rotations of every backward
+    pass (the default is the kernel's shared-memory limit, 64 at 16
+    amplitudes per thread); a lower cap gives more, shorter passes."""
+    desc = workloads.adjoint_brick(n=16, batch=1, layers=20)
+    circ = workloads.build_circuit(desc, engine="fused")
+    lo = engine.lower(circ.circuit)
+    full = engine.Program(lo, "p0", keep_state=True, segments=4)
+    capped = engine.Program(lo, "p0", keep_state=True, segments=4, bwd_max_grad=32)
+
+    assert max(p["ngrad"] for p in capped.passes(backward=True)) <= 32
+    assert max(p["ngrad"] for p in full.passes(backward=True)) <= 64
+    assert capped.info.backward_passes > full.info.backward_passes
+    assert sum(p["ngrad"] for p in capped.passes(backward=True)) == sum(p["ngrad"] for p in full.passes(backward=True))
+    with pytest.raises(RuntimeError):
+        engine.Program(lo, "p0", keep_state=True, bwd_max_grad=-1)
 
 
 def test_fusion_reduces_passes():
