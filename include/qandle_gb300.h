@@ -207,9 +207,10 @@ typedef struct qg_plan_options {
                            new register set is the one the next gates ask for), 1 = try
                            every register set of the tile's qubits and keep the one that
                            places the most gates (backward passes always search) */
-    int32_t bwd_max_grad; /* gradient-carrying rotations per backward pass: 0 = as many as
-                             the pass kernel's shared memory holds (64 at 16 amplitudes per
-                             thread); fewer makes more, shorter backward passes */
+    int32_t bwd_max_grad; /* gradient-carrying rotations per backward pass (at most 64, what
+                             the pass kernel's shared memory holds): 0 = the default, 28;
+                             longer passes leave the instruction cache, shorter ones add
+                             HBM round trips */
 } qg_plan_options;
 
 typedef struct qg_program qg_program;

@@ -602,6 +602,14 @@ void emit_pass(Program& P, PassPlan& pp, const std::vector<LGate>& G, bool backw
     (void)nps;
 }
 
+// Default cap on the gradient-carrying rotations of a backward pass.  Each
+// rotation unrolls into its 2x2 on psi and on lambda and a gradient partial;
+// passes of more rotations leave the instruction cache.  Measured on the
+// 16-qubit, 20-layer adjoint at batch 1024 (backward ms per step by cap):
+// 64 (the shared-memory limit) 48.9, 40 51.6, 36 51.5, 32 42.9, 28 40.0,
+// 24 40.7, 16 45.4.
+constexpr int kBwdGradPerPass = 28;
+
 // Split a segment of gates into passes (tile selection).
 void plan_segment(Program& P, const std::vector<LGate>& G, std::vector<int> pending, int tb,
                   bool backward, std::vector<PassPlan>& out) {
@@ -612,10 +620,10 @@ void plan_segment(Program& P, const std::vector<LGate>& G, std::vector<int> pend
         Selector s;
         s.backward = backward;
         if (backward) {
-            // gradient partials per pass: the kernel's shared memory holds
-            // max_grad_per_pass; the plan may ask for fewer (shorter passes)
-            s.max_grad = max_grad_per_pass(kBwdRegBits);
-            if (P.opt.bwd_max_grad > 0) s.max_grad = std::min(s.max_grad, P.opt.bwd_max_grad);
+            // gradient-carrying rotations per pass: at most what the kernel's
+            // shared memory holds (max_grad_per_pass), by default kBwdGradPerPass
+            const int cap = P.opt.bwd_max_grad > 0 ? P.opt.bwd_max_grad : kBwdGradPerPass;
+            s.max_grad = std::min(max_grad_per_pass(kBwdRegBits), cap);
         }
         if (n <= tb) {
             s.S = (n >= 32) ? 0xffffffffu : ((1u << n) - 1);

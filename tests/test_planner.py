@@ -109,13 +109,16 @@ def test_backward_plan_matches_oracle(case, rb, cap):
 
 def test_backward_rotation_cap_splits_passes():
     """bwd_max_grad caps the gradient-carrying rotations of every backward
-    pass (the default is the kernel's shared-memory limit, 64 at 16
+    pass (default 28; at most the kernel's shared-memory limit, 64 at 16
     amplitudes per thread); a lower cap gives more, shorter passes."""
     desc = workloads.adjoint_brick(n=16, batch=1, layers=20)
     circ = workloads.build_circuit(desc, engine="fused")
     lo = engine.lower(circ.circuit)
-    full = engine.Program(lo, "p0", keep_state=True, segments=4)
+    full = engine.Program(lo, "p0", keep_state=True, segments=4, bwd_max_grad=100)  # the 64 limit
     capped = engine.Program(lo, "p0", keep_state=True, segments=4, bwd_max_grad=32)
+    default = engine.Program(lo, "p0", keep_state=True, segments=4)
+    assert max(p["ngrad"] for p in default.passes(backward=True)) <= 28
+    assert max(p["ngrad"] for p in full.passes(backward=True)) == 64
 
     assert max(p["ngrad"] for p in capped.passes(backward=True)) <= 32
     assert max(p["ngrad"] for p in full.passes(backward=True)) <= 64
