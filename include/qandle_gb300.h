@@ -211,6 +211,8 @@ typedef struct qg_plan_options {
                              the pass kernel's shared memory holds): 0 = the default, 28;
                              longer passes leave the instruction cache, shorter ones add
                              HBM round trips */
+    int32_t fwd_max_mats; /* 2x2 slots per forward pass (a run of single-qubit gates on one
+                             qubit is one slot): 0 = no cap */
 } qg_plan_options;
 
 typedef struct qg_program qg_program;

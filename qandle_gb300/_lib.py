@@ -31,7 +31,7 @@ class PlanOptions(ctypes.Structure):
     """qg_plan_options."""
     _fields_ = [(f, ctypes.c_int32) for f in ("tile_bits", "low_bits", "max_high", "measure",
                                               "keep_state", "segments", "reg_bits", "reg_search",
-                                              "bwd_max_grad")]
+                                              "bwd_max_grad", "fwd_max_mats")]
 
 
 class ProgramInfo(ctypes.Structure):

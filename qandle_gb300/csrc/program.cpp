@@ -130,6 +130,11 @@ struct Selector {
     bool backward = false;
     const int* remap = nullptr;  // nullptr: identity
     int max_grad = 1 << 30;      // gradient-carrying gates per selection (backward tiles)
+    // Forward tiles: 2x2 slots per selection.  A run of single-qubit gates on
+    // one qubit with nothing else touching it in between becomes one slot;
+    // run_open marks the qubits whose last placed touch is such a run.
+    int max_mats = 1 << 30;
+    uint32_t run_open = 0;
 
     int m(int b) const { return remap ? remap[b] : b; }
 
@@ -184,6 +189,8 @@ struct Selector {
                     ok = !((sZ | sX | sG) & bm);
             }
             if (ok && backward && g.grad && max_grad <= 0) ok = false;
+            const bool new_mat = !backward && is_1q(g) && !(run_open & (1u << m(g.b0)));
+            if (ok && new_mat && max_mats <= 0) ok = false;
             if (ok) {
                 uint32_t req = 0;
                 uint32_t r = requirement(g, backward);
@@ -212,6 +219,15 @@ struct Selector {
                     placed.push_back(pi);
                 }
                 if (ok && backward && g.grad) --max_grad;
+                if (ok && !backward) {
+                    if (is_1q(g)) {
+                        if (new_mat) --max_mats;
+                        run_open |= 1u << m(g.b0);
+                    } else {
+                        for (int k = 0; k < t.count; ++k)
+                            if (t.bit[k] >= 0) run_open &= ~(1u << m(t.bit[k]));
+                    }
+                }
             }
             if (!ok) {
                 for (int k = 0; k < t.count; ++k) {
@@ -619,6 +635,7 @@ void plan_segment(Program& P, const std::vector<LGate>& G, std::vector<int> pend
     while (!pending.empty()) {
         Selector s;
         s.backward = backward;
+        if (!backward && P.opt.fwd_max_mats > 0) s.max_mats = P.opt.fwd_max_mats;
         if (backward) {
             // gradient-carrying rotations per pass: at most what the kernel's
             // shared memory holds (max_grad_per_pass), by default kBwdGradPerPass
@@ -1064,6 +1081,7 @@ int qg_program_create(const qg_gate* gates, int ngates, const int32_t* qlist, in
     if (o.segments < 1) o.segments = 1;
     if (o.reg_search != 0 && o.reg_search != 1) return qg::set_error("reg_search must be 0 or 1"), QG_EINVAL;
     if (o.bwd_max_grad < 0) return qg::set_error("bwd_max_grad must be >= 0"), QG_EINVAL;
+    if (o.fwd_max_mats < 0) return qg::set_error("fwd_max_mats must be >= 0"), QG_EINVAL;
     std::unique_ptr<Program> P(new Program());
     P->n = n;
     P->opt = o;

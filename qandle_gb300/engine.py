@@ -179,7 +179,7 @@ class Program:
 
     def __init__(self, lowered: Lowered, measure: str, keep_state: bool, tile_bits: int = 13,
                  low_bits: int = 6, max_high: int = 0, segments: int = 1, reg_bits: int = 5,
-                 reg_search: int = 0, bwd_max_grad: int = 0):
+                 reg_search: int = 0, bwd_max_grad: int = 0, fwd_max_mats: int = 0):
         lib = _lib.load()
         self.n = lowered.n
         self.measure = measure
@@ -198,6 +198,7 @@ class Program:
         opt.reg_bits = reg_bits
         opt.reg_search = int(reg_search)
         opt.bwd_max_grad = int(bwd_max_grad)
+        opt.fwd_max_mats = int(fwd_max_mats)
         handle = ctypes.c_void_p()
         _lib.check(lib.qg_program_create(gates, len(lowered.gates), ctypes.cast(ql, ctypes.c_void_p),
                                          self.n, ctypes.byref(opt), ctypes.byref(handle)))
@@ -578,7 +579,7 @@ class FusedExecutor:
 
     def __init__(self, circuit, tile_bits: int = 13, low_bits: int = 6, max_high: int = 0,
                  checkpoint_segments: int = 1, reg_bits: int = 5, compiled: bool = None,
-                 graphs: bool = None, reg_search: int = 0, bwd_max_grad: int = 0):
+                 graphs: bool = None, reg_search: int = 0, bwd_max_grad: int = 0, fwd_max_mats: int = 0):
         self.circuit = circuit
         # graphs = True: an inference call (no gradient needed, a measured
         # output) replays one captured CUDA graph of the whole forward, kept
@@ -606,7 +607,8 @@ class FusedExecutor:
             self.fusible = False
             warnings.warn(f"{e}; this circuit runs one kernel per gate")
         self.options = dict(tile_bits=tile_bits, low_bits=low_bits, max_high=max_high, reg_bits=reg_bits,
-                            reg_search=int(reg_search), bwd_max_grad=int(bwd_max_grad))
+                            reg_search=int(reg_search), bwd_max_grad=int(bwd_max_grad),
+                            fwd_max_mats=int(fwd_max_mats))
         self.checkpoint_segments = checkpoint_segments
         self._programs = {}
         # timing hook: a list of 2 x (backward passes) CUDA events makes the
