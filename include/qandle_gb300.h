@@ -212,7 +212,9 @@ typedef struct qg_plan_options {
                              longer passes leave the instruction cache, shorter ones add
                              HBM round trips */
     int32_t fwd_max_mats; /* 2x2 slots per forward pass (a run of single-qubit gates on one
-                             qubit is one slot): 0 = no cap */
+                             qubit is one slot): 0 = the default, 24 (the compiled passes
+                             unroll every op, and longer ones leave the instruction cache);
+                             a large value plans passes as long as the tile allows */
 } qg_plan_options;
 
 typedef struct qg_program qg_program;

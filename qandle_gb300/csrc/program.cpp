@@ -626,6 +626,14 @@ void emit_pass(Program& P, PassPlan& pp, const std::vector<LGate>& G, bool backw
 // 24 40.7, 16 45.4.
 constexpr int kBwdGradPerPass = 28;
 
+// Default cap on the 2x2 slots of a forward pass, for the same reason: the
+// compiled pass unrolls every op.  Measured forward ms by cap (uncapped /
+// 48 / 32 / 24 / 16): 16 qubits x 1024, 20 layers 10.26 / 10.28 / 8.22 /
+// 7.99 / 8.84; 13 qubits x 4096, 20 SEL layers (one pass uncapped) 12.9 /
+// 6.54 / 5.85 / 5.22 / 5.43; 28 qubits x 1 156.6 / 156.7 / 153.5 / 154.2 /
+// 162.0; the 20-qubit SEL forward already has at most 24 per pass.
+constexpr int kFwdMatsPerPass = 24;
+
 // Split a segment of gates into passes (tile selection).
 void plan_segment(Program& P, const std::vector<LGate>& G, std::vector<int> pending, int tb,
                   bool backward, std::vector<PassPlan>& out) {
@@ -635,7 +643,7 @@ void plan_segment(Program& P, const std::vector<LGate>& G, std::vector<int> pend
     while (!pending.empty()) {
         Selector s;
         s.backward = backward;
-        if (!backward && P.opt.fwd_max_mats > 0) s.max_mats = P.opt.fwd_max_mats;
+        if (!backward) s.max_mats = P.opt.fwd_max_mats > 0 ? P.opt.fwd_max_mats : kFwdMatsPerPass;
         if (backward) {
             // gradient-carrying rotations per pass: at most what the kernel's
             // shared memory holds (max_grad_per_pass), by default kBwdGradPerPass

@@ -191,7 +191,9 @@ class Server:
         self.max_queue_wait_s = float(max_queue_wait_s)
         self.tile_bits = tile_bits
         self.max_inflight_steps = max(1, int(max_inflight_steps))
-        self.opts = dict(tile_bits=tile_bits, low_bits=low_bits)
+        # passes as long as the tile allows: every pass of a request is one
+        # scheduling step, and the interpreted kernel does not unroll its ops
+        self.opts = dict(tile_bits=tile_bits, low_bits=low_bits, fwd_max_mats=1 << 30)
         # lowering and planning run off the caller's thread, several at once
         # (the C planner releases the interpreter lock)
         self._planner = cf.ThreadPoolExecutor(max_workers=max(1, int(planning_threads)))

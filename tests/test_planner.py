@@ -51,7 +51,8 @@ CASES = [
 OPTS = [dict(tile_bits=13, low_bits=6, max_high=0), dict(tile_bits=12, low_bits=4, max_high=2),
         dict(tile_bits=11, low_bits=5, max_high=1), dict(tile_bits=13, low_bits=8, max_high=3),
         dict(tile_bits=13, low_bits=6, reg_bits=4), dict(tile_bits=12, low_bits=5, reg_bits=4),
-        dict(tile_bits=13, low_bits=6, reg_search=1), dict(tile_bits=13, low_bits=6, max_high=4, reg_search=1)]
+        dict(tile_bits=13, low_bits=6, reg_search=1), dict(tile_bits=13, low_bits=6, max_high=4, reg_search=1),
+        dict(tile_bits=13, low_bits=6, fwd_max_mats=3), dict(tile_bits=12, low_bits=5, fwd_max_mats=1 << 30)]
 
 
 @pytest.mark.parametrize("case", [c[0] for c in CASES])
@@ -126,6 +127,27 @@ def test_backward_rotation_cap_splits_passes():
     assert sum(p["ngrad"] for p in capped.passes(backward=True)) == sum(p["ngrad"] for p in full.passes(backward=True))
     with pytest.raises(RuntimeError):
         engine.Program(lo, "p0", keep_state=True, bwd_max_grad=-1)
+
+
+def test_forward_mat_cap():
+    """A forward pass holds at most 24 2x2 slots by default (fwd_max_mats):
+    a 13-qubit, 20-layer SEL circuit that fits one pass uncapped is split,
+    with the same gates in the same order."""
+    desc = workloads.sel_reupload(n=13, batch=2, layers=20)
+    circ = workloads.build_circuit(desc, engine="fused")
+    lo = engine.lower(circ.circuit)
+
+    def mats(prog):
+        return [int(np.sum((p["ops"][:, 0] == 2) | (p["ops"][:, 0] == 3))) for p in prog.passes()]
+
+    default = engine.Program(lo, "z", keep_state=False)
+    uncapped = engine.Program(lo, "z", keep_state=False, fwd_max_mats=1 << 30)
+    assert uncapped.info.forward_passes == 1 and max(mats(uncapped)) > 24
+    assert max(mats(default)) <= 24 and default.info.forward_passes > 1
+    assert sum(mats(default)) == sum(mats(uncapped))
+    assert max(mats(engine.Program(lo, "z", keep_state=False, fwd_max_mats=10))) <= 10
+    with pytest.raises(RuntimeError):
+        engine.Program(lo, "z", keep_state=False, fwd_max_mats=-1)
 
 
 def test_fusion_reduces_passes():
