@@ -11,13 +11,17 @@ The best plan depends on the circuit and the batch:
   smaller k gives lighter passes (and more of them);
 * qubit-remap schedule (``reg_search``): which tile qubits each exchange
   brings into the registers -- the greedy set the next gates ask for, or the
-  set (searched over all of them) that places the most gates.
+  set (searched over all of them) that places the most gates;
+* pass length (``fwd_max_mats``): the 2x2 slots a pass may hold (default 24);
+  longer passes make fewer HBM round trips but their unrolled code leaves
+  the instruction cache.
 
 ``autotune`` plans and runs candidates on the device with the circuit's own
 structure at the given batch and times each forward with CUDA events.
 Without an explicit candidate list it searches in stages: the tile shapes
 first, then k one and two below the tile's limit on the best shape, then the
-searched remap schedule on the best of those.  Results are kept in a JSON
+searched remap schedule on the best of those, then pass lengths of 16 and 32
+2x2 slots on the best so far.  Results are kept in a JSON
 file keyed by the circuit's gate structure (gate kinds and qubits, not
 angles), the batch, the device and whether passes are compiled, so a later
 process gets the answer without running anything.
@@ -155,6 +159,7 @@ def autotune(circuit, batch: int, device="cuda", candidates: typing.Optional[typ
         if timings:
             run(_k_candidates(min(timings, key=lambda t: t[1])[0], built.num_qubits))
             run([dict(min(timings, key=lambda t: t[1])[0], reg_search=1)])
+            run([dict(min(timings, key=lambda t: t[1])[0], fwd_max_mats=m) for m in (16, 32)])
     if not timings:
         raise RuntimeError("no candidate plan could be run for this circuit")
     best = min(timings, key=lambda t: t[1])

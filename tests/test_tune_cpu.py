@@ -66,7 +66,8 @@ def test_autotune_needs_a_runnable_candidate(tmp_path):
 def test_staged_search_tries_k_and_remap_schedule(tmp_path):
     """Without a candidate list the search runs the tile shapes, then k one
     and two below the tile's strided limit on the best shape, then the
-    searched remap schedule on the best so far."""
+    searched remap schedule on the best so far, then pass lengths of 16 and
+    32 2x2 slots."""
     circ = _circuit(workloads.sel_reupload(n=16, batch=4, layers=2, reupload_every=1))
     calls = []
 
@@ -83,5 +84,8 @@ def test_staged_search_tries_k_and_remap_schedule(tmp_path):
     assert calls[:len(tune.DEFAULT_CANDIDATES)] == tune.DEFAULT_CANDIDATES
     ks = [c.get("max_high") for c in calls if "max_high" in c and not c.get("reg_search")]
     assert ks == [5, 4]
-    assert calls[-1].get("reg_search") == 1 and calls[-1].get("max_high") == 5
-    assert res["options"] == calls[-1] and res["ms"] == 1.25
+    rs = [c for c in calls if c.get("reg_search")]
+    assert rs[0].get("max_high") == 5 and "fwd_max_mats" not in rs[0]
+    assert [c.get("fwd_max_mats") for c in calls[-2:]] == [16, 32]
+    assert all(c.get("reg_search") == 1 and c.get("max_high") == 5 for c in calls[-2:])
+    assert res["options"] == rs[0] and res["ms"] == 1.25
