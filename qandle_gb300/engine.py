@@ -666,6 +666,11 @@ class FusedExecutor:
         b.set_from(inp, state)
         if b.graph is None:
             b.capture()
+            if state is not None:
+                # the capture's warm-up launch ran the forward on the static
+                # buffers, and a plan of several passes stores its state
+                # between passes in place: the call's input state goes in again
+                b.set_from(inp, state)
         b.replay()  # records the status word
         if _CHECK_STATUS:
             check_status(b.ws)
@@ -842,6 +847,10 @@ class BoundForward:
             STATUS.record(self.ws, "forward")
 
     def capture(self) -> None:
+        """Capture the forward into a CUDA graph.  A warm-up launch runs
+        first (outside the graph), and it advances the static state buffer
+        when the plan has several passes: set an input state again before
+        the first replay."""
         s = torch.cuda.Stream(device=self.device)
         s.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(s):

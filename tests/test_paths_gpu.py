@@ -246,3 +246,20 @@ def test_timed_backward_records_every_pass(cuda_device):
     assert torch.equal(g0, g1)
     ms = [evs[2 * i].elapsed_time(evs[2 * i + 1]) for i in range(nb)]
     assert all(m >= 0 for m in ms) and sum(ms) > 0
+
+
+def test_first_graph_call_multi_pass_with_input_state(cuda_device):
+    """The first inference call captures the graph; its warm-up launch
+    advances the static state of a plan with several passes, and the call's
+    input state must go in again before the replay (an 8-qubit circuit
+    planned into 11 passes)."""
+    desc = workloads.deep_u(n=8, batch=3, layers=6)
+    circ = workloads.build_circuit(desc, engine="fused", fwd_max_mats=4).to(cuda_device)
+    st = torch.zeros(3, 1 << 8, dtype=torch.complex64, device=cuda_device)
+    st[:, 0] = 1
+    ref = oracle.forward(desc)
+    for _ in range(2):  # the capturing call and a replay
+        with torch.no_grad():
+            out = circ(st)
+        assert circ._executor.program(False).info.forward_passes > 1
+        assert np.abs(out.cpu().numpy() - ref).max() < TOL
