@@ -21,7 +21,7 @@ structure at the given batch and times each forward with CUDA events.
 Without an explicit candidate list it searches in stages: the tile shapes
 first, then k one and two below the tile's limit on the best shape, then the
 searched remap schedule on the best of those, then pass lengths of 16 and 32
-2x2 slots on the best so far.  Results are kept in a JSON
+2x2 slots and uncapped passes on the best so far.  Results are kept in a JSON
 file keyed by the circuit's gate structure (gate kinds and qubits, not
 angles), the batch, the device and whether passes are compiled, so a later
 process gets the answer without running anything.
@@ -47,6 +47,11 @@ DEFAULT_CANDIDATES: typing.List[dict] = [
     dict(tile_bits=12, low_bits=6, reg_bits=4),
     dict(tile_bits=13, low_bits=6, reg_bits=4),
 ]
+
+
+# fwd_max_mats that plans passes as long as the tile allows (a small state
+# pays per pass in latency, not in HBM traffic)
+UNCAPPED = 1 << 30
 
 
 def _k_candidates(best: dict, n: int) -> typing.List[dict]:
@@ -159,7 +164,7 @@ def autotune(circuit, batch: int, device="cuda", candidates: typing.Optional[typ
         if timings:
             run(_k_candidates(min(timings, key=lambda t: t[1])[0], built.num_qubits))
             run([dict(min(timings, key=lambda t: t[1])[0], reg_search=1)])
-            run([dict(min(timings, key=lambda t: t[1])[0], fwd_max_mats=m) for m in (16, 32)])
+            run([dict(min(timings, key=lambda t: t[1])[0], fwd_max_mats=m) for m in (16, 32, UNCAPPED)])
     if not timings:
         raise RuntimeError("no candidate plan could be run for this circuit")
     best = min(timings, key=lambda t: t[1])

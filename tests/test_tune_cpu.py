@@ -67,7 +67,7 @@ def test_staged_search_tries_k_and_remap_schedule(tmp_path):
     """Without a candidate list the search runs the tile shapes, then k one
     and two below the tile's strided limit on the best shape, then the
     searched remap schedule on the best so far, then pass lengths of 16 and
-    32 2x2 slots."""
+    32 2x2 slots and uncapped passes."""
     circ = _circuit(workloads.sel_reupload(n=16, batch=4, layers=2, reupload_every=1))
     calls = []
 
@@ -86,6 +86,6 @@ def test_staged_search_tries_k_and_remap_schedule(tmp_path):
     assert ks == [5, 4]
     rs = [c for c in calls if c.get("reg_search")]
     assert rs[0].get("max_high") == 5 and "fwd_max_mats" not in rs[0]
-    assert [c.get("fwd_max_mats") for c in calls[-2:]] == [16, 32]
-    assert all(c.get("reg_search") == 1 and c.get("max_high") == 5 for c in calls[-2:])
+    assert [c.get("fwd_max_mats") for c in calls[-3:]] == [16, 32, tune.UNCAPPED]
+    assert all(c.get("reg_search") == 1 and c.get("max_high") == 5 for c in calls[-3:])
     assert res["options"] == rs[0] and res["ms"] == 1.25
