@@ -539,6 +539,16 @@ class _Inputs:
             self.umats = torch.zeros(1, 2, 2, dtype=torch.complex64, device=device)
 
 
+_SM_COUNT: dict = {}
+
+
+def _sm_count(device: torch.device) -> int:
+    idx = device.index if device.index is not None else torch.cuda.current_device()
+    if idx not in _SM_COUNT:
+        _SM_COUNT[idx] = torch.cuda.get_device_properties(idx).multi_processor_count
+    return _SM_COUNT[idx]
+
+
 def _out_shape(measure, out, n, unbatched):
     if measure in ("p0", "z"):
         return out.transpose(0, 1).squeeze().transpose(-1, 0)
@@ -610,19 +620,42 @@ class FusedExecutor:
                             reg_search=int(reg_search), bwd_max_grad=int(bwd_max_grad),
                             fwd_max_mats=int(fwd_max_mats))
         self.checkpoint_segments = checkpoint_segments
-        self._programs = {}
+        self._programs = {}  # (training, uncapped passes) -> Program
+        self._last_long: dict = {}
         # timing hook: a list of 2 x (backward passes) CUDA events makes the
         # next backward record a pair around every backward pass (then clears)
         self.backward_events = None
 
-    def program(self, training: bool) -> Program:
-        key = bool(training)
+    def program(self, training: bool, batch: int = None, device=None) -> Program:
+        """The planned program for inference or training.  With the pass
+        length left at its default, a call whose passes have fewer tiles than
+        the device has SMs gets the plan with uncapped forward passes: such a
+        pass does not fill the GPU, so it costs a tile's latency, and fewer,
+        longer passes are faster.  Without `batch`, the plan the last call
+        with this `training` used (the default plan before any call)."""
+        training = bool(training)
+        if batch is None:
+            long = self._last_long.get(training, False)
+        else:
+            long = self.options.get("fwd_max_mats", 0) == 0 and self._small(batch, device)
+            self._last_long[training] = long
+        key = (training, long)
         p = self._programs.get(key)
         if p is None:
-            p = Program(self.lowered, self.lowered.measure, keep_state=key,
-                        segments=self.checkpoint_segments if key else 1, **self.options)
+            opts = dict(self.options, fwd_max_mats=1 << 30) if long else self.options
+            p = Program(self.lowered, self.lowered.measure, keep_state=training,
+                        segments=self.checkpoint_segments if training else 1, **opts)
             self._programs[key] = p
         return p
+
+    def _small(self, batch: int, device) -> bool:
+        """True when a forward pass at `batch` has fewer tiles than `device`
+        has SMs."""
+        tb = self.options.get("tile_bits", 13)
+        n = self.n
+        tiles = batch << (n - tb) if n >= tb else -(-batch // (1 << (tb - n)))
+        dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        return tiles < _sm_count(dev)
 
     def __call__(self, state=None, **kwargs):
         if self.n < 5 or not self.fusible:
@@ -644,7 +677,7 @@ class FusedExecutor:
         if not training and self.graphs and self.lowered.measure != "state":
             out = self._replay(inp, state, dev)
             return _out_shape(self.lowered.measure, out, self.n, inp.unbatched)
-        out = _FusedRun.apply(self, self.program(training), state, inp.params, inp.named, inp.umats,
+        out = _FusedRun.apply(self, self.program(training, inp.batch, dev), state, inp.params, inp.named, inp.umats,
                               inp.batch, zero_init)
         return _out_shape(self.lowered.measure, out, self.n, inp.unbatched)
 
@@ -791,7 +824,7 @@ class BoundForward:
 
     def __init__(self, ex: "FusedExecutor", batch: int, device, has_state: bool = False):
         self.ex = ex
-        self.prog = ex.program(False)
+        self.prog = ex.program(False, batch, device)
         self.n = ex.n
         self.batch = batch
         self.device = torch.device(device)

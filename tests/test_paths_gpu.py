@@ -263,3 +263,21 @@ def test_first_graph_call_multi_pass_with_input_state(cuda_device):
             out = circ(st)
         assert circ._executor.program(False).info.forward_passes > 1
         assert np.abs(out.cpu().numpy() - ref).max() < TOL
+
+
+def test_small_calls_plan_uncapped_passes(cuda_device):
+    """With the default pass length, a call whose passes have fewer tiles
+    than the GPU has SMs runs the uncapped plan (one pass for this 13-qubit,
+    12-layer circuit), a larger call the capped one; both give the oracle's
+    <Z>."""
+    sms = torch.cuda.get_device_properties(cuda_device).multi_processor_count
+    for batch, one_pass in ((4, True), (2 * sms, False)):
+        desc = workloads.sel_reupload(n=13, batch=batch, layers=12, reupload_every=4)
+        circ = workloads.build_circuit(desc, engine="fused").to(cuda_device)
+        with torch.no_grad():
+            out = circ(**workloads.circuit_inputs(desc, cuda_device))
+        passes = circ._executor.program(False).info.forward_passes
+        assert (passes == 1) == one_pass, (batch, passes)
+        ref = oracle.forward(dict(desc, batch=min(batch, 8),
+                                  inputs={k: v[:8] for k, v in desc["inputs"].items()}))
+        assert np.abs(out[:8].cpu().numpy() - ref).max() < TOL
