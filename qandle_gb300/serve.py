@@ -132,6 +132,46 @@ class _Slot:
         return self.tiles * (self.prog.info.forward_passes - self.next_pass)
 
 
+class _CompileQueue:
+    """Programs waiting for their compile, largest work first.  A program
+    (by identity: the server keeps every program it planned) enters at most
+    once; after close, pop returns None and queued programs are dropped."""
+
+    def __init__(self):
+        self._heap: list = []  # (-work, seq, program)
+        self._seq = itertools.count()
+        self._seen: set = set()
+        self._cv = threading.Condition()
+        self._closed = False
+
+    def push(self, prog, work: int) -> bool:
+        with self._cv:
+            if self._closed or id(prog) in self._seen:
+                return False
+            self._seen.add(id(prog))
+            heapq.heappush(self._heap, (-int(work), next(self._seq), prog))
+            self._cv.notify()
+            return True
+
+    def claim(self, prog) -> None:
+        """Mark a program compiled elsewhere, so that it is not queued."""
+        with self._cv:
+            self._seen.add(id(prog))
+
+    def pop(self):
+        with self._cv:
+            while not self._heap and not self._closed:
+                self._cv.wait()
+            if self._closed:
+                return None
+            return heapq.heappop(self._heap)[2]
+
+    def close(self) -> None:
+        with self._cv:
+            self._closed = True
+            self._cv.notify_all()
+
+
 class Request:
     def __init__(self, desc: dict, arrival: float | None = None):
         self.desc = desc
@@ -203,17 +243,12 @@ class Server:
         # passes in parallel), largest work first; a structure is compiled at
         # most once
         self.compile_min_tiles = None if not compile_min_tiles else int(compile_min_tiles)
-        self._compile_heap: list = []  # (-work, seq, program)
-        self._compile_seq = itertools.count()
-        self._compile_cv = threading.Condition()
-        self._compile_stop = False
-        self._compiling: set = set()  # programs queued or compiled (ids)
-        self._ready: set = set()      # programs whose compiled kernels are loaded (ids)
+        self._compileq = _CompileQueue()
+        self._ready: set = set()  # programs whose compiled kernels are loaded (ids)
         self.compile_errors: list = []
-        self.compiled_programs = 0
+        self._plock = threading.Lock()
         self._compiler = threading.Thread(target=self._compile_loop, daemon=True)
         self._compiler.start()
-        self._plock = threading.Lock()
         self.stream = torch.cuda.Stream(device=self.device)
         self._queue = []
         self._cv = threading.Condition()
@@ -247,16 +282,17 @@ class Server:
         lo = lower_description(desc)[0]
         prog = self._program(lo)
         if self.compile_min_tiles is not None:
-            with self._plock:
-                first = id(prog) not in self._compiling
-                self._compiling.add(id(prog))
+            self._compileq.claim(prog)
             with torch.cuda.device(self.device):
                 prog.ensure_compiled(self.device)
             with self._plock:
                 self._ready.add(id(prog))
-                if first:
-                    self.compiled_programs += 1
         return prog
+
+    @property
+    def compiled_programs(self) -> int:
+        """Programs whose compiled kernels are loaded."""
+        return len(self._ready)
 
     def _plan(self, req: "Request") -> None:
         try:
@@ -270,7 +306,7 @@ class Server:
             req.future.set_exception(e)
             return
         if self.compile_min_tiles is not None and tiles >= self.compile_min_tiles and need <= self.budget:
-            self._compile_later(req.prog, req.work)
+            self._compileq.push(req.prog, req.work)
         if need > self.budget:
             req.future.set_exception(MemoryError(
                 f"request needs {need} bytes of device memory (state, workspace, output), more than the "
@@ -287,36 +323,19 @@ class Server:
             self._cv.notify()
         self._worker.join()
         self._poller.join()
-        with self._compile_cv:
-            self._compile_stop = True  # a compile in progress finishes; queued ones are dropped
-            self._compile_cv.notify()
+        self._compileq.close()  # a compile in progress finishes; queued ones are dropped
         self._compiler.join()
-
-    def _compile_later(self, prog: Program, work: int) -> None:
-        """Queue the compile of a program's forward passes (once per
-        program), ahead of programs whose request has less work."""
-        with self._plock:
-            if id(prog) in self._compiling:
-                return
-            self._compiling.add(id(prog))
-        with self._compile_cv:
-            heapq.heappush(self._compile_heap, (-int(work), next(self._compile_seq), prog))
-            self._compile_cv.notify()
 
     def _compile_loop(self):
         while True:
-            with self._compile_cv:
-                while not self._compile_heap and not self._compile_stop:
-                    self._compile_cv.wait()
-                if self._compile_stop:
-                    return
-                prog = heapq.heappop(self._compile_heap)[2]
+            prog = self._compileq.pop()
+            if prog is None:
+                return
             try:
                 with torch.cuda.device(self.device):
                     prog.ensure_compiled(self.device, background=True)
                 with self._plock:
                     self._ready.add(id(prog))
-                    self.compiled_programs += 1
             except RuntimeError as e:  # NVRTC missing or failing: the interpreter serves it
                 self.compile_errors.append(str(e).splitlines()[0])
 

@@ -100,3 +100,25 @@ def test_tiles_per_pass():
     assert serve._tiles_per_pass(20, 3, 13) == 3 << 7
     assert serve._tiles_per_pass(8, 33, 13) == 2             # 32 samples of 2^8 per 2^13 tile
     assert serve._tiles_per_pass(13, 1, 13) == 1
+
+
+def test_compile_queue_orders_by_work_and_dedupes():
+    """The background compile queue hands out programs largest work first,
+    takes each program once (also one compiled by prepare), and after close
+    hands out nothing."""
+    import threading
+
+    q = serve._CompileQueue()
+    a, b, c, d = object(), object(), object(), object()
+    assert q.push(a, 5) and q.push(b, 50) and q.push(c, 20)
+    assert not q.push(b, 500)  # already queued
+    q.claim(d)
+    assert not q.push(d, 1000)  # compiled elsewhere
+    assert [q.pop(), q.pop(), q.pop()] == [b, c, a]
+    got = []
+    t = threading.Thread(target=lambda: got.append(q.pop()))
+    t.start()  # waits for work
+    q.close()
+    t.join(timeout=10)
+    assert not t.is_alive() and got == [None]
+    assert not q.push(object(), 1)
