@@ -72,6 +72,9 @@ enum Opcode : int32_t {
     OP_SWAP = 6,  // exchange register positions y and z
     OP_GRAD = 7,  // backward: gradient partial Im<lam|P|psi> of axis z on register
                   //   position y into grad slot w (no state change)
+    OP_XMAT = 8,  // apply the pending X of register position y to the registers
+                  //   (no state change: inserted before an exchange whose writes
+                  //   it would bank-conflict)
 };
 constexpr int32_t LOC_REG = 0x100;  // location = register position (low bits); else global bit
 constexpr int32_t OPF_PER_SAMPLE = 1;  // matrix slot is per sample

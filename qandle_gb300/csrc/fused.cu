@@ -169,6 +169,9 @@ __device__ __forceinline__ void papply_op(const int4 op, PTile<RB>* const (&ts)[
                 for (int i = 0; i < NTILE; ++i) pnegate_mask<RB>(*ts[i], mask);
             break;
         }
+        case OP_XMAT:
+            pmaterialize<RB, NTILE>(ts, xm, op.y);
+            break;
         case OP_SWAP: {
             if (op.y == op.z) break;
             // as the compiled passes' jswap: swap the physical bits and their

@@ -359,6 +359,9 @@ std::string pass_source(const ProgramRun& R, int p) {
                 if (y != z) s << "jswap<" << y << ", " << z << ", RB>(pt, xm);\n";
                 else s << "\n";
                 break;
+            case OP_XMAT:
+                s << "jmaterialize<" << y << ", RB>(pt, xm);\n";
+                break;
             default:
                 s << "// op " << k << " has no forward form\n";
                 break;
@@ -450,6 +453,9 @@ std::string bwd_pass_source(const ProgramRun& R, int p) {
             case OP_SWAP:
                 if (y != z) s << "jswap2<" << y << ", " << z << ", RB>(pt, lt, xm);\n";
                 else s << "\n";
+                break;
+            case OP_XMAT:
+                s << "jmaterialize2<" << y << ", RB>(pt, lt, xm);\n";
                 break;
             default:
                 s << "// op " << k << " has no backward form\n";

@@ -381,6 +381,86 @@ namespace {
 // Emit the device ops of one pass from its placed gates.
 // Phase planning: greedily choose register sets; merge runs of single-qubit
 // gates on one qubit into one matrix slot (forward only).
+// An exchange writes each register to the slot of its logical index, so the
+// thread's pending X (register r holds logical amplitude r ^ xm) is folded into
+// the write address.  A CNOT whose control is a lane bit makes that pending X
+// depend on the lane, and the write's lane -> bank map then carries the bank
+// image of the register as well: it can become singular (bank conflicts).
+// Walk the pass's ops tracking, per register position, the global bits its
+// pending X depends on, and before every exchange whose write map would be
+// singular insert OP_XMAT for registers with lane-dependent pending X until
+// the map has full rank.
+void materialize_before_exchanges(std::vector<int32_t>& ops, const PassDesc& d, int op_begin, int rb) {
+    auto rank5 = [](const int v[5]) {
+        int basis[5], nb = 0;
+        for (int j = 0; j < 5; ++j) {
+            int x = v[j];
+            for (int e = 0; e < nb; ++e) x = std::min(x, x ^ basis[e]);
+            if (x) basis[nb++] = x;
+        }
+        return nb;
+    };
+    int reg[5], lane[5];
+    auto set_map = [&](int32_t y, int32_t z) {
+        for (int k = 0; k < rb; ++k) reg[k] = (y >> (4 * k)) & 15;
+        for (int j = 0; j < 5; ++j) lane[j] = (z >> (4 * j)) & 15;
+    };
+    {
+        Mapping nat = natural_mapping(d.tile_bits, rb);
+        int32_t e[3];
+        nat.encode(e);
+        if (d.init == INIT_EMBED) set_map(d.init_map[0], d.init_map[1]);
+        else set_map(e[0], e[1]);
+    }
+    uint32_t form[5] = {0, 0, 0, 0, 0};  // global bits the pending X of each register position depends on
+    std::vector<int32_t> out(ops.begin(), ops.begin() + 4 * (size_t)op_begin);
+    for (size_t i = 4 * (size_t)op_begin; i < ops.size(); i += 4) {
+        const int32_t k = ops[i], y = ops[i + 1], z = ops[i + 2];
+        if (k == OP_MAP) {
+            uint32_t lane_g = 0;  // global bits of the lanes (qubit bits of the tile only)
+            int lg[5];
+            for (int j = 0; j < 5; ++j) {
+                lg[j] = lane[j] < d.nq_tile ? d.gbit[lane[j]] : -1;
+                if (lg[j] >= 0) lane_g |= 1u << lg[j];
+            }
+            auto write_rank = [&](uint32_t skip) {
+                int v[5];
+                for (int j = 0; j < 5; ++j) {
+                    v[j] = qg::bank_image(lane[j]);
+                    if (lg[j] < 0) continue;
+                    for (int r = 0; r < rb; ++r)
+                        if (!((skip >> r) & 1u) && ((form[r] >> lg[j]) & 1u)) v[j] ^= qg::bank_image(reg[r]);
+                }
+                return rank5(v);
+            };
+            while (write_rank(0) < 5) {
+                // materialize one register that restores full rank if there is
+                // one, else the first with a lane-dependent pending X
+                int pick = -1;
+                for (int r = 0; r < rb && pick < 0; ++r)
+                    if ((form[r] & lane_g) && write_rank(1u << r) == 5) pick = r;
+                for (int r = 0; r < rb && pick < 0; ++r)
+                    if (form[r] & lane_g) pick = r;
+                if (pick < 0) break;  // (cannot happen: without lane-dependent X the map is the lanes')
+                out.insert(out.end(), {OP_XMAT, pick, 0, 0});
+                form[pick] = 0;
+            }
+            set_map(y, z);
+            for (int r = 0; r < 5; ++r) form[r] = 0;
+        } else if (k == OP_CX) {
+            if (z & LOC_REG) form[y] ^= form[z & 7];
+            else if (z >= 0 && z < 32) form[y] ^= 1u << z;
+        } else if (k == OP_SWAP && y != z) {
+            std::swap(form[y], form[z]);
+        } else if (k == OP_CZ) {
+            if (y & LOC_REG) form[y & 7] = 0;
+            if (z & LOC_REG) form[z & 7] = 0;
+        }
+        out.insert(out.end(), ops.begin() + i, ops.begin() + i + 4);
+    }
+    ops.swap(out);
+}
+
 void emit_pass(Program& P, PassPlan& pp, const std::vector<LGate>& G, bool backward,
                std::vector<int32_t>& ops, std::vector<Slot>& slots, int& nshared, int& nps,
                int& nexchanges) {
@@ -613,6 +693,7 @@ void emit_pass(Program& P, PassPlan& pp, const std::vector<LGate>& G, bool backw
         }
         nat.encode(d.end_map);
     }
+    materialize_before_exchanges(ops, d, d.op_begin, rb);
     d.op_count = (int)ops.size() / 4 - d.op_begin;
     (void)nshared;
     (void)nps;

@@ -10,7 +10,9 @@ the GPU against the oracle.
 """
 import numpy as np
 
-OP_MAP, OP_MAT, OP_DIAG, OP_CX, OP_CZ, OP_SWAP, OP_GRAD = 1, 2, 3, 4, 5, 6, 7
+OP_MAP, OP_MAT, OP_DIAG, OP_CX, OP_CZ, OP_SWAP, OP_GRAD, OP_XMAT = 1, 2, 3, 4, 5, 6, 7, 8
+# OP_XMAT applies a register's pending X, a representation detail of the
+# kernels: in the emulator's logical view it changes nothing
 LOC_REG = 0x100
 OPF_PER_SAMPLE, OPF_GRAD = 1, 2
 INIT_LOAD, INIT_ZERO, INIT_EMBED = 0, 1, 2
