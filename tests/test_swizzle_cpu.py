@@ -5,8 +5,10 @@ shared memory: local index j goes to slot j ^ L(j >> 5), L taking the bank
 images of the high bits (qandle_gb300/csrc/engine.h, swz_image).  A warp's
 access is conflict-free when its five lane bits have linearly independent
 bank images over GF(2).  These tests read the image table from the header,
-check that it leaves such a lane choice for almost every register set, and
-that the planner's exchanges on the benchmark circuits all pick one."""
+check that it leaves such a lane choice for almost every register set, that
+the planner's exchanges on the benchmark circuits all pick one, and that no
+lane-dependent pending X (folded into the write addresses) makes an
+exchange's writes conflict."""
 import itertools
 import os
 import re
@@ -64,3 +66,69 @@ def test_planned_exchanges_use_independent_lanes(name):
                 maps = [op for op in pd["ops"] if op[0] == 1]
                 for op in maps:
                     assert _rank([img[b] for b in _lanes(op[2])]) == 5, (name, backward)
+
+
+def _write_map_ranks(pd, rb, tb, img):
+    """Rank of each exchange's write lane -> bank map of a planned pass, with
+    the pending X of every register tracked through the ops as the global
+    bits it depends on (a CNOT controlled by a thread bit makes the target's
+    pending X depend on that bit; the exchange folds the pending X into its
+    write addresses)."""
+    OP_MAP, OP_CX, OP_CZ, OP_SWAP, OP_XMAT, LOC_REG = 1, 4, 5, 6, 8, 0x100
+    gbit = pd["gbit"]
+    if pd["init"] == 2:
+        y, z = pd["init_map"][0], pd["init_map"][1]
+    else:
+        y = sum((5 + k) << (4 * k) for k in range(rb))
+        z = 0x43210
+    reg = [(y >> (4 * k)) & 15 for k in range(rb)]
+    lane = _lanes(z)
+    form = [0] * rb
+    ranks = []
+    for op in pd["ops"]:
+        k, oy, oz, ow = (int(v) for v in op)
+        if k == OP_MAP:
+            vs = []
+            for j in range(5):
+                v = img[lane[j]]
+                if lane[j] < len(gbit):
+                    for r in range(rb):
+                        if (form[r] >> gbit[lane[j]]) & 1:
+                            v ^= img[reg[r]]
+                vs.append(v)
+            ranks.append(_rank(vs))
+            reg = [(oy >> (4 * q)) & 15 for q in range(rb)]
+            lane = _lanes(oz)
+            form = [0] * rb
+        elif k == OP_CX:
+            form[oy] ^= form[oz & 7] if oz & LOC_REG else (1 << oz)
+        elif k == OP_SWAP and oy != oz:
+            form[oy], form[oz] = form[oz], form[oy]
+        elif k == OP_CZ:
+            for loc in (oy, oz):
+                if loc & LOC_REG:
+                    form[loc & 7] = 0
+        elif k == OP_XMAT:
+            form[oy] = 0
+    return ranks
+
+
+@pytest.mark.parametrize("name", ["sel_reupload", "adjoint_brick", "deep_u"])
+def test_exchange_writes_stay_conflict_free_under_pending_x(name):
+    """The planner applies a lane-dependent pending X (OP_XMAT) before an
+    exchange whose write map it would make singular: every exchange of the
+    benchmark circuits, forward and backward, writes without bank
+    conflicts, and the headline forward needs OP_XMAT at all."""
+    desc = getattr(workloads, name)()
+    if name == "deep_u":
+        desc = workloads.deep_u(n=20, layers=10)
+    lo = engine.lower(workloads.build_circuit(desc).circuit)
+    img = _images()
+    prog = engine.Program(lo, "p0", keep_state=True, segments=2)
+    xmats = 0
+    for backward, rb, tb in ((False, 5, 13), (True, 4, 12)):
+        for pd in prog.passes(backward):
+            assert all(r == 5 for r in _write_map_ranks(pd, rb, tb, img)), (name, backward)
+            xmats += int(sum(1 for op in pd["ops"] if op[0] == 8))
+    if name == "sel_reupload":
+        assert xmats > 0
