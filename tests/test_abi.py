@@ -41,3 +41,14 @@ def test_version_and_error_reporting():
     assert b"state is null" in lib.qg_last_error()
     with pytest.raises(RuntimeError, match="out of range"):
         _lib.call("qg_apply_cz", 16, 1, 3, 0, 7, None)
+
+
+def test_job_entry_points_refuse_bad_arguments_on_the_host():
+    """The multi-job and compiled-job pass launches reject a null job list /
+    job and an out-of-range job count before any CUDA call."""
+    lib = _lib.load()
+    assert lib.qg_job_run_pass_compiled(None, None) == 1
+    assert b"job is null" in lib.qg_last_error()
+    assert lib.qg_jobs_run_pass(None, 33, None) == 1
+    assert lib.qg_jobs_run_pass(None, 1, None) == 1
+    assert lib.qg_jobs_run_pass(None, 0, None) == 0  # nothing to launch

@@ -137,3 +137,26 @@ def test_prepare_compiles_before_traffic(cuda_device):
         srv.close()
     assert srv.compiled_launches == prog.info.forward_passes
     assert np.abs(out.numpy() - oracle.forward(desc)).max() < 1e-5
+
+
+def test_compiled_job_launch_refuses_uncompiled_program(cuda_device):
+    """qg_job_run_pass_compiled launches nothing and returns QG_EINVAL for a
+    program whose pass kernels are not compiled on the device."""
+    import ctypes
+
+    from qandle_gb300 import _lib
+
+    rng = np.random.default_rng(6)
+    desc = workloads.random_sel_request(rng, n_range=(10, 10), depth_range=(2, 2), batch_max=2)
+    lo, params, named, _ = serve.lower_description(desc)
+    prog = serve.Program(lo, lo.measure, keep_state=False, tile_bits=13, low_bits=6)
+    assert not prog.compiled(cuda_device)
+    B = desc["batch"] or 1
+    ws = prog.workspace(B, False, cuda_device)
+    state = torch.zeros(B, 1 << lo.n, dtype=torch.complex64, device=cuda_device)
+    out = torch.zeros(B, lo.n, dtype=torch.float32, device=cuda_device)
+    job = _lib.Job(prog.handle, prog.table(cuda_device).data_ptr(), ws.data_ptr(), ws.numel(), state.data_ptr(), B,
+                   0, 0, out.data_ptr())
+    lib = _lib.load()
+    assert lib.qg_job_run_pass_compiled(ctypes.byref(job), _lib.stream()) == 1
+    assert b"not compiled" in lib.qg_last_error()
