@@ -246,7 +246,7 @@ def _random_mix(seed: int, n: int = 14, ngates: int = 160) -> dict:
 
 
 @pytest.mark.parametrize("seed", range(12))
-@pytest.mark.parametrize("oi", [0, 1, 2, 4])
+@pytest.mark.parametrize("oi", [0, 1, 2, 4, 8, 9])
 def test_held_diagonals_random_circuits_match_oracle(seed, oi):
     desc = _random_mix(seed)
     circ = workloads.build_circuit(desc, engine="fused")
@@ -257,7 +257,8 @@ def test_held_diagonals_random_circuits_match_oracle(seed, oi):
     assert np.abs(st - oracle.run(desc)).max() < 1e-10
 
 
-@pytest.mark.parametrize("opts", [dict(tile_bits=13, low_bits=6), dict(tile_bits=11, low_bits=4, max_high=2)])
+@pytest.mark.parametrize("opts", [dict(tile_bits=13, low_bits=6), dict(tile_bits=11, low_bits=4, max_high=2),
+                                  dict(tile_bits=13, low_bits=6, fwd_max_mats=5)])
 def test_random_circuits_plan_matches_reference(opts):
     """The reference's output states for 30 random circuits over every gate
     kind of the path (tests/golden/random_circuits.npz): the front-end
@@ -281,8 +282,8 @@ def test_random_circuits_plan_matches_reference(opts):
     assert ran >= 15
 
 
-@pytest.mark.parametrize("rb", [5, 4])
-def test_random_circuits_backward_plan_matches_reference_autograd(rb):
+@pytest.mark.parametrize("rb,cap", [(5, 0), (4, 0), (4, 3)])
+def test_random_circuits_backward_plan_matches_reference_autograd(rb, cap):
     """The adjoint plan, emulated, gives torch autograd's gradients through
     the reference (tests/golden/random_grads.npz: loss sum(W * joint
     probabilities)) for the random circuits of 5 qubits or more, with a
@@ -298,7 +299,8 @@ def test_random_circuits_backward_plan_matches_reference_autograd(rb):
         d = dict(desc, measure="probs")
         n, B = d["n"], d["batch"]
         lo = engine.lower(workloads.build_circuit(d).circuit)
-        prog = engine.Program(lo, "probs", keep_state=True, segments=2, tile_bits=13, low_bits=5, reg_bits=rb)
+        prog = engine.Program(lo, "probs", keep_state=True, segments=2, tile_bits=13, low_bits=5, reg_bits=rb,
+                              bwd_max_grad=cap)
         params, named, umats, embed = _runtime(lo, d, B)
         st, ck = emu.run_forward(prog, n, B, params, named, umats, state=psi.astype(complex), embed=embed)
         lam = z[f"{name}_w"].astype(np.float64) * st  # dL/dpsi* for L = sum(W |psi|^2)

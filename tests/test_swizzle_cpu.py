@@ -13,6 +13,7 @@ import itertools
 import os
 import re
 
+import numpy as np
 import pytest
 
 from qandle_gb300 import engine, workloads
@@ -132,3 +133,27 @@ def test_exchange_writes_stay_conflict_free_under_pending_x(name):
             xmats += int(sum(1 for op in pd["ops"] if op[0] == 8))
     if name == "sel_reupload":
         assert xmats > 0
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_circuit_exchange_writes_conflict_free(seed):
+    """Random circuits dense in CNOTs and CZs (many lane-controlled CNOTs,
+    hence lane-dependent pending X): every exchange write of their forward
+    and backward plans is conflict-free."""
+    rng = np.random.default_rng(100 + seed)
+    n = 16
+    gates = []
+    for _ in range(240):
+        r = rng.random()
+        if r < 0.5:
+            gates.append((("rx", "ry", "rz")[rng.integers(3)], int(rng.integers(n)), float(rng.uniform(-3, 3)), None))
+        else:
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            gates.append(("cnot", a, b) if r < 0.85 else ("cz", a, b))
+    desc = {"name": "mix", "n": n, "batch": 2, "gates": gates, "inputs": {}, "measure": "p0", "targets": None}
+    lo = engine.lower(workloads.build_circuit(desc).circuit)
+    img = _images()
+    prog = engine.Program(lo, "p0", keep_state=True, segments=2)
+    for backward, rb, tb in ((False, 5, 13), (True, 4, 12)):
+        for pd in prog.passes(backward):
+            assert all(r == 5 for r in _write_map_ranks(pd, rb, tb, img)), (seed, backward)
