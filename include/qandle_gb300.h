@@ -332,7 +332,8 @@ int qg_jobs_run_pass(const qg_job* jobs, int njobs, void* stream);
 /* Pass job->pass of one job as its own launch of the program's compiled pass
  * kernel (qg_program_compile) for the current device: the kernel
  * qg_program_forward runs for that pass.  Returns QG_EINVAL, launching
- * nothing, when that kernel is not compiled and loaded on this device. */
+ * nothing, when that kernel is not compiled and loaded on this device.  (No
+ * counterpart in the reference, which has no serving loop.) */
 int qg_job_run_pass_compiled(const qg_job* job, void* stream);
 
 int qg_program_finish(const qg_program* prog, const void* dev_table, void* workspace,
