@@ -373,6 +373,7 @@ struct Program {
     std::vector<unsigned char> table;
     int f_shared = 0, f_ps = 0, b_shared = 0, b_ps = 0;
     std::string stats;
+    std::string plan_error;  // set when a pass could not place its gates (the program is refused)
     void* jit = nullptr;  // compiled pass kernels (jit.cpp), owned by the program
 };
 
@@ -527,6 +528,12 @@ void emit_pass(Program& P, PassPlan& pp, const std::vector<LGate>& G, bool backw
             s.backward = backward;
             s.remap = local_remap;
             placed = s.run(pending, G);
+            if (placed.empty()) {
+                // the next gate needs bits that are not qubits of this tile:
+                // refuse the program rather than loop
+                P.plan_error = "a gate does not fit the pass's tile (tile_bits / low_bits leave too few strided qubits)";
+                return;
+            }
             uint32_t R = s.S;
             // fill to 5 register bits: prefer the natural registers, then low qubit bits
             for (int k = 0; k < rb && popc(R) < rb; ++k)
@@ -719,7 +726,9 @@ constexpr int kFwdMatsPerPass = 24;
 void plan_segment(Program& P, const std::vector<LGate>& G, std::vector<int> pending, int tb,
                   bool backward, std::vector<PassPlan>& out) {
     const int n = P.n;
-    const int L = std::min(P.opt.low_bits, std::min(n, tb));
+    // the low run leaves at least two strided slots, so that a two-qubit gate
+    // between two strided qubits fits a tile
+    const int L = n > tb ? std::min(P.opt.low_bits, tb - 2) : std::min(P.opt.low_bits, std::min(n, tb));
     const int kmax = P.opt.max_high > 0 ? std::min(P.opt.max_high, tb - L) : tb - L;
     while (!pending.empty()) {
         Selector s;
@@ -1181,6 +1190,7 @@ int qg_program_create(const qg_gate* gates, int ngates, const int32_t* qlist, in
     for (int s = 1; s <= P->nsegments; ++s) P->seg_end.push_back((int)((int64_t)G * s / P->nsegments));
     qg::plan_forward(*P);
     qg::plan_backward(*P);
+    if (!P->plan_error.empty()) return qg::set_error("qg_program_create: " + P->plan_error), QG_EINVAL;
     qg::layout_tables(*P);
     *out = reinterpret_cast<qg_program*>(P.release());
     return QG_OK;

@@ -313,3 +313,29 @@ def test_random_circuits_backward_plan_matches_reference_autograd(rb, cap):
             assert np.abs(v - z[f"{name}_dnamed_{nm}"]).max() < 1e-5, (name, nm)
         ran += 1
     assert ran >= 5
+
+
+@pytest.mark.timeout(120)
+@pytest.mark.parametrize("training", [False, True])
+def test_long_low_run_leaves_room_for_two_qubit_gates(training):
+    """With low_bits = tile_bits - 1 a two-qubit gate between two strided
+    qubits does not fit a tile of one strided slot.  The planner keeps at
+    least two strided slots (the forward and the narrower backward tiles),
+    so such options plan in bounded time and give the oracle's state (this
+    case used to loop in the planner)."""
+    rng = np.random.default_rng(11)
+    n = 14
+    gates = []
+    for _ in range(40):
+        if rng.random() < 0.5:
+            gates.append((("rx", "ry", "rz")[rng.integers(3)], int(rng.integers(n)), float(rng.uniform(-3, 3)), None))
+        else:
+            a, b = (int(x) for x in rng.choice(3, 2, replace=False))  # qubits 0..2: the strided bits
+            gates.append(("cnot", a, b))
+    desc = {"name": "mix", "n": n, "batch": 2, "gates": gates, "inputs": {}, "measure": "state", "targets": None}
+    lo = engine.lower(workloads.build_circuit(desc, engine="fused").circuit)
+    prog = engine.Program(lo, "state", keep_state=training, segments=2 if training else 1,
+                          tile_bits=12, low_bits=11, max_high=1)
+    params, named, umats, embed = _runtime(lo, desc, 2)
+    st, _ = emu.run_forward(prog, n, 2, params, named, umats, embed=embed)
+    assert np.abs(st - oracle.run(desc)).max() < 1e-10
