@@ -339,3 +339,26 @@ def test_long_low_run_leaves_room_for_two_qubit_gates(training):
     params, named, umats, embed = _runtime(lo, desc, 2)
     st, _ = emu.run_forward(prog, n, 2, params, named, umats, embed=embed)
     assert np.abs(st - oracle.run(desc)).max() < 1e-10
+
+
+def test_executor_picks_uncapped_plan_for_calls_that_do_not_fill_the_gpu(monkeypatch):
+    """FusedExecutor.program(training, batch, device): with the default pass
+    length, a call whose passes have fewer tiles than the device has SMs
+    gets the uncapped plan (one pass for this 13-qubit circuit), a larger
+    call the capped plan; without a batch, the plan the last call used.  An
+    explicit fwd_max_mats is always kept."""
+    import torch
+
+    monkeypatch.setattr(engine, "_sm_count", lambda dev: 152)
+    desc = workloads.sel_reupload(n=13, batch=2, layers=12, reupload_every=4)
+    circ = workloads.build_circuit(desc, engine="fused")
+    ex = engine.FusedExecutor(circ.circuit)
+    dev = torch.device("cuda", 0)
+    small = ex.program(False, 4, dev)        # 4 tiles
+    assert small.info.forward_passes == 1
+    assert ex.program(False) is small        # the last call's plan
+    large = ex.program(False, 304, dev)      # 304 tiles
+    assert large.info.forward_passes > 1
+    assert ex.program(False) is large
+    fixed = engine.FusedExecutor(circ.circuit, fwd_max_mats=10)
+    assert fixed.program(False, 4, dev).info.forward_passes > 1
