@@ -56,3 +56,24 @@ def test_compile_reports_errors_through_status():
     lib = _lib.load()
     assert lib.qg_program_compile(None, 1) == 1  # QG_EINVAL
     assert b"null" in lib.qg_last_error()
+
+
+def test_pending_x_ops_compile_forward_and_backward():
+    """OP_XMAT (a register's pending X applied before an exchange whose
+    writes it would bank-conflict) unrolls into jmaterialize in the forward
+    and jmaterialize2 (psi and lambda) in the backward, and both build."""
+    desc = workloads.adjoint_brick(n=15, batch=1, layers=6)
+    desc["measure"] = "p0"
+    lo = engine.lower(workloads.build_circuit(desc, engine="plain").circuit)
+    prog = engine.Program(lo, "p0", keep_state=True, segments=2)
+    fwd = [p for p, pd in enumerate(prog.passes()) if (pd["ops"][:, 0] == 8).any()]
+    bwd = [p for p, pd in enumerate(prog.passes(True)) if (pd["ops"][:, 0] == 8).any()]
+    assert fwd and bwd
+    assert "jmaterialize<" in prog.pass_source(fwd[0])
+    assert "jmaterialize2<" in prog.pass_source(bwd[0], backward=True)
+    try:
+        prog.compile(load=False, backward=True)
+    except RuntimeError as e:
+        if "libnvrtc" in str(e):
+            pytest.skip("NVRTC is not installed")
+        raise
